@@ -1,0 +1,591 @@
+/*
+ * CPU oracle: restatement of the reference's persistent graph kernels and
+ * non-persistent tasks.  TEST INFRASTRUCTURE ONLY (see wgm_oracle.h).
+ *
+ * Each inter-barrier phase of a reference kernel becomes a sequential loop
+ * over vertices.  The comment above each loop states why the phase's result
+ * does not depend on the order in which the GPU's work-items ran it, which is
+ * what makes a sequential restatement a valid oracle for a racy parallel
+ * kernel.
+ */
+#include "wgm_oracle.h"
+
+#include <float.h>
+#include <limits.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+int oracle_omp_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+/* Vertex degree as the Lonestar kernel computes it: psrc[nn+1]-psrc[nn]
+ * (bfs.cl:165).  With the loader quirk an isolated last vertex yields -1; the
+ * kernel's gather loop then runs zero times for that vertex, so it is 0 here. */
+static inline int32_t lonestar_degree(const int32_t *row_ptr, int32_t v) {
+  int32_t d = row_ptr[v + 1] - row_ptr[v];
+  return d < 0 ? 0 : d;
+}
+
+void oracle_lonestar_csr_from_gr(int64_t V, int64_t E, const uint64_t *out_idx,
+                                 const uint32_t *outs, int32_t *row_ptr,
+                                 int32_t *col) {
+  /* bfs.h:41-43: psrc[nnodes] = nedges; edgessrcdst is 1-based.
+   * bfs.h:141-148: psrc[0] = 1, psrc[ii] = outIdx[ii-1] + 1.
+   * bfs.h:149-157: edgessrcdst[psrc[ii]+jj] = outs[psrc[ii]+jj-1] for
+   * jj < outIdx[ii]-outIdx[ii-1].  In 0-based form the kernel sees
+   * row_ptr[ii] = psrc[ii]-1 and col[k] = outs[k]; row_ptr[V] = E-1. */
+  for (int64_t i = 0; i < V; i++)
+    row_ptr[i] = (i == 0) ? 0 : (int32_t)out_idx[i - 1];
+  row_ptr[V] = (int32_t)(E - 1);
+  for (int64_t k = 0; k < E; k++) col[k] = (int32_t)outs[k];
+}
+
+/* ------------------------------------------------------------------------ */
+/* Lonestar BFS: lonestar/graph_apps/bfs/device/bfs.cl                       */
+/* ------------------------------------------------------------------------ */
+
+int oracle_lonestar_bfs(int32_t V, const int32_t *row_ptr, const int32_t *col,
+                        int32_t source, uint32_t *dist) {
+  /* bfs.h:250-262: dist = MYINFINITY everywhere, then dist[source] = 0. */
+  for (int32_t i = 0; i < V; i++) dist[i] = ORACLE_LONESTAR_INF;
+  if (V <= 0) return 0;
+  dist[source] = 0;
+  int32_t *in_wl = (int32_t *)malloc(sizeof(int32_t) * (size_t)(V + 1));
+  int32_t *out_wl = (int32_t *)malloc(sizeof(int32_t) * (size_t)(V + 1));
+  /* bfs.cl:235-241: iteration 0 pushes the source only. */
+  int32_t in_n = 1;
+  in_wl[0] = source;
+  int iteration = 1;
+  /* bfs.cl:278-300: while(1) { drelax; barrier; swap; iteration++; barrier;
+   * if (*in_index <= 0) break; }.  Phase order independence: a vertex is
+   * written only when its dist is MYINFINITY and always with the value
+   * `iteration`, so every interleaving of the unsynchronised writes at
+   * bfs.cl:121-123 stores the same value; duplicates in the worklist change
+   * nothing but the worklist length. */
+  while (in_n > 0) {
+    int32_t out_n = 0;
+    for (int32_t k = 0; k < in_n; k++) {
+      int32_t nn = in_wl[k];
+      int32_t start = row_ptr[nn], deg = lonestar_degree(row_ptr, nn);
+      for (int32_t j = 0; j < deg; j++) {
+        uint32_t dst = (uint32_t)col[start + j];
+        if (dst >= (uint32_t)V) continue; /* bfs.cl:116 */
+        if (dist[dst] == ORACLE_LONESTAR_INF) {
+          dist[dst] = (uint32_t)iteration; /* bfs.cl:121-123 */
+          out_wl[out_n++] = (int32_t)dst;
+        }
+      }
+    }
+    int32_t *t = in_wl;
+    in_wl = out_wl;
+    out_wl = t;
+    in_n = out_n;
+    iteration++;
+  }
+  free(in_wl);
+  free(out_wl);
+  return iteration;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Lonestar SSSP: lonestar/graph_apps/sssp/device/sssp.cl                    */
+/* ------------------------------------------------------------------------ */
+
+int oracle_lonestar_sssp(int32_t V, const int32_t *row_ptr, const int32_t *col,
+                         const uint32_t *wt, int32_t source, uint32_t *dist) {
+  for (int32_t i = 0; i < V; i++) dist[i] = ORACLE_LONESTAR_INF;
+  if (V <= 0) return 0;
+  dist[source] = 0;
+  int32_t *in_wl = (int32_t *)malloc(sizeof(int32_t) * (size_t)(V + 1));
+  int32_t *out_wl = (int32_t *)malloc(sizeof(int32_t) * (size_t)(V + 1));
+  uint8_t *queued = (uint8_t *)calloc((size_t)V, 1);
+  int32_t in_n = 1;
+  in_wl[0] = source;
+  int iteration = 1;
+  /* sssp.cl:104-133: altdist = dist[src] + wt; if (altdist < dist[dst])
+   * { atomic_min(&dist[dst], altdist); push dst }.  Every decrease of a
+   * vertex's distance pushes it, so the loop ends at the fixpoint of the
+   * relaxation, which is the unique shortest-path distance vector whatever
+   * the order of relaxations.  A vertex queued twice in one round is
+   * processed once here: its second visit would relax the same edges with
+   * the same distance, a no-op. */
+  while (in_n > 0) {
+    int32_t out_n = 0;
+    for (int32_t k = 0; k < in_n; k++) {
+      int32_t nn = in_wl[k];
+      int32_t start = row_ptr[nn], deg = lonestar_degree(row_ptr, nn);
+      for (int32_t j = 0; j < deg; j++) {
+        uint32_t dst = (uint32_t)col[start + j];
+        if (dst >= (uint32_t)V) continue;           /* sssp.cl:117 */
+        uint32_t w = wt[start + j];
+        if (w >= ORACLE_LONESTAR_INF) continue;     /* sssp.cl:120 */
+        uint32_t alt = dist[nn] + w;                /* sssp.cl:123 */
+        if (alt < dist[dst]) {                      /* sssp.cl:126-129 */
+          dist[dst] = alt;
+          if (!queued[dst]) {
+            queued[dst] = 1;
+            out_wl[out_n++] = (int32_t)dst;
+          }
+        }
+      }
+    }
+    for (int32_t k = 0; k < out_n; k++) queued[out_wl[k]] = 0;
+    int32_t *t = in_wl;
+    in_wl = out_wl;
+    out_wl = t;
+    in_n = out_n;
+    iteration++;
+  }
+  free(in_wl);
+  free(out_wl);
+  free(queued);
+  return iteration;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Pannotia colour: pannotia/graph_apps/color/device/color.cl:3-97           */
+/* ------------------------------------------------------------------------ */
+
+int oracle_pannotia_color(int32_t V, const int32_t *row_ptr,
+                          const int32_t *col, const float *node_value,
+                          int32_t *color) {
+  int32_t num_edges = row_ptr[V];
+  float *max_d = (float *)malloc(sizeof(float) * (size_t)(V > 0 ? V : 1));
+  for (int32_t i = 0; i < V; i++) color[i] = -1; /* color.h:50 */
+  int graph_color = 1;
+  int stop[2] = {0, 0}; /* stop1, stop2 (color.h:73-76) */
+  int w = 0;            /* write_stop = stop1, read_stop = stop2 */
+  for (;;) {
+    /* Phase color1 (color.cl:27-55).  Reads color[] (not written in this
+     * phase) and writes max_d[i] for the vertex's own i: order independent.
+     * `start != end - 1` (color.cl:46) skips every neighbour of a degree-1
+     * vertex. */
+    for (int32_t i = 0; i < V; i++) {
+      if (color[i] != -1) continue;
+      int32_t start = row_ptr[i];
+      int32_t end = (i + 1 < V) ? row_ptr[i + 1] : num_edges;
+      float maximum = -1;
+      for (int32_t e = start; e < end; e++) {
+        if (color[col[e]] == -1 && start != end - 1) {
+          stop[w] = 1;
+          if (node_value[col[e]] > maximum) maximum = node_value[col[e]];
+        }
+      }
+      max_d[i] = maximum;
+    }
+    int r = w; /* swap: read_stop = the flag just written (color.cl:59-61) */
+    w = 1 - w;
+    /* Phase color2 (color.cl:74-83): each i writes only color[i]. */
+    for (int32_t i = 0; i < V; i++)
+      if (color[i] == -1 && node_value[i] > max_d[i]) color[i] = graph_color;
+    if (stop[r] == 0) break; /* color.cl:85-87 */
+    graph_color++;
+    stop[w] = 0; /* color.cl:90 */
+  }
+  free(max_d);
+  return graph_color;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Pannotia MIS: pannotia/graph_apps/mis/device/mis.cl:5-125                 */
+/* ------------------------------------------------------------------------ */
+
+#define MIS_BIGNUM 99999999 /* mis.cl:1 */
+
+int oracle_pannotia_mis(int32_t V, const int32_t *row_ptr, const int32_t *col,
+                        const float *node_value, int32_t *s_array) {
+  int32_t num_edges = row_ptr[V];
+  size_t n = (size_t)(V > 0 ? V : 1);
+  int32_t *c = (int32_t *)malloc(sizeof(int32_t) * n);
+  int32_t *cu = (int32_t *)malloc(sizeof(int32_t) * n);
+  float *min_array = (float *)malloc(sizeof(float) * n);
+  /* mis.h:58-92: s = 0, c = cu = -1, min_array = 6666666.0, stop = 0. */
+  for (int32_t i = 0; i < V; i++) {
+    s_array[i] = 0;
+    c[i] = -1;
+    cu[i] = -1;
+    min_array[i] = 6666666.0f;
+  }
+  int stop = 0, rounds = 0;
+  for (;;) {
+    rounds++;
+    /* mis1 (mis.cl:29-53): reads c[] (unchanged in this phase), writes
+     * min_array[tid] only: order independent. */
+    for (int32_t t = 0; t < V; t++) {
+      if (c[t] != -1) continue;
+      stop = 1;
+      int32_t start = row_ptr[t];
+      int32_t end = (t + 1 < V) ? row_ptr[t + 1] : num_edges;
+      float mn = (float)MIS_BIGNUM;
+      for (int32_t e = start; e < end; e++)
+        if (c[col[e]] == -1 && node_value[col[e]] < mn) mn = node_value[col[e]];
+      min_array[t] = mn;
+    }
+    int local_stop = stop; /* mis.cl:59 */
+    /* mis2 (mis.cl:66-96).  A vertex joins when its value is below the
+     * minimum over its active neighbours; two adjacent active vertices can
+     * never both satisfy that, so the c[] writes of joiners never change the
+     * c[col] tests another joiner makes (the neighbours it tests are never
+     * joiners).  cu[] is only written, with one value.  Order independent. */
+    for (int32_t t = 0; t < V; t++) {
+      if (node_value[t] < min_array[t] && c[t] == -1) {
+        s_array[t] = 2;
+        int32_t start = row_ptr[t];
+        int32_t end = (t + 1 < V) ? row_ptr[t + 1] : num_edges;
+        c[t] = -2;
+        for (int32_t e = start; e < end; e++)
+          if (c[col[e]] == -1) cu[col[e]] = -2;
+      }
+    }
+    if (local_stop == 0) break; /* mis.cl:106-108 */
+    stop = 0;                   /* mis.cl:109 */
+    /* mis3 (mis.cl:114-118): own-index writes. */
+    for (int32_t t = 0; t < V; t++)
+      if (cu[t] == -2) c[t] = cu[t];
+  }
+  free(c);
+  free(cu);
+  free(min_array);
+  return rounds;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Pannotia SSSP: pannotia/graph_apps/sssp/device/sssp.cl:10-88              */
+/* ------------------------------------------------------------------------ */
+
+int oracle_pannotia_sssp(int32_t V, const int32_t *row_ptr, const int32_t *col,
+                         const int32_t *data, int32_t source, int32_t *cost) {
+  size_t n = (size_t)(V > 0 ? V : 1);
+  int32_t *y = (int32_t *)malloc(sizeof(int32_t) * n);
+  /* sssp.h:58-66: x = y = BIG_NUM except the source. */
+  for (int32_t i = 0; i < V; i++)
+    cost[i] = y[i] = (i == source) ? 0 : ORACLE_PANNOTIA_BIG;
+  int rounds = 0;
+  for (;;) {
+    rounds++;
+    /* vector_assign (sssp.cl:31-33) */
+    for (int32_t i = 0; i < V; i++) cost[i] = y[i];
+    /* spmv_min_dot_plus (sssp.cl:51-64): reads x, writes y[own]: a Jacobi
+     * step, order independent. */
+    for (int32_t it = 0; it < V; it++) {
+      int32_t mn = cost[it];
+      for (int32_t j = row_ptr[it]; j < row_ptr[it + 1]; j++)
+        if (data[j] + cost[col[j]] < mn) mn = data[j] + cost[col[j]];
+      y[it] = mn;
+    }
+    /* vector_diff (sssp.cl:77-80) and the exit test (sssp.cl:88-90) */
+    int stop = 0;
+    for (int32_t i = 0; i < V; i++)
+      if (y[i] != cost[i]) stop = 1;
+    if (!stop) break;
+  }
+  free(y);
+  return rounds;
+}
+
+/* ------------------------------------------------------------------------ */
+/* PageRank (no reference implementation)                                    */
+/* ------------------------------------------------------------------------ */
+
+void oracle_pagerank_f64(int32_t V, const int32_t *row_ptr, const int32_t *col,
+                         double damping, int iterations, double *pr) {
+  size_t n = (size_t)(V > 0 ? V : 1);
+  double *contrib = (double *)malloc(sizeof(double) * n);
+  double *next = (double *)malloc(sizeof(double) * n);
+  for (int32_t i = 0; i < V; i++) pr[i] = 1.0 / (double)V;
+  for (int it = 0; it < iterations; it++) {
+    double dangling = 0.0;
+    for (int32_t u = 0; u < V; u++) {
+      int32_t d = row_ptr[u + 1] - row_ptr[u];
+      if (d > 0) {
+        contrib[u] = pr[u] / (double)d;
+      } else {
+        contrib[u] = 0.0;
+        dangling += pr[u];
+      }
+    }
+    double base = (1.0 - damping) / (double)V + damping * dangling / (double)V;
+    for (int32_t v = 0; v < V; v++) {
+      double s = 0.0;
+      for (int32_t j = row_ptr[v]; j < row_ptr[v + 1]; j++) s += contrib[col[j]];
+      next[v] = base + damping * s;
+    }
+    memcpy(pr, next, sizeof(double) * (size_t)V);
+  }
+  free(contrib);
+  free(next);
+}
+
+void oracle_pagerank_f32_omp(int32_t V, const int32_t *row_ptr,
+                             const int32_t *col, float damping, int iterations,
+                             float *pr, float *scratch) {
+  float *contrib = scratch;
+  float *next = scratch + V;
+  for (int32_t i = 0; i < V; i++) pr[i] = 1.0f / (float)V;
+  for (int it = 0; it < iterations; it++) {
+    double dangling = 0.0;
+#pragma omp parallel for reduction(+ : dangling) schedule(static)
+    for (int32_t u = 0; u < V; u++) {
+      int32_t d = row_ptr[u + 1] - row_ptr[u];
+      if (d > 0) {
+        contrib[u] = pr[u] / (float)d;
+      } else {
+        contrib[u] = 0.0f;
+        dangling += pr[u];
+      }
+    }
+    float base = (1.0f - damping) / (float)V + damping * (float)dangling / (float)V;
+#pragma omp parallel for schedule(dynamic, 1024)
+    for (int32_t v = 0; v < V; v++) {
+      float s = 0.0f;
+      for (int32_t j = row_ptr[v]; j < row_ptr[v + 1]; j++) s += contrib[col[j]];
+      next[v] = base + damping * s;
+    }
+    memcpy(pr, next, sizeof(float) * (size_t)V);
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* OpenMP variants (timed CPU baseline); same phase structure                */
+/* ------------------------------------------------------------------------ */
+
+int oracle_lonestar_bfs_omp(int32_t V, const int32_t *row_ptr,
+                            const int32_t *col, int32_t source, uint32_t *dist,
+                            int32_t *scratch) {
+#pragma omp parallel for schedule(static)
+  for (int32_t i = 0; i < V; i++) dist[i] = ORACLE_LONESTAR_INF;
+  if (V <= 0) return 0;
+  dist[source] = 0;
+  int32_t *in_wl = scratch, *out_wl = scratch + V;
+  int32_t in_n = 1, out_n = 0;
+  in_wl[0] = source;
+  int iteration = 1;
+  while (in_n > 0) {
+    out_n = 0;
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int32_t k = 0; k < in_n; k++) {
+      int32_t nn = in_wl[k];
+      int32_t start = row_ptr[nn], deg = lonestar_degree(row_ptr, nn);
+      for (int32_t j = 0; j < deg; j++) {
+        uint32_t dst = (uint32_t)col[start + j];
+        if (dst >= (uint32_t)V) continue;
+        uint32_t expect = ORACLE_LONESTAR_INF;
+        if (__atomic_load_n(&dist[dst], __ATOMIC_RELAXED) == expect &&
+            __atomic_compare_exchange_n(&dist[dst], &expect, (uint32_t)iteration,
+                                        0, __ATOMIC_RELAXED, __ATOMIC_RELAXED)) {
+          int32_t slot = __atomic_fetch_add(&out_n, 1, __ATOMIC_RELAXED);
+          out_wl[slot] = (int32_t)dst;
+        }
+      }
+    }
+    int32_t *t = in_wl;
+    in_wl = out_wl;
+    out_wl = t;
+    in_n = out_n;
+    iteration++;
+  }
+  return iteration;
+}
+
+int oracle_lonestar_sssp_omp(int32_t V, const int32_t *row_ptr,
+                             const int32_t *col, const uint32_t *wt,
+                             int32_t source, uint32_t *dist, int32_t *scratch) {
+  int32_t *in_wl = scratch, *out_wl = scratch + V, *stamp = scratch + 2 * (size_t)V;
+#pragma omp parallel for schedule(static)
+  for (int32_t i = 0; i < V; i++) {
+    dist[i] = ORACLE_LONESTAR_INF;
+    stamp[i] = 0;
+  }
+  if (V <= 0) return 0;
+  dist[source] = 0;
+  int32_t in_n = 1, out_n = 0;
+  in_wl[0] = source;
+  int iteration = 1;
+  while (in_n > 0) {
+    out_n = 0;
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int32_t k = 0; k < in_n; k++) {
+      int32_t nn = in_wl[k];
+      int32_t start = row_ptr[nn], deg = lonestar_degree(row_ptr, nn);
+      uint32_t dsrc = __atomic_load_n(&dist[nn], __ATOMIC_RELAXED);
+      for (int32_t j = 0; j < deg; j++) {
+        uint32_t dst = (uint32_t)col[start + j];
+        if (dst >= (uint32_t)V) continue;
+        uint32_t w = wt[start + j];
+        if (w >= ORACLE_LONESTAR_INF) continue;
+        uint32_t alt = dsrc + w;
+        uint32_t cur = __atomic_load_n(&dist[dst], __ATOMIC_RELAXED);
+        int lowered = 0;
+        while (alt < cur) {
+          if (__atomic_compare_exchange_n(&dist[dst], &cur, alt, 1,
+                                          __ATOMIC_RELAXED, __ATOMIC_RELAXED)) {
+            lowered = 1;
+            break;
+          }
+        }
+        if (lowered &&
+            __atomic_exchange_n(&stamp[dst], iteration, __ATOMIC_RELAXED) != iteration) {
+          int32_t slot = __atomic_fetch_add(&out_n, 1, __ATOMIC_RELAXED);
+          out_wl[slot] = (int32_t)dst;
+        }
+      }
+    }
+    int32_t *t = in_wl;
+    in_wl = out_wl;
+    out_wl = t;
+    in_n = out_n;
+    iteration++;
+  }
+  return iteration;
+}
+
+int oracle_pannotia_color_omp(int32_t V, const int32_t *row_ptr,
+                              const int32_t *col, const float *node_value,
+                              int32_t *color, float *max_d) {
+  int32_t num_edges = row_ptr[V];
+#pragma omp parallel for schedule(static)
+  for (int32_t i = 0; i < V; i++) color[i] = -1;
+  int graph_color = 1;
+  for (;;) {
+    int stop = 0;
+#pragma omp parallel for schedule(dynamic, 256) reduction(| : stop)
+    for (int32_t i = 0; i < V; i++) {
+      if (color[i] != -1) continue;
+      int32_t start = row_ptr[i];
+      int32_t end = (i + 1 < V) ? row_ptr[i + 1] : num_edges;
+      float maximum = -1;
+      for (int32_t e = start; e < end; e++) {
+        if (color[col[e]] == -1 && start != end - 1) {
+          stop = 1;
+          if (node_value[col[e]] > maximum) maximum = node_value[col[e]];
+        }
+      }
+      max_d[i] = maximum;
+    }
+#pragma omp parallel for schedule(static)
+    for (int32_t i = 0; i < V; i++)
+      if (color[i] == -1 && node_value[i] > max_d[i]) color[i] = graph_color;
+    if (!stop) break;
+    graph_color++;
+  }
+  return graph_color;
+}
+
+int oracle_pannotia_mis_omp(int32_t V, const int32_t *row_ptr,
+                            const int32_t *col, const float *node_value,
+                            int32_t *s_array, int32_t *scratch,
+                            float *min_array) {
+  int32_t num_edges = row_ptr[V];
+  int32_t *c = scratch, *cu = scratch + V;
+#pragma omp parallel for schedule(static)
+  for (int32_t i = 0; i < V; i++) {
+    s_array[i] = 0;
+    c[i] = -1;
+    cu[i] = -1;
+    min_array[i] = 6666666.0f;
+  }
+  int rounds = 0;
+  for (;;) {
+    rounds++;
+    int stop = 0;
+#pragma omp parallel for schedule(dynamic, 256) reduction(| : stop)
+    for (int32_t t = 0; t < V; t++) {
+      if (c[t] != -1) continue;
+      stop = 1;
+      int32_t start = row_ptr[t];
+      int32_t end = (t + 1 < V) ? row_ptr[t + 1] : num_edges;
+      float mn = (float)MIS_BIGNUM;
+      for (int32_t e = start; e < end; e++)
+        if (c[col[e]] == -1 && node_value[col[e]] < mn) mn = node_value[col[e]];
+      min_array[t] = mn;
+    }
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int32_t t = 0; t < V; t++) {
+      if (node_value[t] < min_array[t] && c[t] == -1) {
+        s_array[t] = 2;
+        int32_t start = row_ptr[t];
+        int32_t end = (t + 1 < V) ? row_ptr[t + 1] : num_edges;
+        __atomic_store_n(&c[t], -2, __ATOMIC_RELAXED);
+        for (int32_t e = start; e < end; e++)
+          if (__atomic_load_n(&c[col[e]], __ATOMIC_RELAXED) == -1)
+            __atomic_store_n(&cu[col[e]], -2, __ATOMIC_RELAXED);
+      }
+    }
+    if (!stop) break;
+#pragma omp parallel for schedule(static)
+    for (int32_t t = 0; t < V; t++)
+      if (cu[t] == -2) c[t] = cu[t];
+  }
+  return rounds;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Non-persistent tasks                                                      */
+/* ------------------------------------------------------------------------ */
+
+int32_t oracle_matmult_rand_fill(int32_t *M, int32_t rows, int32_t cols,
+                                 int32_t seed) {
+  /* matmult.h:107-119: middle-square; `seed * seed` wraps as 32-bit. */
+  for (int32_t r = 0; r < rows; r++) {
+    for (int32_t c = 0; c < cols; c++) {
+      seed = (int32_t)((uint32_t)seed * (uint32_t)seed);
+      seed = (seed / 1000) % 1000000;
+      M[(int64_t)r * cols + c] = seed % 10;
+    }
+  }
+  return seed;
+}
+
+void oracle_matmult_i32(const int32_t *A, int32_t A_row, int32_t A_col,
+                        const int32_t *B, int32_t B_col, int32_t *C) {
+  /* matmult.cl:48-56 (row-major, wrapping int32 accumulation). */
+  for (int32_t r = 0; r < A_row; r++)
+    for (int32_t c = 0; c < B_col; c++) {
+      uint32_t acc = 0;
+      for (int32_t j = 0; j < A_col; j++)
+        acc += (uint32_t)A[(int64_t)r * A_col + j] * (uint32_t)B[(int64_t)j * B_col + c];
+      C[(int64_t)r * B_col + c] = (int32_t)acc;
+    }
+}
+
+int32_t oracle_hash_diag(const int32_t *M, int32_t rows, int32_t cols) {
+  /* matmult.cl:9-22: djb2 over the diagonal, wrapping int32. */
+  uint32_t h = 5381;
+  for (int32_t i = 0; i < rows && i < cols; i++)
+    h = h * 33u + (uint32_t)M[(int64_t)i * cols + i];
+  return (int32_t)h;
+}
+
+int32_t oracle_reduce_min_i32(const int32_t *buf, int64_t n) {
+  int32_t m = INT_MAX; /* reduce.cl:291: INT_MAX is the identity */
+  for (int64_t i = 0; i < n; i++)
+    if (buf[i] < m) m = buf[i];
+  return m;
+}
+
+void oracle_matmult_f32(const float *A, int32_t M, int32_t K, const float *B,
+                        int32_t N, float *C) {
+  for (int32_t r = 0; r < M; r++)
+    for (int32_t c = 0; c < N; c++) {
+      double acc = 0.0;
+      for (int32_t j = 0; j < K; j++)
+        acc += (double)A[(int64_t)r * K + j] * (double)B[(int64_t)j * N + c];
+      C[(int64_t)r * N + c] = (float)acc;
+    }
+}
+
+float oracle_reduce_min_f32(const float *buf, int64_t n) {
+  float m = FLT_MAX;
+  for (int64_t i = 0; i < n; i++)
+    if (buf[i] < m) m = buf[i];
+  return m;
+}

@@ -1,0 +1,114 @@
+/*
+ * CPU oracle for the persistent graph kernels and the non-persistent tasks.
+ *
+ * TEST INFRASTRUCTURE ONLY.  Nothing in the product library links or calls this
+ * code; only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline and
+ * reference arms load it, and only as the checker or the timed CPU baseline.
+ *
+ * Every function restates one reference algorithm phase by phase and cites the
+ * reference file:line it follows (paths relative to the reference project).
+ * The restatement is pinned by tests against the reference's own OpenCL kernel
+ * source compiled as C++ under a one-work-group shim (oracle/ref_shim), since
+ * the reference ships no golden vectors.
+ *
+ * Graph layout everywhere: 0-based CSR, row_ptr[V+1], col[row_ptr[V]].
+ * Callers that want the Lonestar loader's behaviour pass the CSR produced by
+ * oracle_lonestar_csr_from_gr (the last edge of vertex V-1 is dropped).
+ */
+#ifndef WGM_ORACLE_H
+#define WGM_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ORACLE_LONESTAR_INF 1000000000u /* lonestar/graph_apps/bfs/device/bfs.cl:33 */
+#define ORACLE_PANNOTIA_BIG 99999999    /* pannotia/graph_apps/sssp/sssp.h:3 */
+
+/* Lonestar `.gr` loader semantics (lonestar/graph_apps/bfs/bfs.h:40-46,137-161).
+ * out_idx[i] is the Galois cumulative end index of vertex i; outs[] the
+ * destinations.  Writes the 0-based CSR the device kernel actually walks:
+ * row_ptr[i] = psrc[i]-1 for i<V and row_ptr[V] = nedges-1. */
+void oracle_lonestar_csr_from_gr(int64_t V, int64_t E, const uint64_t *out_idx,
+                                 const uint32_t *outs, int32_t *row_ptr,
+                                 int32_t *col);
+
+/* Lonestar BFS drelax2 (bfs.cl:104-302).  Returns the number of worklist
+ * iterations the persistent loop ran (iteration 0 seeds the source). */
+int oracle_lonestar_bfs(int32_t V, const int32_t *row_ptr, const int32_t *col,
+                        int32_t source, uint32_t *dist);
+
+/* Lonestar SSSP drelax2 (sssp.cl:104-318): worklist Bellman-Ford with
+ * atomic_min relaxations.  Returns the iteration count. */
+int oracle_lonestar_sssp(int32_t V, const int32_t *row_ptr, const int32_t *col,
+                         const uint32_t *wt, int32_t source, uint32_t *dist);
+
+/* Pannotia color_combined (pannotia/graph_apps/color/device/color.cl:3-97).
+ * color[] is written in full (initialised to -1 as color.h:50 does).
+ * Returns the number of rounds (the final graph_color). */
+int oracle_pannotia_color(int32_t V, const int32_t *row_ptr,
+                          const int32_t *col, const float *node_value,
+                          int32_t *color);
+
+/* Pannotia mis_combined (pannotia/graph_apps/mis/device/mis.cl:5-125).
+ * s_array[] gets 2 for members and 0 otherwise (mis.h:60-63). Returns rounds. */
+int oracle_pannotia_mis(int32_t V, const int32_t *row_ptr, const int32_t *col,
+                        const float *node_value, int32_t *s_array);
+
+/* Pannotia sssp_combined (pannotia/graph_apps/sssp/device/sssp.cl:10-88):
+ * Jacobi min-plus iteration to a fixpoint. cost[] is the x vector the host
+ * reads back (sssp.h:166-170). Returns rounds. */
+int oracle_pannotia_sssp(int32_t V, const int32_t *row_ptr, const int32_t *col,
+                         const int32_t *data, int32_t source, int32_t *cost);
+
+/* PageRank has no reference implementation.  FP64 pull PageRank written from
+ * the definition: pr0 = 1/V; pr' = (1-d)/V + d*(sum_{u->v} pr[u]/deg(u) +
+ * dangling/V), dangling = sum of pr over zero-degree vertices. */
+void oracle_pagerank_f64(int32_t V, const int32_t *row_ptr, const int32_t *col,
+                         double damping, int iterations, double *pr);
+
+/* Same recurrence in FP32 with OpenMP (the timed CPU baseline). */
+void oracle_pagerank_f32_omp(int32_t V, const int32_t *row_ptr,
+                             const int32_t *col, float damping, int iterations,
+                             float *pr, float *scratch);
+
+/* OpenMP level-synchronous variants (timed CPU baseline; same outputs). */
+int oracle_lonestar_bfs_omp(int32_t V, const int32_t *row_ptr,
+                            const int32_t *col, int32_t source, uint32_t *dist,
+                            int32_t *scratch /* 2*V */);
+int oracle_lonestar_sssp_omp(int32_t V, const int32_t *row_ptr,
+                             const int32_t *col, const uint32_t *wt,
+                             int32_t source, uint32_t *dist,
+                             int32_t *scratch /* 3*V */);
+int oracle_pannotia_color_omp(int32_t V, const int32_t *row_ptr,
+                              const int32_t *col, const float *node_value,
+                              int32_t *color, float *max_d);
+int oracle_pannotia_mis_omp(int32_t V, const int32_t *row_ptr,
+                            const int32_t *col, const float *node_value,
+                            int32_t *s_array, int32_t *scratch /* 2*V */,
+                            float *min_array);
+
+/* Non-persistent tasks. */
+/* matmult.h:107-119 middle-square fill; returns the updated seed. */
+int32_t oracle_matmult_rand_fill(int32_t *M, int32_t rows, int32_t cols,
+                                 int32_t seed);
+/* matmult.cl:26-56 C = A*B with wrapping int32 arithmetic. */
+void oracle_matmult_i32(const int32_t *A, int32_t A_row, int32_t A_col,
+                        const int32_t *B, int32_t B_col, int32_t *C);
+/* matmult.cl:9-22 djb2 hash of the diagonal (wrapping int32). */
+int32_t oracle_hash_diag(const int32_t *M, int32_t rows, int32_t cols);
+/* reduce.cl:3-39 min over the buffer. */
+int32_t oracle_reduce_min_i32(const int32_t *buf, int64_t n);
+/* FP32 variants of the tasks (no reference counterpart). */
+void oracle_matmult_f32(const float *A, int32_t M, int32_t K, const float *B,
+                        int32_t N, float *C);
+float oracle_reduce_min_f32(const float *buf, int64_t n);
+
+int oracle_omp_threads(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
