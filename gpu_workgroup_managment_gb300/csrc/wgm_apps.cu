@@ -1,0 +1,535 @@
+/*
+ * Persistent app plugins of libwgm (include/wgm.h "persistent app plugins").
+ *
+ * One wgm_app owns the device buffers of one persistent task, the way the
+ * reference's per-app plugin headers own their cl::Buffers
+ * (lonestar/graph_apps/bfs/bfs.h:23-30, pannotia/graph_apps/color/color.h:16-21,
+ * pannotia/graph_apps/mis/mis.h:14-20, pannotia/graph_apps/sssp/sssp.h:16-21).
+ */
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "../../include/wgm.h"
+#include "wgm_internal.h"
+#include "wgm_kernels.cuh"
+
+int wgm_kind_to_kernel(int kind) {
+  switch (kind) {
+    case WGM_APP_LONESTAR_BFS: return WGM_K_BFS;
+    case WGM_APP_LONESTAR_SSSP: return WGM_K_SSSP;
+    case WGM_APP_PANNOTIA_COLOR: return WGM_K_COLOR;
+    case WGM_APP_PANNOTIA_MIS: return WGM_K_MIS;
+    case WGM_APP_PANNOTIA_SSSP: return WGM_K_PSSSP;
+    case WGM_APP_PAGERANK: return WGM_K_PAGERANK;
+    default: return -1;
+  }
+}
+
+extern "C" const char *wgm_persistent_app_name(int kind) {
+  switch (kind) {
+    case WGM_APP_LONESTAR_BFS: return "lonestar_bfs";   /* bfs.h:193 */
+    case WGM_APP_LONESTAR_SSSP: return "lonestar_sssp"; /* sssp.h:195 */
+    case WGM_APP_PANNOTIA_COLOR: return "color";        /* color.h:24 */
+    case WGM_APP_PANNOTIA_MIS: return "mis";            /* mis.h:23 */
+    case WGM_APP_PANNOTIA_SSSP: return "sssp";          /* pannotia sssp.h:25 */
+    case WGM_APP_PAGERANK: return "pagerank";
+    default: return nullptr;
+  }
+}
+
+extern "C" const char *wgm_persistent_kernel_name(int kind) {
+  switch (kind) {
+    case WGM_APP_LONESTAR_BFS: return "drelax2";        /* bfs.h:197 */
+    case WGM_APP_LONESTAR_SSSP: return "drelax2";
+    case WGM_APP_PANNOTIA_COLOR: return "color_combined";
+    case WGM_APP_PANNOTIA_MIS: return "mis_combined";
+    case WGM_APP_PANNOTIA_SSSP: return "sssp_combined";
+    case WGM_APP_PAGERANK: return "pagerank_pull";
+    default: return nullptr;
+  }
+}
+
+static bool wgm_is_lonestar(int kind) {
+  return kind == WGM_APP_LONESTAR_BFS || kind == WGM_APP_LONESTAR_SSSP;
+}
+static bool wgm_needs_weights(int kind) {
+  return kind == WGM_APP_LONESTAR_SSSP || kind == WGM_APP_PANNOTIA_SSSP;
+}
+static bool wgm_uses_static_hubs(int kind) {
+  return kind == WGM_APP_PANNOTIA_COLOR || kind == WGM_APP_PANNOTIA_MIS ||
+         kind == WGM_APP_PANNOTIA_SSSP || kind == WGM_APP_PAGERANK;
+}
+
+/* Reject graphs the kernels cannot walk safely.  The Lonestar loader quirk
+ * (row_ptr[V] one less than the edge count, lonestar bfs.h:43) is accepted for
+ * the Lonestar apps; their kernels also skip out-of-range destinations like
+ * bfs.cl:116, every other app needs every col[] inside [0, V). */
+static int wgm_validate_graph(int kind, const wgm_graph_desc *g) {
+  if (!g || g->num_nodes < 1 || !g->row_ptr || g->num_edges < 0) return WGM_ERR_INVALID;
+  if (g->num_edges > 0 && !g->col) return WGM_ERR_INVALID;
+  if (g->num_edges >= (int64_t)INT32_MAX) return WGM_ERR_INVALID;
+  const int V = g->num_nodes;
+  const int32_t *rp = g->row_ptr;
+  if (rp[0] != 0) return WGM_ERR_INVALID;
+  for (int i = 0; i < V - 1; i++)
+    if (rp[i + 1] < rp[i]) return WGM_ERR_INVALID;
+  int64_t last = rp[V];
+  if (wgm_is_lonestar(kind)) {
+    if (last < (int64_t)rp[V - 1] - 1 || last > g->num_edges) return WGM_ERR_INVALID;
+  } else {
+    if (last < rp[V - 1] || last != g->num_edges) return WGM_ERR_INVALID;
+    for (int64_t k = 0; k < g->num_edges; k++)
+      if ((uint32_t)g->col[k] >= (uint32_t)V) return WGM_ERR_INVALID;
+  }
+  if (wgm_needs_weights(kind) && g->num_edges > 0 && !g->weights) return WGM_ERR_INVALID;
+  if (kind == WGM_APP_PANNOTIA_COLOR || kind == WGM_APP_PANNOTIA_MIS) {
+    /* A self loop makes a vertex its own uncoloured/active neighbour: the
+     * reference's colour and MIS loops never end on such a graph. */
+    for (int v = 0; v < V; v++)
+      for (int k = rp[v]; k < rp[v + 1]; k++)
+        if (g->col[k] == v) return WGM_ERR_INVALID;
+  }
+  return WGM_OK;
+}
+
+/* Hub layout for the static-frontier apps (see wgm_hubs in wgm_graph.cuh). */
+static void wgm_build_hubs(const wgm_graph_desc *g, int T, std::vector<int> &ids,
+                           std::vector<int> &prefix, std::vector<int> &wmap) {
+  ids.clear();
+  prefix.assign(1, 0);
+  wmap.clear();
+  for (int v = 0; v < g->num_nodes; v++) {
+    int d = g->row_ptr[v + 1] - g->row_ptr[v];
+    if (d > T) {
+      ids.push_back(v);
+      prefix.push_back(prefix.back() + d);
+    }
+  }
+  int total = prefix.back();
+  int nwin = (total + 31) / 32;
+  wmap.resize(nwin);
+  int h = 0;
+  for (int k = 0; k < nwin; k++) {
+    while (prefix[h + 1] <= k * 32) h++;
+    wmap[k] = h;
+  }
+}
+
+static void wgm_app_free_buffers(wgm_app *a) {
+  void *ptrs[] = {a->d_row,     a->d_col,       a->d_wt,      a->d_node_value, a->d_out,
+                  a->d_wl,      a->d_cnt,       a->d_stamp,   a->d_stop,       a->d_hub_acc,
+                  a->d_status,  a->d_contrib,   a->d_dang,    a->d_hub_sum,    a->d_rounds,
+                  a->hubs.ids,  a->hubs.prefix, a->hubs.wmap};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  a->hubs = wgm_dev_hubs();
+}
+
+template <class T>
+static cudaError_t wgm_dmalloc(T **p, size_t count) {
+  return cudaMalloc((void **)p, std::max<size_t>(count, 1) * sizeof(T));
+}
+
+static int wgm_upload_hubs(wgm_app *a, const wgm_graph_desc *g) {
+  std::vector<int> ids, prefix, wmap;
+  wgm_build_hubs(g, a->hub_threshold, ids, prefix, wmap);
+  cudaStream_t s = a->rt->stream;
+  cudaError_t e = cudaSuccess;
+  if (a->hubs.ids) {
+    cudaFree(a->hubs.ids);
+    cudaFree(a->hubs.prefix);
+    cudaFree(a->hubs.wmap);
+    a->hubs = wgm_dev_hubs();
+  }
+  if (e == cudaSuccess) e = wgm_dmalloc(&a->hubs.ids, ids.size());
+  if (e == cudaSuccess) e = wgm_dmalloc(&a->hubs.prefix, prefix.size());
+  if (e == cudaSuccess) e = wgm_dmalloc(&a->hubs.wmap, wmap.size());
+  if (e == cudaSuccess && !ids.empty())
+    e = cudaMemcpyAsync(a->hubs.ids, ids.data(), ids.size() * 4, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(a->hubs.prefix, prefix.data(), prefix.size() * 4,
+                        cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess && !wmap.empty())
+    e = cudaMemcpyAsync(a->hubs.wmap, wmap.data(), wmap.size() * 4, cudaMemcpyHostToDevice, s);
+  /* the host vectors die here: finish the copies first */
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return wgm_cuda_fail(a->rt, e);
+  a->hubs.H = (int)ids.size();
+  a->hubs.total = prefix.back();
+  if (a->kind == WGM_APP_PANNOTIA_COLOR || a->kind == WGM_APP_PANNOTIA_MIS ||
+      a->kind == WGM_APP_PAGERANK) {
+    if (a->d_hub_acc) cudaFree(a->d_hub_acc);
+    if (a->d_hub_sum) cudaFree(a->d_hub_sum);
+    a->d_hub_acc = nullptr;
+    a->d_hub_sum = nullptr;
+    if (a->kind == WGM_APP_PAGERANK)
+      e = wgm_dmalloc(&a->d_hub_sum, (size_t)a->hubs.H);
+    else
+      e = wgm_dmalloc(&a->d_hub_acc, (size_t)a->hubs.H * 2);
+    if (e != cudaSuccess) return wgm_cuda_fail(a->rt, e);
+  }
+  return WGM_OK;
+}
+
+extern "C" int wgm_app_upload(wgm_app *a, const wgm_graph_desc *g) {
+  if (!a) return WGM_ERR_INVALID;
+  int s = wgm_validate_graph(a->kind, g);
+  if (s) return s;
+  if (g->num_nodes != a->V || g->num_edges != a->E) return WGM_ERR_INVALID;
+  cudaSetDevice(a->rt->device);
+  cudaStream_t st = a->rt->stream;
+  cudaError_t e =
+      cudaMemcpyAsync(a->d_row, g->row_ptr, (size_t)(a->V + 1) * 4, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess && a->E > 0)
+    e = cudaMemcpyAsync(a->d_col, g->col, (size_t)a->E * 4, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess && wgm_needs_weights(a->kind) && a->E > 0)
+    e = cudaMemcpyAsync(a->d_wt, g->weights, (size_t)a->E * 4, cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return wgm_cuda_fail(a->rt, e);
+  if (wgm_uses_static_hubs(a->kind)) {
+    s = wgm_upload_hubs(a, g);
+    if (s) return s;
+  }
+  return WGM_OK;
+}
+
+extern "C" int wgm_app_create(wgm_runtime *rt, int kind, const wgm_graph_desc *g,
+                              wgm_app **out) {
+  if (!rt || !out) return WGM_ERR_INVALID;
+  *out = nullptr;
+  if (wgm_kind_to_kernel(kind) < 0) return WGM_ERR_INVALID;
+  int s = wgm_validate_graph(kind, g);
+  if (s) return s;
+  cudaSetDevice(rt->device);
+  wgm_app *a = new (std::nothrow) wgm_app();
+  if (!a) return WGM_ERR_OOM;
+  a->rt = rt;
+  a->kind = kind;
+  a->V = g->num_nodes;
+  a->E = g->num_edges;
+  a->hub_threshold = std::max(rt->cfg.hub_threshold, 32);
+  const size_t V = (size_t)a->V, E = (size_t)a->E;
+  cudaError_t e = wgm_dmalloc(&a->d_row, V + 1);
+  if (e == cudaSuccess) e = wgm_dmalloc(&a->d_col, E);
+  if (e == cudaSuccess) e = wgm_dmalloc(&a->d_rounds, 1);
+  if (e == cudaSuccess && wgm_needs_weights(kind)) e = wgm_dmalloc(&a->d_wt, E);
+  switch (kind) {
+    case WGM_APP_LONESTAR_BFS:
+    case WGM_APP_LONESTAR_SSSP:
+      a->out_bytes = V * 4;
+      if (e == cudaSuccess) e = cudaMalloc(&a->d_out, a->out_bytes);
+      if (e == cudaSuccess) e = wgm_dmalloc(&a->d_wl, 2 * V);
+      if (e == cudaSuccess) e = wgm_dmalloc(&a->d_cnt, 6 * WGM_LINE);
+      if (e == cudaSuccess && kind == WGM_APP_LONESTAR_SSSP) e = wgm_dmalloc(&a->d_stamp, V);
+      break;
+    case WGM_APP_PANNOTIA_COLOR:
+    case WGM_APP_PANNOTIA_MIS:
+      a->out_bytes = V * 4;
+      if (e == cudaSuccess) e = cudaMalloc(&a->d_out, a->out_bytes);
+      if (e == cudaSuccess) e = wgm_dmalloc(&a->d_node_value, V);
+      if (e == cudaSuccess) e = wgm_dmalloc(&a->d_stop, 3 * WGM_LINE);
+      if (e == cudaSuccess && kind == WGM_APP_PANNOTIA_MIS) e = wgm_dmalloc(&a->d_status, V);
+      break;
+    case WGM_APP_PANNOTIA_SSSP:
+      a->out_bytes = V * 4;
+      if (e == cudaSuccess) e = cudaMalloc(&a->d_out, a->out_bytes);
+      if (e == cudaSuccess) e = wgm_dmalloc(&a->d_stop, 3 * WGM_LINE);
+      break;
+    case WGM_APP_PAGERANK:
+      a->out_bytes = V * 4;
+      if (e == cudaSuccess) e = cudaMalloc(&a->d_out, a->out_bytes);
+      if (e == cudaSuccess) e = wgm_dmalloc(&a->d_contrib, 2 * V);
+      if (e == cudaSuccess) e = wgm_dmalloc(&a->d_dang, 3 * WGM_LINE);
+      break;
+  }
+  if (e != cudaSuccess) {
+    s = wgm_cuda_fail(rt, e);
+    wgm_app_free_buffers(a);
+    delete a;
+    return s;
+  }
+  s = wgm_app_upload(a, g);
+  if (s == WGM_OK && (kind == WGM_APP_PANNOTIA_COLOR || kind == WGM_APP_PANNOTIA_MIS)) {
+    /* Default priorities: the reference rule node_value[i] = i/(V+1)
+     * (color.h:53, mis.h:55). */
+    std::vector<float> nv(V);
+    for (size_t i = 0; i < V; i++) nv[i] = (float)i / (float)(a->V + 1);
+    s = wgm_app_set_node_values(a, nv.data());
+    a->has_node_values = false;
+  }
+  if (s) {
+    wgm_app_free_buffers(a);
+    delete a;
+    return s;
+  }
+  *out = a;
+  return WGM_OK;
+}
+
+extern "C" int wgm_app_set_source(wgm_app *a, int32_t source) {
+  if (!a || source < 0 || source >= a->V) return WGM_ERR_INVALID;
+  a->source = source;
+  return WGM_OK;
+}
+
+extern "C" int wgm_app_set_node_values(wgm_app *a, const float *nv) {
+  if (!a || !nv || !a->d_node_value) return WGM_ERR_INVALID;
+  for (int i = 0; i < a->V; i++)
+    if (!(nv[i] >= 0.0f && nv[i] < 1.0e30f)) return WGM_ERR_INVALID; /* finite, >= 0 */
+  {
+    /* Equal priorities on adjacent vertices stall colour and MIS forever (in
+     * the reference too): require distinct values. */
+    std::vector<float> sorted(nv, nv + a->V);
+    std::sort(sorted.begin(), sorted.end());
+    for (int i = 1; i < a->V; i++)
+      if (sorted[i] == sorted[i - 1]) return WGM_ERR_INVALID;
+  }
+  cudaSetDevice(a->rt->device);
+  cudaError_t e = cudaMemcpyAsync(a->d_node_value, nv, (size_t)a->V * 4, cudaMemcpyHostToDevice,
+                                  a->rt->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(a->rt->stream);
+  if (e != cudaSuccess) return wgm_cuda_fail(a->rt, e);
+  a->has_node_values = true;
+  return WGM_OK;
+}
+
+extern "C" int wgm_app_set_pagerank(wgm_app *a, float damping, int iterations) {
+  if (!a || a->kind != WGM_APP_PAGERANK || iterations < 0 || !(damping >= 0.f && damping <= 1.f))
+    return WGM_ERR_INVALID;
+  a->damping = damping;
+  a->iterations = iterations;
+  return WGM_OK;
+}
+
+static wgm_hubs wgm_hubs_view(const wgm_app *a) {
+  wgm_hubs h;
+  h.ids = a->hubs.ids;
+  h.prefix = a->hubs.prefix;
+  h.wmap = a->hubs.wmap;
+  h.H = a->hubs.H;
+  h.total = a->hubs.total;
+  return h;
+}
+
+/* Enqueue the app's persistent kernel on `stream`. */
+static cudaError_t wgm_app_enqueue(wgm_app *a, const wgm_launch &L, int grid, int block,
+                                   cudaStream_t stream) {
+  switch (a->kind) {
+    case WGM_APP_LONESTAR_BFS:
+    case WGM_APP_LONESTAR_SSSP: {
+      wgm_lonestar_args x;
+      x.V = a->V;
+      x.row = a->d_row;
+      x.col = a->d_col;
+      x.wt = a->d_wt;
+      x.dist = (unsigned *)a->d_out;
+      x.wl = a->d_wl;
+      x.cnt = a->d_cnt;
+      x.stamp = a->d_stamp;
+      x.source = a->source;
+      x.hub_threshold = a->hub_threshold;
+      x.levels_out = a->d_rounds;
+      return wgm_launch_lonestar(a->kind == WGM_APP_LONESTAR_SSSP, L, x, grid, block, stream);
+    }
+    case WGM_APP_PANNOTIA_COLOR: {
+      wgm_color_args x;
+      x.V = a->V;
+      x.row = a->d_row;
+      x.col = a->d_col;
+      x.node_value = a->d_node_value;
+      x.color = (int *)a->d_out;
+      x.stop = a->d_stop;
+      x.hub_acc = a->d_hub_acc;
+      x.hubs = wgm_hubs_view(a);
+      x.hub_threshold = a->hub_threshold;
+      x.rounds_out = a->d_rounds;
+      return wgm_launch_color(L, x, grid, block, stream);
+    }
+    case WGM_APP_PANNOTIA_MIS: {
+      wgm_mis_args x;
+      x.V = a->V;
+      x.row = a->d_row;
+      x.col = a->d_col;
+      x.node_value = a->d_node_value;
+      x.s_array = (int *)a->d_out;
+      x.status = a->d_status;
+      x.stop = a->d_stop;
+      x.hub_acc = a->d_hub_acc;
+      x.hubs = wgm_hubs_view(a);
+      x.hub_threshold = a->hub_threshold;
+      x.rounds_out = a->d_rounds;
+      return wgm_launch_mis(L, x, grid, block, stream);
+    }
+    case WGM_APP_PANNOTIA_SSSP: {
+      wgm_psssp_args x;
+      x.V = a->V;
+      x.row = a->d_row;
+      x.col = a->d_col;
+      x.data = (const int *)a->d_wt;
+      x.x = (int *)a->d_out;
+      x.stop = a->d_stop;
+      x.hubs = wgm_hubs_view(a);
+      x.hub_threshold = a->hub_threshold;
+      x.source = a->source;
+      x.rounds_out = a->d_rounds;
+      return wgm_launch_psssp(L, x, grid, block, stream);
+    }
+    case WGM_APP_PAGERANK: {
+      wgm_pr_args x;
+      x.V = a->V;
+      x.row = a->d_row;
+      x.col = a->d_col;
+      x.pr = (float *)a->d_out;
+      x.contrib = a->d_contrib;
+      x.dang = a->d_dang;
+      x.hub_sum = a->d_hub_sum;
+      x.hubs = wgm_hubs_view(a);
+      x.hub_threshold = a->hub_threshold;
+      x.iterations = a->iterations;
+      x.damping = a->damping;
+      return wgm_launch_pagerank(L, x, grid, block, stream);
+    }
+  }
+  return cudaErrorInvalidValue;
+}
+
+static int wgm_pick_grid(wgm_app *a, int num_wgs, int block, int *grid) {
+  int hw = 0;
+  int s = wgm_hw_bound_for(a->rt, wgm_kind_to_kernel(a->kind), block, &hw);
+  if (s) return s;
+  if (hw < 1) return WGM_ERR_INVALID;
+  *grid = (num_wgs > 0) ? std::min(num_wgs, hw) : hw;
+  return WGM_OK;
+}
+
+static int wgm_block_size(const wgm_runtime *rt) {
+  int b = rt->cfg.threads_per_wg;
+  if (b < 32 || b > 1024 || b % 32) b = 256;
+  return b;
+}
+
+extern "C" int wgm_launch_persistent(wgm_runtime *rt, wgm_app *a, int num_wgs, void *stream) {
+  if (!rt || !a || a->rt != rt) return WGM_ERR_INVALID;
+  cudaSetDevice(rt->device);
+  int block = wgm_block_size(rt), grid = 0;
+  int s = wgm_pick_grid(a, num_wgs, block, &grid);
+  if (s) return s;
+  if (rt->cfg.host_handshake) {
+    __atomic_store_n(&rt->hf->scheduler_flag, WGM_DEVICE_SCHEDULER_INIT, __ATOMIC_RELEASE);
+    __atomic_store_n(&rt->hf->persistent_flag, -1, __ATOMIC_RELEASE);
+  }
+  wgm_launch L = wgm_make_launch(rt, grid, rt->cfg.host_handshake ? 1 : 0, 0);
+  cudaError_t e = wgm_app_enqueue(a, L, grid, block, stream ? (cudaStream_t)stream : rt->stream);
+  if (e != cudaSuccess) return wgm_cuda_fail(rt, e);
+  return WGM_OK;
+}
+
+extern "C" int wgm_run_persistent(wgm_runtime *rt, wgm_app *a, int num_wgs,
+                                  wgm_run_stats *stats) {
+  if (!rt || !a || a->rt != rt) return WGM_ERR_INVALID;
+  cudaSetDevice(rt->device);
+  int block = wgm_block_size(rt), grid = 0;
+  int s = wgm_pick_grid(a, num_wgs, block, &grid);
+  if (s) return s;
+  const int handshake = rt->cfg.host_handshake ? 1 : 0;
+  if (handshake) {
+    __atomic_store_n(&rt->hf->scheduler_flag, WGM_DEVICE_SCHEDULER_INIT, __ATOMIC_RELEASE);
+    __atomic_store_n(&rt->hf->persistent_flag, -1, __ATOMIC_RELEASE);
+  }
+  wgm_launch L = wgm_make_launch(rt, grid, handshake, 0);
+  cudaError_t e = cudaEventRecord(rt->ev0, rt->stream);
+  if (e == cudaSuccess) e = wgm_app_enqueue(a, L, grid, block, rt->stream);
+  if (e == cudaSuccess) e = cudaEventRecord(rt->ev1, rt->stream);
+  if (e != cudaSuccess) return wgm_cuda_fail(rt, e);
+  double host_ms = 0.0;
+  int hs_status = WGM_OK;
+  if (handshake) {
+    /* skel.cpp:336-340: wait for DEVICE_WAITING, start the clock, release
+     * the task, wait for persistent_flag to drain to 0. */
+    uint64_t budget = rt->cfg.spin_timeout_ns ? rt->cfg.spin_timeout_ns : 2000000000ull;
+    if (!wgm_host_wait(&rt->hf->scheduler_flag, WGM_DEVICE_WAITING, true, budget * 4)) {
+      wgm_set_abort(rt, 1);
+      hs_status = WGM_ERR_TIMEOUT;
+    } else {
+      auto t0 = std::chrono::steady_clock::now();
+      __atomic_store_n(&rt->hf->scheduler_flag, WGM_DEVICE_TO_PERSISTENT_TASK, __ATOMIC_RELEASE);
+      if (!wgm_host_wait(&rt->hf->persistent_flag, 0, true, budget * 16)) {
+        wgm_set_abort(rt, 1);
+        hs_status = WGM_ERR_TIMEOUT;
+      }
+      auto t1 = std::chrono::steady_clock::now();
+      host_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+    }
+  }
+  int ws = wgm_stream_wait(rt, rt->stream);
+  if (ws == WGM_ERR_CUDA) return ws;
+  if (hs_status != WGM_OK) wgm_set_abort(rt, 0);
+  int dev_status = 0, dev_site = 0;
+  int groups = __atomic_load_n(&rt->hf->discovered, __ATOMIC_ACQUIRE);
+  s = wgm_finish_launch(rt, &dev_status, &dev_site);
+  if (stats) {
+    std::memset(stats, 0, sizeof(*stats));
+    stats->groups = groups;
+    stats->device_status = dev_status;
+    stats->device_site = dev_site;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, rt->ev0, rt->ev1);
+    stats->kernel_ms = ms;
+    stats->host_ms = host_ms;
+    int rounds = 0;
+    if (s == WGM_OK && cudaMemcpy(&rounds, a->d_rounds, 4, cudaMemcpyDeviceToHost) == cudaSuccess)
+      stats->rounds = rounds;
+  }
+  if (s == WGM_OK && hs_status != WGM_OK) s = hs_status;
+  if (s == WGM_OK && ws != WGM_OK) s = ws;
+  return s;
+}
+
+extern "C" int wgm_app_read_result(wgm_app *a, void *host_out, size_t bytes) {
+  if (!a || !host_out || bytes < a->out_bytes) return WGM_ERR_INVALID;
+  cudaSetDevice(a->rt->device);
+  cudaError_t e =
+      cudaMemcpyAsync(host_out, a->d_out, a->out_bytes, cudaMemcpyDeviceToHost, a->rt->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(a->rt->stream);
+  if (e != cudaSuccess) return wgm_cuda_fail(a->rt, e);
+  return WGM_OK;
+}
+
+extern "C" int wgm_app_result_device_ptr(wgm_app *a, void **p, size_t *bytes) {
+  if (!a || !p) return WGM_ERR_INVALID;
+  *p = a->d_out;
+  if (bytes) *bytes = a->out_bytes;
+  return WGM_OK;
+}
+
+extern "C" int wgm_app_rounds(wgm_app *a, int *rounds) {
+  if (!a || !rounds) return WGM_ERR_INVALID;
+  cudaSetDevice(a->rt->device);
+  cudaError_t e = cudaMemcpy(rounds, a->d_rounds, 4, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return wgm_cuda_fail(a->rt, e);
+  return WGM_OK;
+}
+
+extern "C" int wgm_app_destroy(wgm_app *a) {
+  if (!a) return WGM_ERR_INVALID;
+  cudaSetDevice(a->rt->device);
+  cudaStreamSynchronize(a->rt->stream);
+  wgm_app_free_buffers(a);
+  delete a;
+  return WGM_OK;
+}
+
+extern "C" void *wgm_host_alloc(size_t bytes) {
+  void *p = nullptr;
+  if (cudaHostAlloc(&p, std::max<size_t>(bytes, 1), cudaHostAllocDefault) != cudaSuccess)
+    return nullptr;
+  return p;
+}
+
+extern "C" void wgm_host_free(void *p) {
+  if (p) cudaFreeHost(p);
+}

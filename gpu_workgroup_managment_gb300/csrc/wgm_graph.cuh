@@ -1,0 +1,782 @@
+/*
+ * Persistent graph kernels for sm_103a: Lonestar BFS/SSSP worklists and
+ * Pannotia colour/MIS/SSSP frontier loops, plus pull PageRank, all running in
+ * one discovery-sized persistent grid synchronised by wgm_barrier.
+ *
+ * Reference kernels and what changed (outputs are bit-identical; each change
+ * is argued where it is made):
+ *   lonestar/graph_apps/bfs/device/bfs.cl:104-302   -> wgm_app_lonestar<false>
+ *   lonestar/graph_apps/sssp/device/sssp.cl:104-318 -> wgm_app_lonestar<true>
+ *   pannotia/graph_apps/color/device/color.cl:3-97  -> wgm_app_color
+ *   pannotia/graph_apps/mis/device/mis.cl:5-125     -> wgm_app_mis
+ *   pannotia/graph_apps/sssp/device/sssp.cl:10-88   -> wgm_app_pannotia_sssp
+ *   (no reference)                                  -> wgm_app_pagerank
+ *
+ * Edge work is warp-level.  A warp owns up to 32 vertices (one per lane),
+ * scans their degrees with shuffles and walks the concatenated adjacency in
+ * windows of 32 edges: lane j of a window handles edge slot w+j, its owner is
+ * found with one __reduce_or_sync and a clz, so col[] is read coalesced and no
+ * CTA-wide __syncthreads is needed inside the edge loop (the reference's
+ * block scan is serial in work-item 0, bfs.cl:43-51).  Vertices whose degree
+ * exceeds `hub_threshold` ("hubs") skip the warp path; their edges are spread
+ * over every warp of the grid so one hub never stalls a level.
+ */
+#ifndef WGM_GRAPH_CUH
+#define WGM_GRAPH_CUH
+
+#include "wgm_device.cuh"
+
+#define WGM_LONESTAR_INF 1000000000u /* bfs.cl:33 */
+#define WGM_PANNOTIA_BIG 99999999    /* pannotia sssp.h:3, mis.cl:1 */
+#define WGM_MAX_WARPS 32
+
+/* Per-CTA shared scratch of the edge-window walker. */
+struct wgm_warp_smem {
+  int tab[WGM_MAX_WARPS][32];
+  int acc[WGM_MAX_WARPS][32];
+};
+
+/* Walk the edge slots [w0, total) of a warp's concatenated adjacency in
+ * windows of 32, window stride `wstep`.  Each lane passes its own range as
+ * (off = exclusive prefix, deg, base = row start - off).  f(valid, edge,
+ * owner_lane) is called by all 32 lanes once per window. */
+template <class F>
+__device__ __forceinline__ void wgm_for_each_edge(int off, int deg, int base, int total,
+                                                  int w0, int wstep, int *tab, F &&f) {
+  const int lane = wgm_lane();
+  for (int w = w0; w < total; w += wstep) {
+    bool in = deg > 0 && off < w + 32 && off + deg > w;
+    int pos = in ? max(off - w, 0) : 0;
+    unsigned mask = __reduce_or_sync(WGM_FULL, in ? (1u << pos) : 0u);
+    if (in) tab[pos] = lane;
+    __syncwarp();
+    unsigned upto = (lane == 31) ? 0xffffffffu : ((2u << lane) - 1u);
+    unsigned mm = mask & upto;
+    int owner = tab[mm ? 31 - __clz(mm) : 0] & 31;
+    __syncwarp();
+    int eb = __shfl_sync(WGM_FULL, base, owner);
+    int slot = w + lane;
+    f(slot < total, eb + slot, owner);
+  }
+}
+
+/* Static hub layout (host-built): hub ids, their edge prefix and, for each
+ * window of 32 hub-edge slots, the first hub it touches.  Hubs have degree
+ * > 32, so a window touches at most two consecutive hubs. */
+struct wgm_hubs {
+  const int *ids;    /* [H] */
+  const int *prefix; /* [H+1] */
+  const int *wmap;   /* [ceil(prefix[H]/32)] */
+  int H;
+  int total;
+};
+
+/* Calls f(valid, hub_index, edge) for one window of hub edges. */
+template <class F>
+__device__ __forceinline__ void wgm_hub_window(const wgm_hubs &hb, const int *row, int k,
+                                               F &&f) {
+  const int lane = wgm_lane();
+  int slot = k * 32 + lane;
+  bool valid = slot < hb.total;
+  int h0 = __ldg(&hb.wmap[k]);
+  int h = h0;
+  if (h0 + 1 < hb.H && slot >= __ldg(&hb.prefix[h0 + 1])) h = h0 + 1;
+  int e = __ldg(&row[__ldg(&hb.ids[h])]) + (slot - __ldg(&hb.prefix[h]));
+  f(valid, h, e);
+}
+
+/* Reduce `v` over the lanes holding hub h0 and hub h0+1 separately; lane 0
+ * receives both results.  op: 0 = max (int bits), 1 = min (int bits), 2 = fp32 sum. */
+__device__ __forceinline__ void wgm_two_seg_reduce(bool first, int v, float fv, int op,
+                                                   int *r0, int *r1, float *f0,
+                                                   float *f1) {
+  int a = first ? v : (op == 0 ? INT_MIN : INT_MAX);
+  int b = first ? (op == 0 ? INT_MIN : INT_MAX) : v;
+  float fa = first ? fv : 0.f, fb = first ? 0.f : fv;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    int ya = __shfl_xor_sync(WGM_FULL, a, o), yb = __shfl_xor_sync(WGM_FULL, b, o);
+    float ga = __shfl_xor_sync(WGM_FULL, fa, o), gb = __shfl_xor_sync(WGM_FULL, fb, o);
+    if (op == 0) {
+      a = max(a, ya);
+      b = max(b, yb);
+    } else if (op == 1) {
+      a = min(a, ya);
+      b = min(b, yb);
+    }
+    fa += ga;
+    fb += gb;
+  }
+  *r0 = a;
+  *r1 = b;
+  *f0 = fa;
+  *f1 = fb;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Lonestar BFS / SSSP                                                       */
+/* ------------------------------------------------------------------------ */
+
+struct wgm_lonestar_args {
+  int V;
+  const int *row; /* [V+1]; row[V] may be row[V-1]-1 (Lonestar loader quirk) */
+  const int *col;
+  const unsigned *wt; /* SSSP weights, nullptr for BFS */
+  unsigned *dist;     /* [V] output */
+  int *wl;            /* [2][V]: small items grow up, hub items grow down */
+  int *cnt;           /* [6 lines]: small[3], big[3] counters (line each) */
+  int *stamp;         /* SSSP: level a vertex was last queued at */
+  int source;
+  int hub_threshold;
+  int *levels_out; /* number of levels run (written by group 0) */
+};
+
+/* Degree as the Lonestar kernel sees it: psrc[nn+1]-psrc[nn] (bfs.cl:165);
+ * the loader quirk can make the last vertex -1, which walks no edges. */
+__device__ __forceinline__ int wgm_ls_degree(const int *row, int v) {
+  return max(__ldg(&row[v + 1]) - __ldg(&row[v]), 0);
+}
+
+/* One relaxation of edge e from a vertex at distance dsrc, at level L.
+ * BFS (bfs.cl:115-125): dist[dst]==MYINFINITY -> dist[dst]=level; the
+ *   reference's unsynchronised store becomes a CAS so each vertex is queued
+ *   exactly once (the stored value is identical: the level).
+ * SSSP (sssp.cl:115-131): altdist = dist[src]+wt; if smaller, atomic_min and
+ *   queue dst; a per-level stamp queues a vertex at most once per level (its
+ *   next visit reads the final dist of the level, so the fixpoint - the
+ *   shortest-path vector - is unchanged). */
+template <bool SSSP>
+__device__ __forceinline__ bool wgm_ls_relax(const wgm_lonestar_args &a, int e, unsigned dsrc,
+                                             int L, int *u_out) {
+  int u = __ldg(&a.col[e]);
+  *u_out = u;
+  if ((unsigned)u >= (unsigned)a.V) return false; /* bfs.cl:116 */
+  if (!SSSP) {
+    if (__ldcg(&a.dist[u]) != WGM_LONESTAR_INF) return false;
+    return atomicCAS(&a.dist[u], WGM_LONESTAR_INF, (unsigned)L) == WGM_LONESTAR_INF;
+  } else {
+    unsigned w = __ldg(&a.wt[e]);
+    if (w >= WGM_LONESTAR_INF) return false; /* sssp.cl:120 */
+    unsigned alt = dsrc + w;
+    if (alt >= __ldcg(&a.dist[u])) return false;
+    unsigned old = atomicMin(&a.dist[u], alt);
+    if (alt >= old) return false;
+    return atomicExch(&a.stamp[u], L) != L;
+  }
+}
+
+template <bool SSSP>
+__device__ __forceinline__ bool wgm_ls_level(const wgm_launch &Lc, wgm_cta *c,
+                                             const wgm_lonestar_args &a, int L,
+                                             wgm_warp_smem *sm) {
+  const int lane = wgm_lane(), warp = threadIdx.x >> 5;
+  const int nwarps_cta = blockDim.x >> 5;
+  const int gw = c->id * nwarps_cta + warp, NW = c->ngroups * nwarps_cta;
+  const int V = a.V;
+  int *cnt = a.cnt;
+  const int ns = __ldcg(&cnt[(L % 3) * WGM_LINE]);
+  const int nb = __ldcg(&cnt[(3 + L % 3) * WGM_LINE]);
+  int *cnt_small_out = &cnt[((L + 1) % 3) * WGM_LINE];
+  int *cnt_big_out = &cnt[(3 + (L + 1) % 3) * WGM_LINE];
+  const int *in = a.wl + (size_t)(L & 1) * V;
+  int *out = a.wl + (size_t)((L + 1) & 1) * V;
+  bool ok = true;
+  auto edge_fn = [&](bool valid, int e, int owner, unsigned dsrc_lane) {
+    unsigned dsrc = SSSP ? __shfl_sync(WGM_FULL, dsrc_lane, owner) : 0u;
+    int u = 0;
+    bool push = valid && wgm_ls_relax<SSSP>(a, e, dsrc, L, &u);
+    bool big = push && (wgm_ls_degree(a.row, u) > a.hub_threshold);
+    ok &= wgm_warp_push(push && !big, u, cnt_small_out, out, V, false);
+    ok &= wgm_warp_push(big, u, cnt_big_out, out, V, true);
+  };
+  /* Small items: each warp takes 32 consecutive worklist entries. */
+  for (int b = gw * 32; b < ns; b += NW * 32) {
+    int i = b + lane, v = -1, deg = 0, start = 0;
+    unsigned dv = 0;
+    if (i < ns) {
+      v = __ldcg(&in[i]);
+      start = __ldg(&a.row[v]);
+      deg = wgm_ls_degree(a.row, v);
+      if (SSSP) dv = __ldcg(&a.dist[v]);
+    }
+    int incl = wgm_warp_incl_scan(deg);
+    int total = __shfl_sync(WGM_FULL, incl, 31);
+    int off = incl - deg;
+    wgm_for_each_edge(off, deg, start - off, total, 0, 32, sm->tab[warp],
+                      [&](bool valid, int e, int owner) { edge_fn(valid, e, owner, dv); });
+  }
+  /* Hub items (stored at the back of the list): every warp of the grid
+   * takes a share of the windows of each batch of 32 hubs. */
+  for (int hb = 0; hb < nb; hb += 32) {
+    int i = hb + lane, v = -1, deg = 0, start = 0;
+    unsigned dv = 0;
+    if (i < nb) {
+      v = __ldcg(&in[V - 1 - i]);
+      start = __ldg(&a.row[v]);
+      deg = wgm_ls_degree(a.row, v);
+      if (SSSP) dv = __ldcg(&a.dist[v]);
+    }
+    int incl = wgm_warp_incl_scan(deg);
+    int total = __shfl_sync(WGM_FULL, incl, 31);
+    int off = incl - deg;
+    wgm_for_each_edge(off, deg, start - off, total, gw * 32, NW * 32, sm->tab[warp],
+                      [&](bool valid, int e, int owner) { edge_fn(valid, e, owner, dv); });
+  }
+  return ok;
+}
+
+/* Persistent BFS/SSSP loop.  One barrier per level (the reference uses two,
+ * bfs.cl:282,295): worklist counters are triple-buffered by level, so the
+ * counter a level fills was cleared two levels earlier and the swap/reset
+ * step needs no barrier of its own. */
+template <bool SSSP>
+static __device__ void wgm_app_lonestar(const wgm_launch &Lc, wgm_cta *c,
+                                 const wgm_lonestar_args &a, wgm_warp_smem *sm) {
+  const int V = a.V;
+  const int tid = c->id * blockDim.x + threadIdx.x, nth = c->ngroups * blockDim.x;
+  /* Host init of the plugin (bfs.h:250-262) done on the device. */
+  for (int i = tid; i < V; i += nth) {
+    a.dist[i] = (i == a.source) ? 0u : WGM_LONESTAR_INF;
+    if (SSSP) a.stamp[i] = 0;
+  }
+  if (c->id == 0 && threadIdx.x == 0) {
+    for (int k = 0; k < 6; k++) a.cnt[k * WGM_LINE] = 0;
+    /* Level 1 processes the source (bfs.cl:235-241 seeds it at iteration 0). */
+    bool big = wgm_ls_degree(a.row, a.source) > a.hub_threshold;
+    if (big) {
+      a.wl[1 * (size_t)V + V - 1] = a.source;
+      a.cnt[(3 + 1) * WGM_LINE] = 1;
+    } else {
+      a.wl[1 * (size_t)V] = a.source;
+      a.cnt[1 * WGM_LINE] = 1;
+    }
+  }
+  if (!wgm_barrier(Lc, c)) return;
+  int L = 1;
+  for (;;) {
+    int ns = __ldcg(&a.cnt[(L % 3) * WGM_LINE]);
+    int nb = __ldcg(&a.cnt[(3 + L % 3) * WGM_LINE]);
+    if (ns + nb == 0) break;
+    if (ns + nb > V) {
+      wgm_fail(Lc, WGM_DEV_OVERFLOW, WGM_SITE_QUEUE, L);
+      return;
+    }
+    if (L > V + 2) { /* Bellman-Ford bound; only a corrupt input gets here */
+      wgm_fail(Lc, WGM_DEV_BAD_INPUT, WGM_SITE_QUEUE, L);
+      return;
+    }
+    if (c->id == 0 && threadIdx.x == 0) {
+      a.cnt[((L + 2) % 3) * WGM_LINE] = 0;
+      a.cnt[(3 + (L + 2) % 3) * WGM_LINE] = 0;
+    }
+    if (!wgm_ls_level<SSSP>(Lc, c, a, L, sm)) wgm_fail(Lc, WGM_DEV_OVERFLOW, WGM_SITE_QUEUE, L);
+    if (!wgm_barrier(Lc, c)) return;
+    L++;
+  }
+  if (c->id == 0 && threadIdx.x == 0 && a.levels_out) *a.levels_out = L;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Pannotia colour                                                           */
+/* ------------------------------------------------------------------------ */
+
+struct wgm_color_args {
+  int V;
+  const int *row; /* [V+1] */
+  const int *col;
+  const float *node_value;
+  int *color;    /* [V] output: 1-based colours */
+  int *stop;     /* [3 lines] */
+  int *hub_acc;  /* [H] running max (float bits) */
+  wgm_hubs hubs;
+  int hub_threshold;
+  int *rounds_out;
+};
+
+/* "Uncoloured at the start of round r": colours are written as the round
+ * number, so a vertex coloured earlier in the same round still counts as
+ * uncoloured for its neighbours - exactly the reference's view, where colours
+ * only change in the color2 phase after the barrier (color.cl:66-83). */
+__device__ __forceinline__ bool wgm_uncoloured_at(int cval, int r) {
+  return cval == -1 || cval == r;
+}
+
+/* One barrier per round when no hub is uncoloured, two otherwise (the
+ * reference uses two every round).  Round r fuses color1 and color2 for every
+ * non-hub vertex: max over the neighbours uncoloured at round start (skipping
+ * all neighbours of degree-1 vertices, color.cl:46), then colour r if the
+ * vertex's value is larger (color.cl:78-81).  Hub maxima accumulate in
+ * hub_acc across the grid and are decided after the first barrier. */
+static __device__ void wgm_app_color(const wgm_launch &Lc, wgm_cta *c, const wgm_color_args &a,
+                              wgm_warp_smem *sm) {
+  const int lane = wgm_lane(), warp = threadIdx.x >> 5;
+  const int nwarps_cta = blockDim.x >> 5;
+  const int gw = c->id * nwarps_cta + warp, NW = c->ngroups * nwarps_cta;
+  const int tid = c->id * blockDim.x + threadIdx.x, nth = c->ngroups * blockDim.x;
+  const int V = a.V;
+  const int NEG1 = __float_as_int(-1.0f);
+  for (int i = tid; i < V; i += nth) a.color[i] = -1; /* color.h:50 */
+  for (int h = tid; h < a.hubs.H; h += nth) a.hub_acc[h] = NEG1;
+  if (c->id == 0 && threadIdx.x == 0)
+    for (int k = 0; k < 3; k++) a.stop[k * WGM_LINE] = 0;
+  if (!wgm_barrier(Lc, c)) return;
+  int r = 1;
+  for (;;) {
+    if (r > V + 2) { /* every round settles at least one vertex of a valid input */
+      wgm_fail(Lc, WGM_DEV_BAD_INPUT, WGM_SITE_QUEUE, r);
+      return;
+    }
+    if (c->id == 0 && threadIdx.x == 0) a.stop[((r + 1) % 3) * WGM_LINE] = 0;
+    bool any = false;
+    /* Non-hub vertices. */
+    for (int b = gw * 32; b < V; b += NW * 32) {
+      int i = b + lane;
+      int deg = 0, start = 0;
+      bool unc = false;
+      if (i < V) {
+        unc = __ldcg(&a.color[i]) == -1;
+        start = __ldg(&a.row[i]);
+        int d = __ldg(&a.row[i + 1]) - start;
+        if (unc && d <= a.hub_threshold) deg = (d == 1) ? 0 : d;
+        if (d > a.hub_threshold) unc = false;
+      }
+      sm->acc[warp][lane] = NEG1;
+      int incl = wgm_warp_incl_scan(deg);
+      int total = __shfl_sync(WGM_FULL, incl, 31);
+      int off = incl - deg;
+      __syncwarp();
+      wgm_for_each_edge(off, deg, start - off, total, 0, 32, sm->tab[warp],
+                        [&](bool valid, int e, int owner) {
+                          if (valid) {
+                            int j = __ldg(&a.col[e]);
+                            if (wgm_uncoloured_at(__ldcg(&a.color[j]), r)) {
+                              any = true;
+                              atomicMax(&sm->acc[warp][owner],
+                                        __float_as_int(__ldg(&a.node_value[j])));
+                            }
+                          }
+                        });
+      __syncwarp();
+      if (unc && __ldg(&a.node_value[i]) > __int_as_float(sm->acc[warp][lane]))
+        a.color[i] = r;
+    }
+    /* Hubs still uncoloured: spread their edges over every warp. */
+    int nwin = (a.hubs.total + 31) >> 5;
+    for (int k = gw; k < nwin; k += NW) {
+      wgm_hub_window(a.hubs, a.row, k, [&](bool valid, int h, int e) {
+        int h0 = __shfl_sync(WGM_FULL, h, 0);
+        int val = INT_MIN;
+        if (valid && __ldcg(&a.color[__ldg(&a.hubs.ids[h])]) == -1) {
+          int j = __ldg(&a.col[e]);
+          if (wgm_uncoloured_at(__ldcg(&a.color[j]), r)) {
+            any = true;
+            val = __float_as_int(__ldg(&a.node_value[j]));
+          }
+        }
+        int m0, m1;
+        float f0, f1;
+        wgm_two_seg_reduce(h == h0, val, 0.f, 0, &m0, &m1, &f0, &f1);
+        if (lane == 0) {
+          if (m0 != INT_MIN) atomicMax(&a.hub_acc[h0], m0);
+          if (m1 != INT_MIN && h0 + 1 < a.hubs.H) atomicMax(&a.hub_acc[h0 + 1], m1);
+        }
+      });
+    }
+    if (__any_sync(WGM_FULL, any) && lane == 0) a.stop[(r % 3) * WGM_LINE] = 1;
+    if (!wgm_barrier(Lc, c)) return;
+    if (a.hubs.H > 0) {
+      /* Hub decisions (color.cl:77-81 for hubs), then reset the maxima. */
+      for (int h = tid; h < a.hubs.H; h += nth) {
+        int v = __ldg(&a.hubs.ids[h]);
+        if (__ldcg(&a.color[v]) == -1 &&
+            __ldg(&a.node_value[v]) > __int_as_float(__ldcg(&a.hub_acc[h])))
+          a.color[v] = r;
+        a.hub_acc[h] = NEG1;
+      }
+      if (!wgm_barrier(Lc, c)) return;
+    }
+    if (__ldcg(&a.stop[(r % 3) * WGM_LINE]) == 0) break; /* color.cl:85-87 */
+    r++;
+  }
+  if (c->id == 0 && threadIdx.x == 0 && a.rounds_out) *a.rounds_out = r;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Pannotia MIS                                                              */
+/* ------------------------------------------------------------------------ */
+
+struct wgm_mis_args {
+  int V;
+  const int *row;
+  const int *col;
+  const float *node_value;
+  int *s_array; /* [V] output: 2 = member, 0 = not */
+  int *status;  /* [V]: -1 active, 2r removed in round r, 2r+1 joined in r */
+  int *stop;    /* [3 lines] */
+  int *hub_acc; /* [2][H] running min (float bits), by round parity */
+  wgm_hubs hubs;
+  int hub_threshold;
+  int *rounds_out;
+};
+
+/* The reference's c_array/cu_array pair (mis.cl:73-118) becomes one status
+ * word stamped with the round: a vertex is "active at the start of round r"
+ * iff status == -1 or status>>1 == r, which is exactly what mis1/mis2 of round
+ * r see in the reference (cu is only committed to c in mis3, after the
+ * barrier).  That lets mis1+mis2+mis3 run between two barriers instead of
+ * three; s_array, the only output the reference checks (mis.h:199-202), is
+ * identical. */
+__device__ __forceinline__ bool wgm_active_at(int st, int r) {
+  return st == -1 || (st >> 1) == r;
+}
+
+static __device__ void wgm_app_mis(const wgm_launch &Lc, wgm_cta *c, const wgm_mis_args &a,
+                            wgm_warp_smem *sm) {
+  const int lane = wgm_lane(), warp = threadIdx.x >> 5;
+  const int nwarps_cta = blockDim.x >> 5;
+  const int gw = c->id * nwarps_cta + warp, NW = c->ngroups * nwarps_cta;
+  const int tid = c->id * blockDim.x + threadIdx.x, nth = c->ngroups * blockDim.x;
+  const int V = a.V;
+  const int BIG = __float_as_int((float)WGM_PANNOTIA_BIG);
+  for (int i = tid; i < V; i += nth) {
+    a.s_array[i] = 0; /* mis.h:58-92 */
+    a.status[i] = -1;
+  }
+  for (int h = tid; h < 2 * a.hubs.H; h += nth) a.hub_acc[h] = BIG;
+  if (c->id == 0 && threadIdx.x == 0)
+    for (int k = 0; k < 3; k++) a.stop[k * WGM_LINE] = 0;
+  if (!wgm_barrier(Lc, c)) return;
+  int r = 1;
+  for (;;) {
+    if (r > V + 2) { /* every round settles at least one vertex of a valid input */
+      wgm_fail(Lc, WGM_DEV_BAD_INPUT, WGM_SITE_QUEUE, r);
+      return;
+    }
+    if (c->id == 0 && threadIdx.x == 0) a.stop[((r + 1) % 3) * WGM_LINE] = 0;
+    int *hacc = a.hub_acc + (size_t)(r & 1) * a.hubs.H;
+    bool any = false;
+    for (int b = gw * 32; b < V; b += NW * 32) {
+      int i = b + lane;
+      int deg = 0, start = 0;
+      bool act = false;
+      if (i < V) {
+        act = __ldcg(&a.status[i]) == -1; /* active: nothing else can stamp it yet */
+        start = __ldg(&a.row[i]);
+        int d = __ldg(&a.row[i + 1]) - start;
+        if (act) any = true; /* mis.cl:33 */
+        if (d > a.hub_threshold) act = false;
+        else if (act) deg = d;
+      }
+      sm->acc[warp][lane] = BIG;
+      int incl = wgm_warp_incl_scan(deg);
+      int total = __shfl_sync(WGM_FULL, incl, 31);
+      int off = incl - deg;
+      __syncwarp();
+      /* mis1: min over neighbours active at round start (mis.cl:44-51). */
+      wgm_for_each_edge(off, deg, start - off, total, 0, 32, sm->tab[warp],
+                        [&](bool valid, int e, int owner) {
+                          if (valid) {
+                            int j = __ldg(&a.col[e]);
+                            if (wgm_active_at(__ldcg(&a.status[j]), r))
+                              atomicMin(&sm->acc[warp][owner],
+                                        __float_as_int(__ldg(&a.node_value[j])));
+                          }
+                        });
+      __syncwarp();
+      /* mis2: join, then mark the neighbours removed (mis.cl:68-95). */
+      bool join = act && __ldg(&a.node_value[i]) < __int_as_float(sm->acc[warp][lane]);
+      if (join) {
+        a.s_array[i] = 2;
+        a.status[i] = 2 * r + 1;
+      }
+      int jdeg = join ? deg : 0;
+      int jincl = wgm_warp_incl_scan(jdeg);
+      int jtotal = __shfl_sync(WGM_FULL, jincl, 31);
+      int joff = jincl - jdeg;
+      wgm_for_each_edge(joff, jdeg, start - joff, jtotal, 0, 32, sm->tab[warp],
+                        [&](bool valid, int e, int owner) {
+                          if (valid) {
+                            int j = __ldg(&a.col[e]);
+                            if (wgm_active_at(__ldcg(&a.status[j]), r)) a.status[j] = 2 * r;
+                          }
+                        });
+    }
+    /* Hub minima across the grid (mis1 for hubs). */
+    int nwin = (a.hubs.total + 31) >> 5;
+    for (int k = gw; k < nwin; k += NW) {
+      wgm_hub_window(a.hubs, a.row, k, [&](bool valid, int h, int e) {
+        int h0 = __shfl_sync(WGM_FULL, h, 0);
+        int val = INT_MAX;
+        if (valid && wgm_active_at(__ldcg(&a.status[__ldg(&a.hubs.ids[h])]), r)) {
+          int j = __ldg(&a.col[e]);
+          if (wgm_active_at(__ldcg(&a.status[j]), r))
+            val = __float_as_int(__ldg(&a.node_value[j]));
+        }
+        int m0, m1;
+        float f0, f1;
+        wgm_two_seg_reduce(h == h0, val, 0.f, 1, &m0, &m1, &f0, &f1);
+        if (lane == 0) {
+          if (m0 != INT_MAX) atomicMin(&hacc[h0], m0);
+          if (m1 != INT_MAX && h0 + 1 < a.hubs.H) atomicMin(&hacc[h0 + 1], m1);
+        }
+      });
+    }
+    if (__any_sync(WGM_FULL, any) && lane == 0) a.stop[(r % 3) * WGM_LINE] = 1;
+    if (!wgm_barrier(Lc, c)) return;
+    if (a.hubs.H > 0) {
+      /* mis2 for hubs.  The join test is a pure function of the final hub
+       * minimum and the round-start status (a joined hub reads 2r+1, still
+       * "active at r"), so every warp re-derives it while marking neighbours
+       * and one thread per hub records the join.  The other parity's minima
+       * are reset here for the next round. */
+      int *hnext = a.hub_acc + (size_t)((r + 1) & 1) * a.hubs.H;
+      for (int h = tid; h < a.hubs.H; h += nth) {
+        int v = __ldg(&a.hubs.ids[h]);
+        if (__ldcg(&a.status[v]) == -1 &&
+            __ldg(&a.node_value[v]) < __int_as_float(__ldcg(&hacc[h]))) {
+          a.s_array[v] = 2;
+          a.status[v] = 2 * r + 1;
+        }
+        hnext[h] = BIG;
+      }
+      for (int k = gw; k < nwin; k += NW) {
+        wgm_hub_window(a.hubs, a.row, k, [&](bool valid, int h, int e) {
+          if (!valid) return;
+          int v = __ldg(&a.hubs.ids[h]);
+          int stv = __ldcg(&a.status[v]);
+          if (wgm_active_at(stv, r) && stv != 2 * r &&
+              __ldg(&a.node_value[v]) < __int_as_float(__ldcg(&hacc[h]))) {
+            int j = __ldg(&a.col[e]);
+            if (wgm_active_at(__ldcg(&a.status[j]), r) && j != v) a.status[j] = 2 * r;
+          }
+        });
+      }
+      if (!wgm_barrier(Lc, c)) return;
+    }
+    if (__ldcg(&a.stop[(r % 3) * WGM_LINE]) == 0) break; /* mis.cl:106-108 */
+    r++;
+  }
+  if (c->id == 0 && threadIdx.x == 0 && a.rounds_out) *a.rounds_out = r;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Pannotia SSSP (pull min-plus)                                             */
+/* ------------------------------------------------------------------------ */
+
+struct wgm_psssp_args {
+  int V;
+  const int *row;
+  const int *col;
+  const int *data;
+  int *x;    /* [V] output cost (sssp.h:168 reads x) */
+  int *stop; /* [3 lines] */
+  wgm_hubs hubs;
+  int hub_threshold;
+  int source;
+  int *rounds_out;
+};
+
+/* sssp.cl's vector_assign / spmv_min_dot_plus / vector_diff (three barriers
+ * per round) become one in-place relaxation pass per round:
+ * x[v] = min(x[v], min_j data[j] + x[col[j]]).  The reference's Jacobi
+ * iteration and this chaotic (in-place) iteration both stop at the fixpoint
+ * of the min-plus system started from x = BIG_NUM except x[source] = 0, which
+ * is unique (the shortest-path distances, BIG_NUM where unreachable), so the
+ * returned vector is identical; only the round count can be smaller. */
+static __device__ void wgm_app_pannotia_sssp(const wgm_launch &Lc, wgm_cta *c,
+                                      const wgm_psssp_args &a, wgm_warp_smem *sm) {
+  const int lane = wgm_lane(), warp = threadIdx.x >> 5;
+  const int nwarps_cta = blockDim.x >> 5;
+  const int gw = c->id * nwarps_cta + warp, NW = c->ngroups * nwarps_cta;
+  const int tid = c->id * blockDim.x + threadIdx.x, nth = c->ngroups * blockDim.x;
+  const int V = a.V;
+  for (int i = tid; i < V; i += nth) a.x[i] = (i == a.source) ? 0 : WGM_PANNOTIA_BIG;
+  if (c->id == 0 && threadIdx.x == 0)
+    for (int k = 0; k < 3; k++) a.stop[k * WGM_LINE] = 0;
+  if (!wgm_barrier(Lc, c)) return;
+  int r = 1;
+  for (;;) {
+    if (r > V + 2) { /* every round settles at least one vertex of a valid input */
+      wgm_fail(Lc, WGM_DEV_BAD_INPUT, WGM_SITE_QUEUE, r);
+      return;
+    }
+    if (c->id == 0 && threadIdx.x == 0) a.stop[((r + 1) % 3) * WGM_LINE] = 0;
+    bool changed = false;
+    for (int b = gw * 32; b < V; b += NW * 32) {
+      int i = b + lane, deg = 0, start = 0;
+      if (i < V) {
+        start = __ldg(&a.row[i]);
+        int d = __ldg(&a.row[i + 1]) - start;
+        deg = d > a.hub_threshold ? 0 : d;
+      }
+      sm->acc[warp][lane] = INT_MAX;
+      int incl = wgm_warp_incl_scan(deg);
+      int total = __shfl_sync(WGM_FULL, incl, 31);
+      int off = incl - deg;
+      __syncwarp();
+      wgm_for_each_edge(off, deg, start - off, total, 0, 32, sm->tab[warp],
+                        [&](bool valid, int e, int owner) {
+                          if (valid) {
+                            int cand = __ldg(&a.data[e]) + __ldcg(&a.x[__ldg(&a.col[e])]);
+                            atomicMin(&sm->acc[warp][owner], cand);
+                          }
+                        });
+      __syncwarp();
+      if (deg > 0) {
+        int cand = sm->acc[warp][lane];
+        if (cand < __ldcg(&a.x[i])) {
+          atomicMin(&a.x[i], cand);
+          changed = true;
+        }
+      }
+    }
+    int nwin = (a.hubs.total + 31) >> 5;
+    for (int k = gw; k < nwin; k += NW) {
+      wgm_hub_window(a.hubs, a.row, k, [&](bool valid, int h, int e) {
+        int h0 = __shfl_sync(WGM_FULL, h, 0);
+        int val = INT_MAX;
+        if (valid) val = __ldg(&a.data[e]) + __ldcg(&a.x[__ldg(&a.col[e])]);
+        int m0, m1;
+        float f0, f1;
+        wgm_two_seg_reduce(h == h0, val, 0.f, 1, &m0, &m1, &f0, &f1);
+        if (lane == 0) {
+          int v0 = __ldg(&a.hubs.ids[h0]);
+          if (m0 < __ldcg(&a.x[v0]) && atomicMin(&a.x[v0], m0) > m0) changed = true;
+          if (h0 + 1 < a.hubs.H && m1 != INT_MAX) {
+            int v1 = __ldg(&a.hubs.ids[h0 + 1]);
+            if (m1 < __ldcg(&a.x[v1]) && atomicMin(&a.x[v1], m1) > m1) changed = true;
+          }
+        }
+      });
+    }
+    if (__any_sync(WGM_FULL, changed) && lane == 0) a.stop[(r % 3) * WGM_LINE] = 1;
+    if (!wgm_barrier(Lc, c)) return;
+    if (__ldcg(&a.stop[(r % 3) * WGM_LINE]) == 0) break;
+    r++;
+  }
+  if (c->id == 0 && threadIdx.x == 0 && a.rounds_out) *a.rounds_out = r;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Pull PageRank (FP32; no reference implementation)                          */
+/* ------------------------------------------------------------------------ */
+
+struct wgm_pr_args {
+  int V;
+  const int *row;
+  const int *col;
+  float *pr;       /* [V] output */
+  float *contrib;  /* [2][V] pr/deg of the previous iteration */
+  float *dang;     /* [3 lines] dangling mass by iteration */
+  float *hub_sum;  /* [H] */
+  wgm_hubs hubs;
+  int hub_threshold;
+  int iterations;
+  float damping;
+};
+
+/* pr' = (1-d)/V + d*(sum_{u in N(v)} pr[u]/deg(u) + dangling/V); one barrier
+ * per iteration (two when hubs exist: hub sums accumulate over the grid and
+ * are finalised after the first).  Per-vertex sums run in a fixed order (a
+ * segmented warp scan per window), so only the dangling mass and hub sums
+ * depend on atomic order. */
+static __device__ void wgm_app_pagerank(const wgm_launch &Lc, wgm_cta *c, const wgm_pr_args &a,
+                                 wgm_warp_smem *sm) {
+  const int lane = wgm_lane(), warp = threadIdx.x >> 5;
+  const int nwarps_cta = blockDim.x >> 5;
+  const int gw = c->id * nwarps_cta + warp, NW = c->ngroups * nwarps_cta;
+  const int tid = c->id * blockDim.x + threadIdx.x, nth = c->ngroups * blockDim.x;
+  const int V = a.V;
+  const float d = a.damping;
+  float *acc = reinterpret_cast<float *>(sm->acc[warp]);
+  {
+    float dl = 0.f;
+    for (int i = tid; i < V; i += nth) {
+      int deg = __ldg(&a.row[i + 1]) - __ldg(&a.row[i]);
+      float p = 1.0f / (float)V;
+      a.contrib[i] = deg > 0 ? p / (float)deg : 0.f;
+      if (deg == 0) dl += p;
+    }
+    for (int h = tid; h < a.hubs.H; h += nth) a.hub_sum[h] = 0.f;
+    if (c->id == 0 && threadIdx.x == 0)
+      for (int k = 0; k < 3; k++) a.dang[k * WGM_LINE] = 0.f;
+    if (!wgm_barrier(Lc, c)) return;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) dl += __shfl_xor_sync(WGM_FULL, dl, o);
+    if (lane == 0 && dl != 0.f) atomicAdd(&a.dang[0], dl);
+    if (!wgm_barrier(Lc, c)) return;
+  }
+  for (int t = 0; t < a.iterations; t++) {
+    const float *cin = a.contrib + (size_t)(t & 1) * V;
+    float *cout = a.contrib + (size_t)((t + 1) & 1) * V;
+    const float base = (1.0f - d) / (float)V + d * __ldcg(&a.dang[(t % 3) * WGM_LINE]) / (float)V;
+    if (c->id == 0 && threadIdx.x == 0) a.dang[((t + 2) % 3) * WGM_LINE] = 0.f;
+    float dl = 0.f;
+    for (int b = gw * 32; b < V; b += NW * 32) {
+      int i = b + lane, deg = 0, start = 0, dfull = 0;
+      if (i < V) {
+        start = __ldg(&a.row[i]);
+        dfull = __ldg(&a.row[i + 1]) - start;
+        deg = dfull > a.hub_threshold ? 0 : dfull;
+      }
+      acc[lane] = 0.f;
+      int incl = wgm_warp_incl_scan(deg);
+      int total = __shfl_sync(WGM_FULL, incl, 31);
+      int off = incl - deg;
+      __syncwarp();
+      wgm_for_each_edge(off, deg, start - off, total, 0, 32, sm->tab[warp],
+                        [&](bool valid, int e, int owner) {
+                          float v = valid ? __ldcg(&cin[__ldg(&a.col[e])]) : 0.f;
+                          /* segmented inclusive scan over lanes with equal owner */
+                          int own = valid ? owner : -1;
+#pragma unroll
+                          for (int o = 1; o < 32; o <<= 1) {
+                            float y = __shfl_up_sync(WGM_FULL, v, o);
+                            int oy = __shfl_up_sync(WGM_FULL, own, o);
+                            if (lane >= o && oy == own) v += y;
+                          }
+                          int nxt = __shfl_down_sync(WGM_FULL, own, 1);
+                          if (own >= 0 && (lane == 31 || nxt != own)) acc[own] += v;
+                          __syncwarp();
+                        });
+      __syncwarp();
+      if (i < V && dfull <= a.hub_threshold) {
+        float p = base + d * acc[lane];
+        a.pr[i] = p;
+        cout[i] = dfull > 0 ? p / (float)dfull : 0.f;
+        if (dfull == 0) dl += p;
+      }
+    }
+    int nwin = (a.hubs.total + 31) >> 5;
+    for (int k = gw; k < nwin; k += NW) {
+      wgm_hub_window(a.hubs, a.row, k, [&](bool valid, int h, int e) {
+        int h0 = __shfl_sync(WGM_FULL, h, 0);
+        float v = valid ? __ldcg(&cin[__ldg(&a.col[e])]) : 0.f;
+        int m0, m1;
+        float f0, f1;
+        wgm_two_seg_reduce(h == h0, 0, v, 2, &m0, &m1, &f0, &f1);
+        if (lane == 0) {
+          atomicAdd(&a.hub_sum[h0], f0);
+          if (h0 + 1 < a.hubs.H && f1 != 0.f) atomicAdd(&a.hub_sum[h0 + 1], f1);
+        }
+      });
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) dl += __shfl_xor_sync(WGM_FULL, dl, o);
+    if (lane == 0 && dl != 0.f) atomicAdd(&a.dang[((t + 1) % 3) * WGM_LINE], dl);
+    if (!wgm_barrier(Lc, c)) return;
+    if (a.hubs.H > 0) {
+      for (int h = tid; h < a.hubs.H; h += nth) {
+        int v = __ldg(&a.hubs.ids[h]);
+        int dg = __ldg(&a.row[v + 1]) - __ldg(&a.row[v]);
+        float p = base + d * __ldcg(&a.hub_sum[h]);
+        a.pr[v] = p;
+        cout[v] = p / (float)dg;
+        a.hub_sum[h] = 0.f;
+      }
+      if (!wgm_barrier(Lc, c)) return;
+    }
+  }
+}
+
+#endif

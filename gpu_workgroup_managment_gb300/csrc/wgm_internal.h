@@ -1,0 +1,70 @@
+/*
+ * Internal host-side structures of libwgm (not part of the C-ABI).
+ */
+#ifndef WGM_INTERNAL_H
+#define WGM_INTERNAL_H
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <vector>
+
+#include "../../include/wgm.h"
+#include "wgm_common.h"
+#include "wgm_device.cuh"
+
+struct wgm_runtime {
+  wgm_config cfg{};
+  int device = -1;
+  cudaDeviceProp prop{};
+  cudaStream_t stream = nullptr;
+  wgm_dev_state *st = nullptr;        /* device */
+  wgm_host_flags *hf = nullptr;       /* mapped pinned host memory */
+  wgm_host_flags *hf_dev = nullptr;   /* its device alias */
+  char *d_scratch = nullptr;          /* 64 bytes of small kernel outputs */
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t tev0 = nullptr, tev1 = nullptr; /* wgm_timer_* */
+  int gen = 1;                        /* launch generation */
+  int last_cuda = 0;
+};
+
+/* Static hub layout on the device (see wgm_hubs in wgm_graph.cuh). */
+struct wgm_dev_hubs {
+  int *ids = nullptr, *prefix = nullptr, *wmap = nullptr;
+  int H = 0, total = 0;
+};
+
+struct wgm_app {
+  wgm_runtime *rt = nullptr;
+  int kind = 0;
+  int V = 0;
+  int64_t E = 0;
+  int hub_threshold = 256;
+  /* graph */
+  int *d_row = nullptr, *d_col = nullptr;
+  uint32_t *d_wt = nullptr; /* Lonestar SSSP weights / Pannotia SSSP data */
+  float *d_node_value = nullptr;
+  wgm_dev_hubs hubs;
+  /* outputs and scratch */
+  void *d_out = nullptr;
+  size_t out_bytes = 0;
+  int *d_wl = nullptr, *d_cnt = nullptr, *d_stamp = nullptr, *d_stop = nullptr;
+  int *d_hub_acc = nullptr, *d_status = nullptr;
+  float *d_contrib = nullptr, *d_dang = nullptr, *d_hub_sum = nullptr;
+  int *d_rounds = nullptr;
+  int source = 0;
+  float damping = 0.85f;
+  int iterations = 20;
+  bool has_node_values = false;
+};
+
+int wgm_cuda_fail(wgm_runtime *rt, cudaError_t e);
+wgm_launch wgm_make_launch(wgm_runtime *rt, int grid, int handshake, int im_exit);
+int wgm_hw_bound_for(wgm_runtime *rt, int kid, int block, int *groups);
+int wgm_status_from_device(int dev);
+int wgm_finish_launch(wgm_runtime *rt, int *dev_status, int *dev_site);
+bool wgm_host_wait(const volatile int32_t *p, int want, bool equal, uint64_t timeout_ns);
+int wgm_kind_to_kernel(int app_kind);
+int wgm_stream_wait(wgm_runtime *rt, cudaStream_t stream);
+
+#endif

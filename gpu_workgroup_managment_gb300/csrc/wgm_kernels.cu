@@ -1,0 +1,120 @@
+/*
+ * Standalone persistent kernels (one per app) and the barrier
+ * microbenchmark, compiled for sm_103a.
+ */
+#include "wgm_kernels.cuh"
+
+#define WGM_PERSISTENT_PROLOGUE                                  \
+  __shared__ wgm_cta c;                                          \
+  __shared__ wgm_warp_smem sm;                                   \
+  if (!wgm_discover(L, &c)) return;                              \
+  if (L.handshake && !wgm_standalone_handshake(L, &c)) {         \
+    wgm_standalone_exit(L);                                      \
+    return;                                                      \
+  }
+
+#define WGM_PERSISTENT_EPILOGUE \
+  if (L.handshake) wgm_standalone_exit(L);
+
+__global__ void __launch_bounds__(1024) wgm_k_bfs(wgm_launch L, wgm_lonestar_args a) {
+  WGM_PERSISTENT_PROLOGUE
+  wgm_app_lonestar<false>(L, &c, a, &sm);
+  WGM_PERSISTENT_EPILOGUE
+}
+
+__global__ void __launch_bounds__(1024) wgm_k_sssp(wgm_launch L, wgm_lonestar_args a) {
+  WGM_PERSISTENT_PROLOGUE
+  wgm_app_lonestar<true>(L, &c, a, &sm);
+  WGM_PERSISTENT_EPILOGUE
+}
+
+__global__ void __launch_bounds__(1024) wgm_k_color(wgm_launch L, wgm_color_args a) {
+  WGM_PERSISTENT_PROLOGUE
+  wgm_app_color(L, &c, a, &sm);
+  WGM_PERSISTENT_EPILOGUE
+}
+
+__global__ void __launch_bounds__(1024) wgm_k_mis(wgm_launch L, wgm_mis_args a) {
+  WGM_PERSISTENT_PROLOGUE
+  wgm_app_mis(L, &c, a, &sm);
+  WGM_PERSISTENT_EPILOGUE
+}
+
+__global__ void __launch_bounds__(1024) wgm_k_psssp(wgm_launch L, wgm_psssp_args a) {
+  WGM_PERSISTENT_PROLOGUE
+  wgm_app_pannotia_sssp(L, &c, a, &sm);
+  WGM_PERSISTENT_EPILOGUE
+}
+
+__global__ void __launch_bounds__(1024) wgm_k_pagerank(wgm_launch L, wgm_pr_args a) {
+  WGM_PERSISTENT_PROLOGUE
+  wgm_app_pagerank(L, &c, a, &sm);
+  WGM_PERSISTENT_EPILOGUE
+}
+
+/* os_freq (test_suite/os_freq/device/os_freq.cl:8-46): discovery, then
+ * num_iterations x 10 barriers over every discovered CTA. */
+__global__ void __launch_bounds__(1024) wgm_k_barrier_bench(wgm_launch L,
+                                                            wgm_barrier_bench_args a) {
+  __shared__ wgm_cta c;
+  if (!wgm_discover(L, &c)) return;
+  unsigned long long t0 = 0;
+  for (int i = 0; i < a.iterations; i++) {
+    for (int j = 0; j < 10; j++) {
+      if (!wgm_barrier(L, &c)) return;
+      if (i == 0 && j == 0) t0 = wgm_globaltimer();
+    }
+  }
+  if (c.id == 0 && threadIdx.x == 0) {
+    *a.t_first = t0;
+    *a.t_last = wgm_globaltimer();
+    *a.groups_out = c.ngroups;
+  }
+}
+
+const void *wgm_kernel_fn(int kid) {
+  switch (kid) {
+    case WGM_K_BFS: return (const void *)wgm_k_bfs;
+    case WGM_K_SSSP: return (const void *)wgm_k_sssp;
+    case WGM_K_COLOR: return (const void *)wgm_k_color;
+    case WGM_K_MIS: return (const void *)wgm_k_mis;
+    case WGM_K_PSSSP: return (const void *)wgm_k_psssp;
+    case WGM_K_PAGERANK: return (const void *)wgm_k_pagerank;
+    case WGM_K_BARRIER_BENCH: return (const void *)wgm_k_barrier_bench;
+    default: return nullptr;
+  }
+}
+
+cudaError_t wgm_launch_lonestar(bool sssp, const wgm_launch &L, const wgm_lonestar_args &a,
+                                int grid, int block, cudaStream_t s) {
+  if (sssp)
+    wgm_k_sssp<<<grid, block, 0, s>>>(L, a);
+  else
+    wgm_k_bfs<<<grid, block, 0, s>>>(L, a);
+  return cudaGetLastError();
+}
+cudaError_t wgm_launch_color(const wgm_launch &L, const wgm_color_args &a, int grid, int block,
+                             cudaStream_t s) {
+  wgm_k_color<<<grid, block, 0, s>>>(L, a);
+  return cudaGetLastError();
+}
+cudaError_t wgm_launch_mis(const wgm_launch &L, const wgm_mis_args &a, int grid, int block,
+                           cudaStream_t s) {
+  wgm_k_mis<<<grid, block, 0, s>>>(L, a);
+  return cudaGetLastError();
+}
+cudaError_t wgm_launch_psssp(const wgm_launch &L, const wgm_psssp_args &a, int grid, int block,
+                             cudaStream_t s) {
+  wgm_k_psssp<<<grid, block, 0, s>>>(L, a);
+  return cudaGetLastError();
+}
+cudaError_t wgm_launch_pagerank(const wgm_launch &L, const wgm_pr_args &a, int grid, int block,
+                                cudaStream_t s) {
+  wgm_k_pagerank<<<grid, block, 0, s>>>(L, a);
+  return cudaGetLastError();
+}
+cudaError_t wgm_launch_barrier_bench(const wgm_launch &L, const wgm_barrier_bench_args &a,
+                                     int grid, int block, cudaStream_t s) {
+  wgm_k_barrier_bench<<<grid, block, 0, s>>>(L, a);
+  return cudaGetLastError();
+}

@@ -1,0 +1,50 @@
+/*
+ * Kernel entry points of the standalone persistent form and their host-side
+ * launch helpers (internal to libwgm; the public C-ABI is include/wgm.h).
+ *
+ * Every persistent kernel has the reference's standalone shape
+ * (lonestar/graph_apps/bfs/device/standalone.cl:247-320): discovery, optional
+ * host handshake, the app's barrier-synchronised loop, and a persistent_flag
+ * decrement per group when the host handshake is on.
+ */
+#ifndef WGM_KERNELS_CUH
+#define WGM_KERNELS_CUH
+
+#include <cuda_runtime.h>
+
+#include "wgm_graph.cuh"
+
+enum wgm_kernel_id {
+  WGM_K_BFS = 0,
+  WGM_K_SSSP,
+  WGM_K_COLOR,
+  WGM_K_MIS,
+  WGM_K_PSSSP,
+  WGM_K_PAGERANK,
+  WGM_K_BARRIER_BENCH,
+  WGM_K_COUNT
+};
+
+struct wgm_barrier_bench_args {
+  int iterations;              /* os_freq.cl:35: num_iterations x 10 barriers */
+  int *groups_out;
+  unsigned long long *t_first; /* %globaltimer after the first barrier */
+  unsigned long long *t_last;  /* %globaltimer after the last barrier */
+};
+
+/* Host helpers (wgm_kernels.cu). */
+const void *wgm_kernel_fn(int kid);
+cudaError_t wgm_launch_lonestar(bool sssp, const wgm_launch &L, const wgm_lonestar_args &a,
+                                int grid, int block, cudaStream_t s);
+cudaError_t wgm_launch_color(const wgm_launch &L, const wgm_color_args &a, int grid, int block,
+                             cudaStream_t s);
+cudaError_t wgm_launch_mis(const wgm_launch &L, const wgm_mis_args &a, int grid, int block,
+                           cudaStream_t s);
+cudaError_t wgm_launch_psssp(const wgm_launch &L, const wgm_psssp_args &a, int grid, int block,
+                             cudaStream_t s);
+cudaError_t wgm_launch_pagerank(const wgm_launch &L, const wgm_pr_args &a, int grid, int block,
+                                cudaStream_t s);
+cudaError_t wgm_launch_barrier_bench(const wgm_launch &L, const wgm_barrier_bench_args &a,
+                                     int grid, int block, cudaStream_t s);
+
+#endif

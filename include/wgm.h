@@ -1,0 +1,200 @@
+/*
+ * wgm.h - C-ABI of the GB300 cooperative-kernel runtime (libwgm.so).
+ *
+ * Drop-in boundary for the reference's persistent path (reference paths are
+ * relative to the reference project):
+ *   - host runtime:  src/scheduler_rt/rt_host/cl_scheduler.h:7-88,
+ *                    src/scheduler_rt/rt_host/discovery.h:6-29,
+ *                    src/scheduler_rt/rt_host/cl_communicator.h:19-465,
+ *                    src/host_skeleton/skel.cpp:127-240 (reset/occupancy helpers);
+ *   - app plugins:   src/lonestar/graph_apps/{bfs,sssp}/*.h,
+ *                    src/pannotia/graph_apps/{color,mis,sssp}/*.h,
+ *                    src/non_persistent_kernels/{matmult,reduce}/*.h;
+ *   - microbenchmark: src/test_suite/os_freq/host/os_freq.cpp:274-330.
+ * Each declaration names the reference interface it replaces.
+ *
+ * Conventions: every call returns an int status (WGM_OK or a negative
+ * WGM_ERR_*); nothing calls exit().  Pointers are host pointers unless the
+ * name says _device.  A runtime object may be used from one thread at a time,
+ * except wgm_comm_* calls which are internally locked.
+ */
+#ifndef WGM_H
+#define WGM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (the reference calls exit(1) instead: rt_host/ggc_ocl.h:11-18) */
+#define WGM_OK 0
+#define WGM_ERR_INVALID (-1)
+#define WGM_ERR_TOO_MANY_GROUPS (-2) /* cl_communicator.h:125-130,209-214 */
+#define WGM_ERR_TIMEOUT (-3)
+#define WGM_ERR_OOM (-4)
+#define WGM_ERR_CUDA (-5)
+#define WGM_ERR_OVERFLOW (-6)
+#define WGM_ERR_NO_DEVICE (-7)
+#define WGM_ERR_ABORTED (-8)
+#define WGM_ERR_STATE (-9)
+
+/* ---- discovery / barrier flavours */
+#define WGM_DISCOVERY_TICKET 0
+#define WGM_DISCOVERY_REFERENCE 1
+#define WGM_BARRIER_SENSE 0
+#define WGM_BARRIER_XF 1
+#define WGM_BARRIER_TREE 2
+
+/* ---- persistent apps (the reference selects them by macro, skel.cpp:50-77) */
+#define WGM_APP_LONESTAR_BFS 1
+#define WGM_APP_LONESTAR_SSSP 2
+#define WGM_APP_PANNOTIA_COLOR 3
+#define WGM_APP_PANNOTIA_MIS 4
+#define WGM_APP_PANNOTIA_SSSP 5
+#define WGM_APP_PAGERANK 6
+
+typedef struct wgm_runtime wgm_runtime;
+typedef struct wgm_app wgm_app;
+typedef struct wgm_host_graph wgm_host_graph;
+
+/* Runtime configuration: the reference's gflags of skel.cpp:21-44 that apply
+ * to the persistent path, plus the GB300 knobs. */
+typedef struct wgm_config {
+  int device;
+  int threads_per_wg;          /* skel.cpp:39 */
+  int num_wgs;                 /* skel.cpp:40; <=0: every co-resident CTA */
+  int use_query_barrier;       /* skel.cpp:34 */
+  int non_persistent_wgs;      /* skel.cpp:30 */
+  int non_persistent_frequency_ms; /* skel.cpp:32 */
+  int skip_tasks;              /* skel.cpp:31 */
+  int host_handshake;          /* standalone.cl:277-289 handshake on/off */
+  int discovery_mode;          /* WGM_DISCOVERY_* */
+  int discovery_extra_rounds;  /* discovery.cl:43 (reference mode) */
+  int barrier_kind;            /* WGM_BARRIER_* */
+  int tree_fanin;              /* groups per leaf of WGM_BARRIER_TREE */
+  int hub_threshold;           /* degree above which edges spread grid-wide */
+  uint64_t spin_timeout_ns;    /* budget of every device wait */
+  uint64_t run_timeout_ns;     /* host budget of one blocking run; then abort */
+  uint64_t discovery_window_ns;/* ticket discovery closing window */
+} wgm_config;
+
+/* Statistics of one persistent run (skel.cpp:346-354 records time, error and
+ * occupancy per iteration). */
+typedef struct wgm_run_stats {
+  int groups;          /* discovered groups that ran the task */
+  int rounds;          /* levels / rounds / iterations executed */
+  int device_status;   /* 0, or the first device-side failure */
+  int device_site;     /* which wait failed */
+  double kernel_ms;    /* CUDA-event time of the launch */
+  double host_ms;      /* host handshake time (skel.cpp:337-340), 0 without it */
+} wgm_run_stats;
+
+/* Host CSR (0-based): row_ptr[num_nodes+1], col[row_ptr[num_nodes]]. */
+typedef struct wgm_graph_desc {
+  int32_t num_nodes;
+  int64_t num_edges;        /* entries in col/weights */
+  const int32_t *row_ptr;
+  const int32_t *col;
+  const uint32_t *weights;  /* may be NULL */
+} wgm_graph_desc;
+
+/* ---- runtime ----------------------------------------------------------- */
+void wgm_config_default(wgm_config *cfg);
+const char *wgm_status_string(int status);
+/* Replaces mk_init_scheduler_ctx + mk_init_discovery_ctx + the IW_barrier
+ * buffer setup (rt_host/cl_scheduler.h:7-33, rt_host/discovery.h:6-16,
+ * skel.cpp:278-295). */
+int wgm_runtime_create(const wgm_config *cfg, wgm_runtime **out);
+/* Replaces free_scheduler_ctx (rt_host/cl_scheduler.h:52-63). */
+int wgm_runtime_destroy(wgm_runtime *rt);
+/* Replaces restart_scheduler + reset_barrier + reset_discovery
+ * (rt_host/cl_scheduler.h:35-50, skel.cpp:127-155). */
+int wgm_reset(wgm_runtime *rt);
+int wgm_last_cuda_error(const wgm_runtime *rt);
+/* First device-side failure recorded since the last reset (no reference
+ * counterpart: the reference spins forever). */
+int wgm_device_status(const wgm_runtime *rt, int *status, int *site, int *detail);
+/* Raise/clear the host abort word every device wait polls. */
+int wgm_set_abort(wgm_runtime *rt, int value);
+int wgm_sm_count(const wgm_runtime *rt, int *sms);
+
+/* ---- discovery --------------------------------------------------------- */
+/* Replaces get_occupancy_d_ctx (skel.cpp:223-240) and
+ * CL_Communicator::get_occupancy_bound (cl_communicator.h:350-374): launches
+ * the discovery protocol in occupancy-only mode (mk_init_discovery_ctx_occupancy,
+ * rt_host/discovery.h:18-29) and returns the number of co-resident groups. */
+int wgm_get_occupancy_bound(wgm_runtime *rt, int threads_per_wg, int *groups);
+/* Hardware bound: cudaOccupancyMaxActiveBlocksPerMultiprocessor x SMs for the
+ * given app's kernel (no reference counterpart). */
+int wgm_hw_occupancy_bound(wgm_runtime *rt, int app_kind, int threads_per_wg, int *groups);
+
+/* ---- barrier microbenchmark (os_freq.cpp:280-330 / os_freq.cl:8-46) ---- */
+int wgm_barrier_bench(wgm_runtime *rt, int threads_per_wg, int num_wgs, int iterations,
+                      int barrier_kind, double *ns_per_barrier, double *kernel_ms,
+                      int *groups);
+
+/* ---- persistent app plugins -------------------------------------------- */
+/* persistent_app_name / persistent_kernel_name (e.g. bfs.h:192-198). */
+const char *wgm_persistent_app_name(int app_kind);
+const char *wgm_persistent_kernel_name(int app_kind);
+/* init_persistent_app_for_occupancy (e.g. bfs.h:209-282, color.h:41-81):
+ * allocates device buffers and uploads the graph. */
+int wgm_app_create(wgm_runtime *rt, int app_kind, const wgm_graph_desc *g, wgm_app **out);
+/* Re-upload a graph with the same node and edge counts (reset_persistent_task
+ * re-writes the graph buffers, bfs.h:284-313). */
+int wgm_app_upload(wgm_app *app, const wgm_graph_desc *g);
+/* Source vertex (the reference hard-wires 0: bfs.cl:236-240, pannotia sssp.h:21). */
+int wgm_app_set_source(wgm_app *app, int32_t source);
+/* Colour/MIS priorities node_value[V] (color.h:49-55, mis.h:52-56). */
+int wgm_app_set_node_values(wgm_app *app, const float *node_value);
+int wgm_app_set_pagerank(wgm_app *app, float damping, int iterations);
+/* One iteration of run_persistent (skel.cpp:316-355): launch the persistent
+ * kernel on up to num_wgs groups (<=0: all co-resident) and wait. */
+int wgm_run_persistent(wgm_runtime *rt, wgm_app *app, int num_wgs, wgm_run_stats *stats);
+/* Asynchronous launch on a caller stream (cudaStream_t; NULL = the runtime's
+ * stream).  With cfg.host_handshake set the kernel waits for
+ * DEVICE_TO_PERSISTENT_TASK like the reference's standalone kernel, and
+ * nothing here sends it: the wait runs out after spin_timeout_ns and the
+ * launch ends with WGM_ERR_TIMEOUT (used to test the timeout path). */
+int wgm_launch_persistent(wgm_runtime *rt, wgm_app *app, int num_wgs, void *stream);
+/* Wait (bounded by run_timeout_ns, then abort) for everything queued on the
+ * runtime's stream and report the first device-side failure. */
+int wgm_synchronize(wgm_runtime *rt);
+/* check_persistent_task's read-back (bfs.h:367-370): dist (uint32) for the
+ * Lonestar apps, colours / s_array / cost (int32) for Pannotia, pr (float). */
+int wgm_app_read_result(wgm_app *app, void *host_out, size_t bytes);
+int wgm_app_result_device_ptr(wgm_app *app, void **device_ptr, size_t *bytes);
+int wgm_app_rounds(wgm_app *app, int *rounds);
+/* clean_persistent_task (bfs.h:330-334). */
+int wgm_app_destroy(wgm_app *app);
+
+/* ---- device timing on the runtime's stream (CUDA events) --------------- */
+/* os_freq.cpp:311-328 reads CL profiling events; here a pair of CUDA events
+ * brackets everything queued on the runtime's stream in between. */
+int wgm_timer_start(wgm_runtime *rt);
+int wgm_timer_stop(wgm_runtime *rt, double *elapsed_ms);
+
+/* ---- host memory helpers (pinned, for H2D/D2H at full bandwidth) ------- */
+void *wgm_host_alloc(size_t bytes);
+void wgm_host_free(void *p);
+
+/* ---- synthetic inputs (the reference reads them from files) ------------ */
+/* 4-connected rows x cols grid, node id r*cols+c, neighbours in
+ * (up, left, right, down) order.  row_ptr[rows*cols+1], col[...]. */
+int wgm_gen_grid(int32_t rows, int32_t cols, int32_t *row_ptr, int32_t *col, int64_t *num_edges);
+/* RMAT (scale, edge factor, a, b, c), symmetrised, self loops and
+ * duplicates removed, rows sorted; optional seeded relabelling; uint32
+ * weights uniform in [wmin, wmax] per undirected edge when wmax > 0. */
+int wgm_gen_rmat(int scale, int edge_factor, double a, double b, double c, uint64_t seed,
+                 int permute, uint32_t wmin, uint32_t wmax, wgm_host_graph **out);
+int wgm_host_graph_info(const wgm_host_graph *g, int32_t *num_nodes, int64_t *num_edges);
+int wgm_host_graph_arrays(const wgm_host_graph *g, const int32_t **row_ptr,
+                          const int32_t **col, const uint32_t **weights);
+void wgm_host_graph_free(wgm_host_graph *g);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,250 @@
+"""Python access to the CPU oracle (liboracle.so) and to the reference's own
+kernels compiled under the one-work-group shim (oracle/_ref/libref_*.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline / reference arms, always as the checker or the timed
+CPU baseline, never on the product path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liboracle.so")
+REF_DIR = os.path.join(HERE, "_ref")
+
+
+def build(force: bool = False) -> str:
+    src = os.path.join(HERE, "wgm_oracle.c")
+    if force or not os.path.exists(LIB) or os.path.getmtime(src) > os.path.getmtime(LIB):
+        tmp = LIB + ".tmp"
+        subprocess.run(["gcc", "-O2", "-fPIC", "-fopenmp", "-shared", "-o", tmp, src],
+                       check=True)
+        os.replace(tmp, LIB)
+    return LIB
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        build()
+        _lib = C.CDLL(LIB)
+        P, I = C.c_void_p, C.c_int32
+        protos = {
+            "oracle_lonestar_bfs": [I, P, P, I, P],
+            "oracle_lonestar_sssp": [I, P, P, P, I, P],
+            "oracle_pannotia_color": [I, P, P, P, P],
+            "oracle_pannotia_mis": [I, P, P, P, P],
+            "oracle_pannotia_sssp": [I, P, P, P, I, P],
+            "oracle_lonestar_bfs_omp": [I, P, P, I, P, P],
+            "oracle_lonestar_sssp_omp": [I, P, P, P, I, P, P],
+            "oracle_pannotia_color_omp": [I, P, P, P, P, P],
+            "oracle_pannotia_mis_omp": [I, P, P, P, P, P, P],
+            "oracle_omp_threads": [],
+            "oracle_matmult_rand_fill": [P, I, I, I],
+            "oracle_matmult_i32": [P, I, I, P, I, P],
+            "oracle_hash_diag": [P, I, I],
+            "oracle_matmult_f32": [P, I, I, P, I, P],
+        }
+        for name, args in protos.items():
+            fn = getattr(_lib, name)
+            fn.argtypes = args
+            fn.restype = C.c_int
+        _lib.oracle_hash_diag.restype = C.c_int32
+        _lib.oracle_matmult_rand_fill.restype = C.c_int32
+        _lib.oracle_reduce_min_i32.restype = C.c_int32
+        _lib.oracle_reduce_min_f32.restype = C.c_float
+        _lib.oracle_pagerank_f64.argtypes = [C.c_int32, C.c_void_p, C.c_void_p, C.c_double,
+                                             C.c_int, C.c_void_p]
+        _lib.oracle_pagerank_f32_omp.argtypes = [C.c_int32, C.c_void_p, C.c_void_p, C.c_float,
+                                                 C.c_int, C.c_void_p, C.c_void_p]
+        _lib.oracle_reduce_min_i32.argtypes = [C.c_void_p, C.c_int64]
+        _lib.oracle_reduce_min_f32.argtypes = [C.c_void_p, C.c_int64]
+    return _lib
+
+
+def _p(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+def threads() -> int:
+    return lib().oracle_omp_threads()
+
+
+def lonestar_bfs(g, source: int = 0, omp: bool = False) -> np.ndarray:
+    V = g.num_nodes
+    d = np.empty(V, np.uint32)
+    if omp:
+        scratch = np.empty(2 * V, np.int32)
+        lib().oracle_lonestar_bfs_omp(V, _p(g.row_ptr), _p(g.col), source, _p(d), _p(scratch))
+    else:
+        lib().oracle_lonestar_bfs(V, _p(g.row_ptr), _p(g.col), source, _p(d))
+    return d
+
+
+def lonestar_sssp(g, source: int = 0, omp: bool = False) -> np.ndarray:
+    V = g.num_nodes
+    d = np.empty(V, np.uint32)
+    if omp:
+        scratch = np.empty(3 * V, np.int32)
+        lib().oracle_lonestar_sssp_omp(V, _p(g.row_ptr), _p(g.col), _p(g.weights), source, _p(d),
+                                       _p(scratch))
+    else:
+        lib().oracle_lonestar_sssp(V, _p(g.row_ptr), _p(g.col), _p(g.weights), source, _p(d))
+    return d
+
+
+def color(g, node_value: np.ndarray, omp: bool = False) -> np.ndarray:
+    V = g.num_nodes
+    out = np.empty(V, np.int32)
+    nv = np.ascontiguousarray(node_value, np.float32)
+    if omp:
+        md = np.empty(V, np.float32)
+        lib().oracle_pannotia_color_omp(V, _p(g.row_ptr), _p(g.col), _p(nv), _p(out), _p(md))
+    else:
+        lib().oracle_pannotia_color(V, _p(g.row_ptr), _p(g.col), _p(nv), _p(out))
+    return out
+
+
+def mis(g, node_value: np.ndarray, omp: bool = False) -> np.ndarray:
+    V = g.num_nodes
+    out = np.empty(V, np.int32)
+    nv = np.ascontiguousarray(node_value, np.float32)
+    if omp:
+        scratch = np.empty(2 * V, np.int32)
+        mn = np.empty(V, np.float32)
+        lib().oracle_pannotia_mis_omp(V, _p(g.row_ptr), _p(g.col), _p(nv), _p(out), _p(scratch),
+                                      _p(mn))
+    else:
+        lib().oracle_pannotia_mis(V, _p(g.row_ptr), _p(g.col), _p(nv), _p(out))
+    return out
+
+
+def pannotia_sssp(g, source: int = 0) -> np.ndarray:
+    V = g.num_nodes
+    out = np.empty(V, np.int32)
+    data = np.ascontiguousarray(g.weights.view(np.int32))
+    lib().oracle_pannotia_sssp(V, _p(g.row_ptr), _p(g.col), _p(data), source, _p(out))
+    return out
+
+
+def pagerank_f64(g, damping: float = 0.85, iterations: int = 20) -> np.ndarray:
+    pr = np.empty(g.num_nodes, np.float64)
+    lib().oracle_pagerank_f64(g.num_nodes, _p(g.row_ptr), _p(g.col), damping, iterations, _p(pr))
+    return pr
+
+
+def pagerank_f32_omp(g, damping: float = 0.85, iterations: int = 20) -> np.ndarray:
+    V = g.num_nodes
+    pr = np.empty(V, np.float32)
+    scratch = np.empty(2 * V, np.float32)
+    lib().oracle_pagerank_f32_omp(V, _p(g.row_ptr), _p(g.col), damping, iterations, _p(pr),
+                                  _p(scratch))
+    return pr
+
+
+def matmult_inputs(n: int, seed: int = 1234) -> tuple[np.ndarray, np.ndarray]:
+    """matmult.h:163-203: A then B filled by the middle-square generator."""
+    A = np.empty((n, n), np.int32)
+    B = np.empty((n, n), np.int32)
+    s = lib().oracle_matmult_rand_fill(_p(A), n, n, seed)
+    lib().oracle_matmult_rand_fill(_p(B), n, n, s)
+    return A, B
+
+
+def matmult_i32(A: np.ndarray, B: np.ndarray) -> np.ndarray:
+    Cm = np.empty((A.shape[0], B.shape[1]), np.int32)
+    lib().oracle_matmult_i32(_p(A), A.shape[0], A.shape[1], _p(B), B.shape[1], _p(Cm))
+    return Cm
+
+
+def hash_diag(M: np.ndarray) -> int:
+    return int(lib().oracle_hash_diag(_p(np.ascontiguousarray(M, np.int32)), M.shape[0],
+                                      M.shape[1]))
+
+
+def reduce_min_i32(buf: np.ndarray) -> int:
+    return int(lib().oracle_reduce_min_i32(_p(buf), buf.shape[0]))
+
+
+# ---- the reference's own kernels under the shim (built by build_ref.py) ----
+
+def ref_available() -> bool:
+    return os.path.exists(os.path.join(REF_DIR, "libref_lonestar_bfs.so"))
+
+
+_REF_PROTOS = {
+    "ref_run_lonestar": [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int],
+    "ref_run_color": [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int],
+    "ref_run_mis": [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int],
+    "ref_run_pannotia_sssp": [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int],
+    "ref_run_matmult": [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p,
+                        C.c_int],
+    "ref_run_reduce": [C.c_void_p, C.c_int, C.c_int],
+}
+_ref_libs: dict = {}
+
+
+def _ref(name: str) -> C.CDLL:
+    if name not in _ref_libs:
+        lib_ = C.CDLL(os.path.join(REF_DIR, f"libref_{name}.so"))
+        for fn, args in _REF_PROTOS.items():
+            if hasattr(lib_, fn):
+                getattr(lib_, fn).argtypes = args
+                getattr(lib_, fn).restype = C.c_int
+        _ref_libs[name] = lib_
+    return _ref_libs[name]
+
+
+def ref_lonestar_bfs(g, wgs: int = 128) -> np.ndarray:
+    d = np.empty(g.num_nodes, np.uint32)
+    _ref("lonestar_bfs").ref_run_lonestar(g.num_nodes, _p(g.row_ptr), _p(g.col), None, _p(d), wgs)
+    return d
+
+
+def ref_lonestar_sssp(g, wgs: int = 128) -> np.ndarray:
+    d = np.empty(g.num_nodes, np.uint32)
+    _ref("lonestar_sssp").ref_run_lonestar(g.num_nodes, _p(g.row_ptr), _p(g.col), _p(g.weights),
+                                           _p(d), wgs)
+    return d
+
+
+def ref_color(g, node_value: np.ndarray, wgs: int = 128) -> np.ndarray:
+    out = np.empty(g.num_nodes, np.int32)
+    nv = np.ascontiguousarray(node_value, np.float32)
+    _ref("pannotia_color").ref_run_color(g.num_nodes, _p(g.row_ptr), _p(g.col), _p(nv), _p(out),
+                                         wgs)
+    return out
+
+
+def ref_mis(g, node_value: np.ndarray, wgs: int = 128) -> np.ndarray:
+    out = np.empty(g.num_nodes, np.int32)
+    nv = np.ascontiguousarray(node_value, np.float32)
+    _ref("pannotia_mis").ref_run_mis(g.num_nodes, _p(g.row_ptr), _p(g.col), _p(nv), _p(out), wgs)
+    return out
+
+
+def ref_pannotia_sssp(g, wgs: int = 128) -> np.ndarray:
+    out = np.empty(g.num_nodes, np.int32)
+    data = np.ascontiguousarray(g.weights.view(np.int32))
+    _ref("pannotia_sssp").ref_run_pannotia_sssp(g.num_nodes, _p(g.row_ptr), _p(g.col), _p(data),
+                                                _p(out), wgs)
+    return out
+
+
+def ref_matmult(A: np.ndarray, B: np.ndarray, wgs: int = 128) -> tuple[np.ndarray, int]:
+    Cm = np.empty((A.shape[0], B.shape[1]), np.int32)
+    h = _ref("matmult").ref_run_matmult(_p(A), A.shape[0], A.shape[1], _p(B), B.shape[0],
+                                        B.shape[1], _p(Cm), wgs)
+    return Cm, int(h)
+
+
+def ref_reduce(buf: np.ndarray, wgs: int = 256) -> int:
+    return int(_ref("reduce").ref_run_reduce(_p(buf), buf.shape[0], wgs))

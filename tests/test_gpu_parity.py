@@ -1,0 +1,238 @@
+"""GPU parity of the persistent kernels, through the C-ABI (libwgm.so).
+
+Bit-exact against (a) the golden fixtures the reference's own kernels
+produced, (b) the CPU oracle on seeded graphs, across barrier kinds,
+discovery modes, block sizes, grid sizes and hub thresholds, and (c) at the
+full sizes of the benchmark configurations, the OpenMP oracle plus
+size-independent properties (shortest-path optimality, independence and
+maximality).  PageRank: FP32 within 1e-5 relative L-inf (||x-x64||/||x64||)
+of the FP64 oracle.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from gpu_workgroup_managment_gb300 import PersistentApp, Runtime, WgmError, graphs
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+PR_TOL = 1e-5
+
+
+def _run(rt, app, g, **kw):
+    with PersistentApp(rt, app, g, **kw) as a:
+        st = a.run()
+        return a.result(), st
+
+
+@pytest.mark.parametrize("name", ["grid32", "rmat10", "ragged"])
+def test_golden_fixtures(rt, golden_dir, name):
+    z = np.load(os.path.join(golden_dir, f"{name}.npz"))
+    g = graphs.Graph(z["row_ptr"], z["col"], z["weights"])
+    lv = graphs.lonestar_view(g)
+    assert np.array_equal(_run(rt, "lonestar_bfs", lv)[0], z["bfs"])
+    assert np.array_equal(_run(rt, "lonestar_sssp", lv)[0], z["sssp"])
+    for tag in ("ref", "seed"):
+        nv = z[f"node_value_{tag}"]
+        assert np.array_equal(_run(rt, "color", g, node_values=nv)[0], z[f"color_{tag}"])
+        assert np.array_equal(_run(rt, "mis", g, node_values=nv)[0], z[f"mis_{tag}"])
+    assert np.array_equal(_run(rt, "sssp", g)[0], z["psssp"])
+
+
+def _all_apps_vs_oracle(rt, g, source, seed, num_wgs=0):
+    lv = graphs.lonestar_view(g)
+    nv = graphs.seeded_node_values(g.num_nodes, seed)
+    with PersistentApp(rt, "lonestar_bfs", lv, source=source) as a:
+        a.run(num_wgs)
+        assert np.array_equal(a.result(), oracle.lonestar_bfs(lv, source)), "bfs"
+    with PersistentApp(rt, "lonestar_sssp", lv, source=source) as a:
+        a.run(num_wgs)
+        assert np.array_equal(a.result(), oracle.lonestar_sssp(lv, source)), "sssp"
+    with PersistentApp(rt, "color", g, node_values=nv) as a:
+        a.run(num_wgs)
+        assert np.array_equal(a.result(), oracle.color(g, nv)), "color"
+    with PersistentApp(rt, "mis", g, node_values=nv) as a:
+        a.run(num_wgs)
+        assert np.array_equal(a.result(), oracle.mis(g, nv)), "mis"
+    with PersistentApp(rt, "sssp", g, source=source) as a:
+        a.run(num_wgs)
+        assert np.array_equal(a.result(), oracle.pannotia_sssp(g, source)), "pannotia sssp"
+    with PersistentApp(rt, "pagerank", g) as a:
+        a.run(num_wgs)
+        p64 = oracle.pagerank_f64(g)
+        err = np.max(np.abs(a.result().astype(np.float64) - p64)) / np.max(np.abs(p64))
+        assert err <= PR_TOL, f"pagerank rel Linf {err}"
+
+
+@pytest.mark.parametrize("seed", [1, 2])
+def test_rmat_all_apps(rt, seed):
+    g = graphs.rmat(14, 16, seed=seed)
+    _all_apps_vs_oracle(rt, g, graphs.max_degree_vertex(g), seed)
+
+
+def test_grid_all_apps(rt):
+    g = graphs.grid(96, 70)
+    g.weights = graphs.uniform_weights(g, seed=5)
+    _all_apps_vs_oracle(rt, g, 0, 3)
+
+
+@pytest.mark.parametrize("num_wgs", [1, 2, 7, 61])
+def test_few_groups(rt, num_wgs):
+    g = graphs.rmat(12, 8, seed=4)
+    _all_apps_vs_oracle(rt, g, graphs.max_degree_vertex(g), 4, num_wgs=num_wgs)
+
+
+@pytest.mark.parametrize("cfg", [
+    dict(barrier_kind=1), dict(barrier_kind=2), dict(barrier_kind=2, tree_fanin=3),
+    dict(discovery_mode=1, discovery_extra_rounds=2), dict(threads_per_wg=128),
+    dict(threads_per_wg=512), dict(threads_per_wg=1024), dict(hub_threshold=32),
+    dict(hub_threshold=100000), dict(host_handshake=1),
+])
+def test_runtime_variants(cfg):
+    g = graphs.rmat(13, 16, seed=9)
+    with Runtime(**cfg) as r:
+        _all_apps_vs_oracle(r, g, graphs.max_degree_vertex(g), 9)
+
+
+def test_star_and_edge_cases(rt):
+    # star: one hub with every other vertex as a leaf, plus isolated vertices
+    V = 3000
+    leaves = np.arange(1, 2500, dtype=np.int32)
+    rows = [leaves.tolist()] + [[0]] * 2499 + [[]] * (V - 2500)
+    rp = np.zeros(V + 1, np.int32)
+    rp[1:] = np.cumsum([len(r) for r in rows])
+    col = np.array([c for r in rows for c in r], np.int32)
+    g = graphs.Graph(rp, col, graphs.uniform_weights(graphs.Graph(rp, col), 1))
+    _all_apps_vs_oracle(rt, g, 0, 1)
+    _all_apps_vs_oracle(rt, g, 2999, 2)   # isolated source
+    _all_apps_vs_oracle(rt, g, 17, 3)     # leaf source
+
+
+def test_single_vertex(rt):
+    g = graphs.Graph(np.array([0, 0], np.int32), np.zeros(0, np.int32), np.zeros(0, np.uint32))
+    for app in ("lonestar_bfs", "lonestar_sssp", "color", "mis", "sssp", "pagerank"):
+        out, _ = _run(rt, app, g)
+        want = {"lonestar_bfs": 0, "lonestar_sssp": 0, "color": 1, "mis": 2, "sssp": 0,
+                "pagerank": 1.0}[app]
+        assert out[0] == pytest.approx(want), app
+
+
+def test_lonestar_quirk_isolated_last_vertex(rt):
+    # The last vertex has no edges: with the loader's psrc[V] = E its degree
+    # reads -1; the kernels walk nothing for it (like the reference's gather).
+    rows = [[1], [0, 2], [1], []]
+    rp = np.array([0, 1, 3, 4, 4], np.int32)
+    col = np.array([1, 0, 2, 1], np.int32)
+    g = graphs.Graph(rp, col, np.ones(4, np.uint32))
+    lv = graphs.lonestar_view(g)
+    assert lv.row_ptr[-1] == 3 and lv.row_ptr[-2] == 4
+    for src in range(4):
+        with PersistentApp(rt, "lonestar_bfs", lv, source=src) as a:
+            a.run()
+            assert np.array_equal(a.result(), oracle.lonestar_bfs(lv, src))
+
+
+def test_repeated_runs_and_reupload(rt):
+    g = graphs.rmat(12, 16, seed=11)
+    h = graphs.rmat(12, 16, seed=12)
+    lv = graphs.lonestar_view(g)
+    with PersistentApp(rt, "lonestar_bfs", lv, source=3) as a:
+        first = None
+        for _ in range(5):
+            a.run()
+            r = a.result()
+            first = r if first is None else first
+            assert np.array_equal(r, first)
+        if h.num_edges == g.num_edges:
+            a.upload(graphs.lonestar_view(h))
+            a.run()
+            assert np.array_equal(a.result(), oracle.lonestar_bfs(graphs.lonestar_view(h), 3))
+
+
+def test_c1_grid_256_bfs_full_size(rt):
+    """Configuration 1: 256x256 grid, source 0, bit-exact levels."""
+    g = graphs.lonestar_view(graphs.grid(256, 256))
+    with PersistentApp(rt, "lonestar_bfs", g) as a:
+        st = a.run()
+        d = a.result()
+    assert np.array_equal(d, oracle.lonestar_bfs(g, 0))
+    assert d.max() == 510 and st.groups > 0
+
+
+@pytest.fixture(scope="module")
+def rmat20():
+    g = graphs.rmat(20, 16, seed=1)
+    return g, graphs.max_degree_vertex(g)
+
+
+def _check_sssp_optimal(g, src, dist, inf):
+    V = g.num_nodes
+    s = np.repeat(np.arange(V), g.degrees())
+    d = dist.astype(np.int64)
+    w = g.weights.astype(np.int64)
+    fin = d[s] != inf
+    # no edge can improve a distance
+    assert np.all(d[g.col[fin]] <= d[s[fin]] + w[fin])
+    # every reached vertex but the source is tight on some in-edge
+    tight = np.zeros(V, bool)
+    ok = fin & (d[g.col] == d[s] + w)
+    tight[g.col[ok]] = True
+    reached = d != inf
+    reached[src] = False
+    assert np.all(tight[reached])
+
+
+def test_c2_rmat20_sssp_color_mis_full_size(rt, rmat20):
+    """Configuration 2 at full size: RMAT-20, source = max-degree vertex."""
+    g, src = rmat20
+    with PersistentApp(rt, "lonestar_sssp", g, source=src) as a:
+        a.run()
+        d = a.result()
+    assert np.array_equal(d, oracle.lonestar_sssp(g, src, omp=True))
+    _check_sssp_optimal(g, src, d, 1000000000)
+    nv = graphs.seeded_node_values(g.num_nodes, 1)
+    with PersistentApp(rt, "color", g, node_values=nv) as a:
+        a.run()
+        c = a.result()
+    assert np.array_equal(c, oracle.color(g, nv, omp=True))
+    assert c.min() >= 1
+    with PersistentApp(rt, "mis", g, node_values=nv) as a:
+        a.run()
+        m = a.result()
+    assert np.array_equal(m, oracle.mis(g, nv, omp=True))
+    s = np.repeat(np.arange(g.num_nodes), g.degrees())
+    member = m == 2
+    assert not np.any(member[s] & member[g.col])             # independent
+    covered = member.copy()
+    covered[g.col[member[s]]] = True
+    assert np.all(covered)                                    # maximal
+
+
+def test_c2_rmat20_bfs_full_size(rt, rmat20):
+    g, src = rmat20
+    with PersistentApp(rt, "lonestar_bfs", g, source=src) as a:
+        a.run()
+        d = a.result()
+    assert np.array_equal(d, oracle.lonestar_bfs(g, src, omp=True))
+
+
+def test_invalid_inputs_rejected(rt):
+    g = graphs.rmat(8, 8, seed=1)
+    bad = graphs.Graph(g.row_ptr.copy(), g.col.copy(), g.weights)
+    bad.col[5] = g.num_nodes + 3
+    with pytest.raises(WgmError) as e:
+        PersistentApp(rt, "color", bad)
+    assert e.value.name == "WGM_ERR_INVALID"
+    loop = graphs.Graph(np.array([0, 1, 2], np.int32), np.array([0, 0], np.int32))
+    with pytest.raises(WgmError):
+        PersistentApp(rt, "mis", loop)
+    with PersistentApp(rt, "color", g) as a:
+        with pytest.raises(WgmError):
+            a.set_node_values(np.zeros(g.num_nodes, np.float32))
+    with PersistentApp(rt, "lonestar_bfs", g) as a:
+        with pytest.raises(WgmError):
+            a.set_source(g.num_nodes)
+    with pytest.raises(WgmError):
+        PersistentApp(rt, "lonestar_sssp", graphs.Graph(g.row_ptr, g.col, None))
