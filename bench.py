@@ -140,7 +140,7 @@ def _cpu_baseline(g, src, budget_s: float = 12.0) -> dict:
             et, _ = _traversed(g, d)
     return {"value": et * runs / t_tot / 1e9, "unit": "GTEPS", "cores": oracle.threads(),
             "kind": "port",
-            "sample": f"{runs} full SSSP runs on RMAT-{RMAT_SCALE} from the max-degree vertex "
+            "sample": f"{runs} full SSSP runs on the same RMAT graph from the max-degree vertex "
                       f"(OpenMP restatement of lonestar sssp.cl)"}
 
 
@@ -151,7 +151,12 @@ def main() -> int:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="wgm", choices=["wgm", "reference"])
     ap.add_argument("--no-extra", action="store_true")
+    ap.add_argument("--scale", type=int, default=RMAT_SCALE)
+    ap.add_argument("--kernel-only", action="store_true",
+                    help="time the device steps only (no e2e, extras or CPU baseline); "
+                         "the command profiled with ncu")
     args = ap.parse_args()
+    scale = args.scale
     warmup = max(args.warmup, 3)
     ws, rank, local = _dist_env()
     dist = None
@@ -162,17 +167,17 @@ def main() -> int:
 
     from gpu_workgroup_managment_gb300 import graphs
 
-    workload = f"rmat{RMAT_SCALE}_sssp"
-    config = {"workload": f"persistent Lonestar SSSP, RMAT scale {RMAT_SCALE} edge factor "
+    workload = f"rmat{scale}_sssp"
+    config = {"workload": f"persistent Lonestar SSSP, RMAT scale {scale} edge factor "
                           f"{RMAT_EF} (0.57,0.19,0.19) seed {RMAT_SEED}, weights U[1,1000], "
                           f"source = max-degree vertex",
-              "graph": f"rmat{RMAT_SCALE}", "parallelism": f"replicas{args.gpus}",
+              "graph": f"rmat{scale}", "parallelism": f"replicas{args.gpus}",
               "l2": "inputs larger than L2 (CSR+weights > 129 MB), no flush"}
 
     if args.impl == "reference":
         if rank != 0:
             return 0
-        g = graphs.rmat(RMAT_SCALE, RMAT_EF, seed=RMAT_SEED)
+        g = graphs.rmat(scale, RMAT_EF, seed=RMAT_SEED)
         src = graphs.max_degree_vertex(g)
         from oracle import oracle
         for _ in range(1):
@@ -205,12 +210,12 @@ def main() -> int:
     from gpu_workgroup_managment_gb300._lib import lib
     from gpu_workgroup_managment_gb300.runtime import pinned_copy
 
-    g = graphs.rmat(RMAT_SCALE, RMAT_EF, seed=RMAT_SEED)
+    g = graphs.rmat(scale, RMAT_EF, seed=RMAT_SEED)
     src = graphs.max_degree_vertex(g)
     rt = Runtime(device=local)
     app = PersistentApp(rt, "lonestar_sssp", g, source=src)
     # correctness of the benchmarked kernel (checked once, outside the timing)
-    app.run()
+    st0 = app.run()
     d = app.result()
     et, vr = _traversed(g, d)
 
@@ -231,6 +236,14 @@ def main() -> int:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms_step = float(t.item())
     value = et * ws / (ms_step * 1e-3) / 1e9
+    if args.kernel_only:
+        if rank == 0:
+            print(json.dumps({"metric": "SSSP GTEPS", "value": value, "ms_per_step": ms_step,
+                              "levels": st0.rounds, "groups": st0.groups,
+                              "edges_traversed": et, "workload": workload}))
+        app.close()
+        rt.close()
+        return 0
 
     # e2e through the public API with pinned host buffers
     rp, p1 = pinned_copy(g.row_ptr)
@@ -266,7 +279,7 @@ def main() -> int:
                      "frac": achieved / peak, "peak_source": peak_kind,
                      "traffic": _traffic("wgm_k_sssp", workload),
                      "bytes_alg_per_launch": bytes_alg, "edges_traversed": et,
-                     "vertices_reached": vr},
+                     "vertices_reached": vr, "levels": st0.rounds, "groups": st0.groups},
         "clocks": clk.summary(),
         "gpu_launches": args.steps,
     }
