@@ -82,6 +82,7 @@ _PROTOS = {
     "wgm_app_destroy": (_I, [_P]),
     "wgm_timer_start": (_I, [_P]),
     "wgm_timer_stop": (_I, [_P, C.POINTER(C.c_double)]),
+    "wgm_bfs_noalloc": (_I, [_P, _P, C.c_int32, C.c_int64, C.c_int32, _P, _P]),
     "wgm_host_alloc": (_P, [C.c_size_t]),
     "wgm_host_free": (None, [_P]),
     "wgm_gen_grid": (_I, [C.c_int32, C.c_int32, _P, _P, C.POINTER(C.c_int64)]),

@@ -18,7 +18,8 @@ ROOT = os.path.dirname(PKG)
 LIB = os.path.join(PKG, "libwgm.so")
 OBJ = os.path.join(PKG, "_build")
 
-SOURCES = ["wgm_kernels.cu", "wgm_runtime.cu", "wgm_apps.cu", "wgm_graphgen.cpp"]
+SOURCES = ["wgm_kernels.cu", "wgm_runtime.cu", "wgm_apps.cu", "wgm_graphgen.cpp",
+           "wgm_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

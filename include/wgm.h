@@ -176,6 +176,25 @@ int wgm_app_destroy(wgm_app *app);
 int wgm_timer_start(wgm_runtime *rt);
 int wgm_timer_stop(wgm_runtime *rt, double *elapsed_ms);
 
+/* ---- allocation-free BFS ------------------------------------------------ */
+/* No counterpart in the reference.  For callers that cannot allocate GPU
+ * memory (their own pool allocator owns the device, or cudaMalloc/cudaFree's
+ * implicit synchronisation is not acceptable where they call from): runs the
+ * persistent Lonestar BFS from `source` over a device CSR the caller owns and
+ * writes the levels to the caller's d_dist[num_nodes], allocating nothing.
+ * Its scratch is one static device array sized for WGM_NOALLOC_MAX_NODES
+ * vertices (about 8.5 MB, held by every GPU that loads the library until the
+ * process exits); larger graphs return WGM_ERR_INVALID.  The first call on a
+ * device does a one-time set-up (the array's device address), so make it
+ * before any stream capture.  Calls share the array: calls whose kernels
+ * overlap on the GPU race, so keep them ordered on one device.  `stream` is a
+ * cudaStream_t (NULL: the default stream); the call returns when the BFS has
+ * finished.  d_row_ptr must be a valid CSR (row_ptr[V] may be one short of
+ * num_edges, as the Lonestar loader produces). */
+#define WGM_NOALLOC_MAX_NODES (1 << 20)
+int wgm_bfs_noalloc(const int32_t *d_row_ptr, const int32_t *d_col, int32_t num_nodes,
+                    int64_t num_edges, int32_t source, uint32_t *d_dist, void *stream);
+
 /* ---- host memory helpers (pinned, for H2D/D2H at full bandwidth) ------- */
 void *wgm_host_alloc(size_t bytes);
 void wgm_host_free(void *p);
