@@ -155,8 +155,22 @@ def main() -> int:
     ap.add_argument("--kernel-only", action="store_true",
                     help="time the device steps only (no e2e, extras or CPU baseline); "
                          "the command profiled with ncu")
+    ap.add_argument("--barrier-sweep", action="store_true",
+                    help="ns per barrier for every barrier kind and CTA size, one JSON line each")
     args = ap.parse_args()
     scale = args.scale
+    if args.barrier_sweep:
+        from gpu_workgroup_managment_gb300 import Runtime
+        kinds = {0: "sense", 1: "xf", 2: "tree", 3: "count"}
+        with Runtime() as rt:
+            for threads in (128, 256, 512, 1024):
+                for kind, name in kinds.items():
+                    r = rt.barrier_bench(iterations=20000, threads_per_wg=threads,
+                                         barrier_kind=kind)
+                    print(json.dumps({"barrier": name, "threads_per_cta": threads,
+                                      "ctas": r["groups"], "barriers": r["barriers"],
+                                      "ns_per_barrier": r["ns_per_barrier"]}))
+        return 0
     warmup = max(args.warmup, 3)
     ws, rank, local = _dist_env()
     dist = None

@@ -24,7 +24,8 @@ STATUS_CODE = {v: k for k, v in STATUS.items()}
 APP_LONESTAR_BFS, APP_LONESTAR_SSSP, APP_PANNOTIA_COLOR = 1, 2, 3
 APP_PANNOTIA_MIS, APP_PANNOTIA_SSSP, APP_PAGERANK = 4, 5, 6
 DISCOVERY_TICKET, DISCOVERY_REFERENCE = 0, 1
-BARRIER_SENSE, BARRIER_XF, BARRIER_TREE = 0, 1, 2
+BARRIER_SENSE, BARRIER_XF, BARRIER_TREE, BARRIER_COUNT = 0, 1, 2, 3
+NP_NONE, NP_MATMULT_I32, NP_REDUCE_I32, NP_MATMULT_F32, NP_REDUCE_F32 = 0, 1, 2, 3, 4
 
 
 class WgmConfig(C.Structure):
@@ -80,6 +81,42 @@ _PROTOS = {
     "wgm_app_result_device_ptr": (_I, [_P, C.POINTER(_P), C.POINTER(C.c_size_t)]),
     "wgm_app_rounds": (_I, [_P, C.POINTER(_I)]),
     "wgm_app_destroy": (_I, [_P]),
+    "wgm_comm_create": (_I, [_P, _P, _I, _I, C.POINTER(_P)]),
+    "wgm_comm_destroy": (_I, [_P]),
+    "wgm_comm_launch_mega_kernel": (_I, [_P, _I]),
+    "wgm_comm_number_of_discovered_groups": (_I, [_P, C.POINTER(_I)]),
+    "wgm_comm_send_persistent_task": (_I, [_P, _I]),
+    "wgm_comm_send_task_synchronous": (_I, [_P, _I, C.POINTER(C.c_uint64),
+                                            C.POINTER(C.c_uint64)]),
+    "wgm_comm_is_executing_persistent": (_I, [_P, C.POINTER(_I)]),
+    "wgm_comm_get_persistent_time": (_I, [_P, C.POINTER(C.c_uint64)]),
+    "wgm_comm_send_quit": (_I, [_P]),
+    "wgm_comm_finish": (_I, [_P]),
+    "wgm_comm_reset": (_I, [_P]),
+    "wgm_comm_add_redline": (_I, [_P]),
+    "wgm_comm_summary": (_I, [_P, C.c_char_p, C.c_size_t]),
+    "wgm_comm_task_times": (_I, [_P, _P, _P, _I, C.POINTER(_I)]),
+    "wgm_comm_average_persistent_groups": (_I, [_P, C.POINTER(C.c_double)]),
+    "wgm_comm_reset_non_persistent": (_I, [_P]),
+    "wgm_comm_check_non_persistent": (_I, [_P, C.POINTER(_I)]),
+    "wgm_comm_get_occupancy_bound": (_I, [_P, C.POINTER(_I)]),
+    "wgm_run_merged_iteration": (_I, [_P, _I, _I, _I, _I, C.POINTER(_I), C.POINTER(_I)]),
+    "wgm_batch_create": (_I, [_P, _I, _P, _I, _P, _P, _P, C.POINTER(_P)]),
+    "wgm_batch_upload": (_I, [_P, _P]),
+    "wgm_batch_configure": (_I, [_P, _I, _I, _I]),
+    "wgm_batch_configure_teams": (_I, [_P, C.c_int64, _I]),
+    "wgm_batch_job_stats": (_I, [_P, _P, _P, _P, _P]),
+    "wgm_batch_launch": (_I, [_P, _I]),
+    "wgm_batch_run": (_I, [_P, _I, C.POINTER(C.c_double)]),
+    "wgm_batch_launch_per_graph": (_I, [_P]),
+    "wgm_batch_run_per_graph": (_I, [_P, C.POINTER(C.c_double)]),
+    "wgm_batch_read": (_I, [_P, _I, _P, C.c_int64]),
+    "wgm_batch_read_all": (_I, [_P, _P, C.c_int64]),
+    "wgm_batch_info": (_I, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(_I),
+                            C.POINTER(_I), C.POINTER(_I)]),
+    "wgm_batch_autotune": (_I, [_P, _I, C.POINTER(_I), C.POINTER(_I), C.POINTER(_I),
+                                C.POINTER(C.c_double)]),
+    "wgm_batch_destroy": (_I, [_P]),
     "wgm_timer_start": (_I, [_P]),
     "wgm_timer_stop": (_I, [_P, C.POINTER(C.c_double)]),
     "wgm_bfs_noalloc": (_I, [_P, _P, C.c_int32, C.c_int64, C.c_int32, _P, _P]),

@@ -1,0 +1,158 @@
+"""Batched form: many graphs and (graph, algorithm, source) jobs in one
+persistent launch fed by a device work queue (wgm_batch_* in include/wgm.h).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import graphs as G
+from ._lib import WgmGraphDesc, check, lib
+
+ALGOS = {"bfs": 0, "sssp": 1}
+
+
+class Batch:
+    def __init__(self, rt, graphs: list, jobs: list):
+        """jobs: (graph index, "bfs" | "sssp", source) per job."""
+        self.rt = rt
+        self.graphs = graphs
+        self.jobs = jobs
+        self._descs = (WgmGraphDesc * len(graphs))()
+        self._fill(graphs)
+        jg = np.array([j[0] for j in jobs], np.int32)
+        ja = np.array([ALGOS[j[1]] for j in jobs], np.int32)
+        js = np.array([j[2] for j in jobs], np.int32)
+        h = C.c_void_p()
+        check(lib.wgm_batch_create(rt.handle, len(graphs), self._descs, len(jobs),
+                                   jg.ctypes.data, ja.ctypes.data, js.ctypes.data, C.byref(h)),
+              "wgm_batch_create")
+        self._h = h
+        self.sizes = np.array([graphs[j[0]].num_nodes for j in jobs], np.int64)
+        self.offsets = np.concatenate([[0], np.cumsum(self.sizes)])
+
+    def _fill(self, graphs):
+        self._keep = []
+        for i, g in enumerate(graphs):
+            d = self._descs[i]
+            d.num_nodes = g.num_nodes
+            d.num_edges = g.num_edges
+            d.row_ptr = g.row_ptr.ctypes.data
+            d.col = g.col.ctypes.data if g.num_edges else None
+            d.weights = None if g.weights is None else g.weights.ctypes.data
+            self._keep.append((g.row_ptr, g.col, g.weights))
+
+    def upload(self, graphs: list) -> None:
+        self._fill(graphs)
+        check(lib.wgm_batch_upload(self._h, self._descs), "wgm_batch_upload")
+
+    def configure(self, threads: int = 256, ctas_per_sm: int = 0, piece: int = 0) -> None:
+        check(lib.wgm_batch_configure(self._h, threads, ctas_per_sm, piece), "batch_configure")
+
+    def configure_teams(self, team_edges: int = 0, max_team: int = 0) -> None:
+        """A job of E edges runs on ceil(E / team_edges) CTAs, at most max_team
+        (0 = defaults: total edges / grid, a quarter of the grid)."""
+        check(lib.wgm_batch_configure_teams(self._h, team_edges, max_team), "configure_teams")
+
+    def launch(self, use_cuda_graph: bool = True) -> None:
+        check(lib.wgm_batch_launch(self._h, int(use_cuda_graph)), "wgm_batch_launch")
+
+    def launch_per_graph(self) -> None:
+        check(lib.wgm_batch_launch_per_graph(self._h), "wgm_batch_launch_per_graph")
+
+    def run(self, use_cuda_graph: bool = True) -> float:
+        ms = C.c_double()
+        check(lib.wgm_batch_run(self._h, int(use_cuda_graph), C.byref(ms)), "wgm_batch_run")
+        return ms.value
+
+    def run_per_graph(self) -> float:
+        ms = C.c_double()
+        check(lib.wgm_batch_run_per_graph(self._h, C.byref(ms)), "wgm_batch_run_per_graph")
+        return ms.value
+
+    def result(self, job: int) -> np.ndarray:
+        out = np.empty(int(self.sizes[job]), np.uint32)
+        check(lib.wgm_batch_read(self._h, job, out.ctypes.data, out.shape[0]))
+        return out
+
+    def results(self, out: np.ndarray | None = None) -> np.ndarray:
+        if out is None:
+            out = np.empty(int(self.offsets[-1]), np.uint32)
+        check(lib.wgm_batch_read_all(self._h, out.ctypes.data, out.shape[0]))
+        return out
+
+    def info(self) -> dict:
+        n, e, t, c, p = C.c_int64(), C.c_int64(), C.c_int(), C.c_int(), C.c_int()
+        check(lib.wgm_batch_info(self._h, C.byref(n), C.byref(e), C.byref(t), C.byref(c),
+                                 C.byref(p)))
+        return {"total_nodes": n.value, "total_edges": e.value, "threads": t.value,
+                "ctas_per_sm": c.value, "piece": p.value}
+
+    def job_stats(self) -> dict:
+        """Per job of the last batched launch (caller's order): device start and
+        end in ns from the earliest start, team size, levels run."""
+        n = len(self.jobs)
+        st, en = np.empty(n, np.int64), np.empty(n, np.int64)
+        tm, lv = np.empty(n, np.int32), np.empty(n, np.int32)
+        check(lib.wgm_batch_job_stats(self._h, st.ctypes.data, en.ctypes.data, tm.ctypes.data,
+                                      lv.ctypes.data), "wgm_batch_job_stats")
+        return {"start_ns": st, "end_ns": en, "team": tm, "levels": lv}
+
+    def autotune(self, reps: int = 3) -> dict:
+        t, c, p, ms = C.c_int(), C.c_int(), C.c_int(), C.c_double()
+        check(lib.wgm_batch_autotune(self._h, reps, C.byref(t), C.byref(c), C.byref(p),
+                                     C.byref(ms)), "wgm_batch_autotune")
+        return {"threads": t.value, "ctas_per_sm": c.value, "piece": p.value, "ms": ms.value}
+
+    def close(self):
+        if self._h:
+            lib.wgm_batch_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def traversed_edges(g, dist: np.ndarray) -> int:
+    """E_t: out-degree summed over the reached vertices (INF = 1e9)."""
+    return int(g.degrees()[dist != 1000000000].sum())
+
+
+def batch_workload(n_graphs: int = 512, seed: int = 2024, mu: float = 13.0, sigma: float = 2.5,
+                   lo: int = 8, hi: int = 18) -> tuple[list, list, dict]:
+    """Seeded batch: log2(V) ~ Normal(mu, sigma) clamped to [lo, hi]; even
+    graphs RMAT (a,b,c)=(0.57,0.19,0.19) with average degree U{8..32}, odd
+    graphs near-square 2D grids; weights U[1,1000] per undirected edge; one
+    BFS and one SSSP job per graph from seeded sources."""
+    rng = np.random.default_rng(seed)
+    graphs, jobs = [], []
+    for i in range(n_graphs):
+        x = float(np.clip(rng.normal(mu, sigma), lo, hi))
+        if i % 2 == 0:
+            scale = int(round(x))
+            deg = int(rng.integers(8, 33))
+            g = G.rmat(scale, max(1, deg // 2), seed=seed * 1000 + i)
+        else:
+            v = int(round(2 ** x))
+            rows = max(1, int(round(v ** 0.5)))
+            cols = max(1, int(round(v / rows)))
+            g = G.grid(rows, cols)
+            g.weights = G.uniform_weights(g, seed * 1000 + i)
+        graphs.append(g)
+        jobs.append((i, "bfs", int(rng.integers(0, g.num_nodes))))
+        jobs.append((i, "sssp", int(rng.integers(0, g.num_nodes))))
+    meta = {"graphs": n_graphs, "seed": seed, "log2_nodes_mu": mu, "log2_nodes_sigma": sigma,
+            "log2_nodes_range": [lo, hi], "jobs": len(jobs),
+            "nodes_total": int(sum(g.num_nodes for g in graphs)),
+            "edges_total": int(sum(g.num_edges for g in graphs))}
+    return graphs, jobs, meta

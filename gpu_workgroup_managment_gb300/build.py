@@ -19,7 +19,7 @@ LIB = os.path.join(PKG, "libwgm.so")
 OBJ = os.path.join(PKG, "_build")
 
 SOURCES = ["wgm_kernels.cu", "wgm_runtime.cu", "wgm_apps.cu", "wgm_graphgen.cpp",
-           "wgm_noalloc.cu"]
+           "wgm_noalloc.cu", "wgm_mega.cu", "wgm_batch.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

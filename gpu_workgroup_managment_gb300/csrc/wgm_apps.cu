@@ -17,6 +17,7 @@
 #include "../../include/wgm.h"
 #include "wgm_internal.h"
 #include "wgm_kernels.cuh"
+#include "wgm_mega.cuh"
 
 int wgm_kind_to_kernel(int kind) {
   switch (kind) {
@@ -122,7 +123,8 @@ static void wgm_build_hubs(const wgm_graph_desc *g, int T, std::vector<int> &ids
 
 static void wgm_app_free_buffers(wgm_app *a) {
   void *ptrs[] = {a->d_row,     a->d_col,       a->d_wt,      a->d_node_value, a->d_out,
-                  a->d_wl,      a->d_cnt,       a->d_stamp,   a->d_stop,       a->d_hub_acc,
+                  a->d_wl_start, a->d_wl_cnt,   a->d_wl_u,
+                  a->d_cnt,       a->d_stamp,   a->d_stop,       a->d_hub_acc,
                   a->d_status,  a->d_contrib,   a->d_dang,    a->d_hub_sum,    a->d_rounds,
                   a->hubs.ids,  a->hubs.prefix, a->hubs.wmap};
   for (void *p : ptrs)
@@ -194,6 +196,12 @@ extern "C" int wgm_app_upload(wgm_app *a, const wgm_graph_desc *g) {
     s = wgm_upload_hubs(a, g);
     if (s) return s;
   }
+  if (a->kind == WGM_APP_PAGERANK) {
+    /* Initial dangling mass: every vertex starts at 1/V. */
+    int64_t zero = 0;
+    for (int v = 0; v < a->V; v++) zero += (g->row_ptr[v + 1] == g->row_ptr[v]);
+    a->dang0 = (float)((double)zero / (double)a->V);
+  }
   return WGM_OK;
 }
 
@@ -219,13 +227,22 @@ extern "C" int wgm_app_create(wgm_runtime *rt, int kind, const wgm_graph_desc *g
   if (e == cudaSuccess && wgm_needs_weights(kind)) e = wgm_dmalloc(&a->d_wt, E);
   switch (kind) {
     case WGM_APP_LONESTAR_BFS:
-    case WGM_APP_LONESTAR_SSSP:
+    case WGM_APP_LONESTAR_SSSP: {
       a->out_bytes = V * 4;
+      /* Pieces of at most `piece` edges; piece >= E/V keeps a level's list
+       * within V + E/piece <= 2V entries. */
+      int64_t avg = (int64_t)((E + V - 1) / std::max<size_t>(V, 1));
+      a->piece = (int)std::max<int64_t>(32, avg);
+      a->wl_cap = (int)(V + (E + a->piece - 1) / a->piece + 64);
       if (e == cudaSuccess) e = cudaMalloc(&a->d_out, a->out_bytes);
-      if (e == cudaSuccess) e = wgm_dmalloc(&a->d_wl, 2 * V);
-      if (e == cudaSuccess) e = wgm_dmalloc(&a->d_cnt, 6 * WGM_LINE);
+      if (e == cudaSuccess) e = wgm_dmalloc(&a->d_wl_start, 2 * (size_t)a->wl_cap);
+      if (e == cudaSuccess) e = wgm_dmalloc(&a->d_wl_cnt, 2 * (size_t)a->wl_cap);
+      if (e == cudaSuccess && kind == WGM_APP_LONESTAR_SSSP)
+        e = wgm_dmalloc(&a->d_wl_u, 2 * (size_t)a->wl_cap);
+      if (e == cudaSuccess) e = wgm_dmalloc(&a->d_cnt, 3 * WGM_LINE);
       if (e == cudaSuccess && kind == WGM_APP_LONESTAR_SSSP) e = wgm_dmalloc(&a->d_stamp, V);
       break;
+    }
     case WGM_APP_PANNOTIA_COLOR:
     case WGM_APP_PANNOTIA_MIS:
       a->out_bytes = V * 4;
@@ -315,28 +332,31 @@ static wgm_hubs wgm_hubs_view(const wgm_app *a) {
   return h;
 }
 
-/* Enqueue the app's persistent kernel on `stream`. */
-static cudaError_t wgm_app_enqueue(wgm_app *a, const wgm_launch &L, int grid, int block,
-                                   cudaStream_t stream) {
+/* Fill the kernel arguments of the app (also used by the megakernel). */
+int wgm_app_fill_mega(wgm_app *a, wgm_mega_args *A) {
+  A->app = wgm_kind_to_kernel(a->kind);
   switch (a->kind) {
     case WGM_APP_LONESTAR_BFS:
     case WGM_APP_LONESTAR_SSSP: {
-      wgm_lonestar_args x;
+      wgm_lonestar_args &x = A->ls;
       x.V = a->V;
       x.row = a->d_row;
       x.col = a->d_col;
       x.wt = a->d_wt;
       x.dist = (unsigned *)a->d_out;
-      x.wl = a->d_wl;
+      x.wl_start = a->d_wl_start;
+      x.wl_cnt = a->d_wl_cnt;
+      x.wl_u = a->d_wl_u;
+      x.cap = a->wl_cap;
+      x.piece = a->piece;
       x.cnt = a->d_cnt;
       x.stamp = a->d_stamp;
       x.source = a->source;
-      x.hub_threshold = a->hub_threshold;
       x.levels_out = a->d_rounds;
-      return wgm_launch_lonestar(a->kind == WGM_APP_LONESTAR_SSSP, L, x, grid, block, stream);
+      return WGM_OK;
     }
     case WGM_APP_PANNOTIA_COLOR: {
-      wgm_color_args x;
+      wgm_color_args &x = A->color;
       x.V = a->V;
       x.row = a->d_row;
       x.col = a->d_col;
@@ -347,10 +367,10 @@ static cudaError_t wgm_app_enqueue(wgm_app *a, const wgm_launch &L, int grid, in
       x.hubs = wgm_hubs_view(a);
       x.hub_threshold = a->hub_threshold;
       x.rounds_out = a->d_rounds;
-      return wgm_launch_color(L, x, grid, block, stream);
+      return WGM_OK;
     }
     case WGM_APP_PANNOTIA_MIS: {
-      wgm_mis_args x;
+      wgm_mis_args &x = A->mis;
       x.V = a->V;
       x.row = a->d_row;
       x.col = a->d_col;
@@ -362,10 +382,10 @@ static cudaError_t wgm_app_enqueue(wgm_app *a, const wgm_launch &L, int grid, in
       x.hubs = wgm_hubs_view(a);
       x.hub_threshold = a->hub_threshold;
       x.rounds_out = a->d_rounds;
-      return wgm_launch_mis(L, x, grid, block, stream);
+      return WGM_OK;
     }
     case WGM_APP_PANNOTIA_SSSP: {
-      wgm_psssp_args x;
+      wgm_psssp_args &x = A->psssp;
       x.V = a->V;
       x.row = a->d_row;
       x.col = a->d_col;
@@ -376,10 +396,10 @@ static cudaError_t wgm_app_enqueue(wgm_app *a, const wgm_launch &L, int grid, in
       x.hub_threshold = a->hub_threshold;
       x.source = a->source;
       x.rounds_out = a->d_rounds;
-      return wgm_launch_psssp(L, x, grid, block, stream);
+      return WGM_OK;
     }
     case WGM_APP_PAGERANK: {
-      wgm_pr_args x;
+      wgm_pr_args &x = A->pr;
       x.V = a->V;
       x.row = a->d_row;
       x.col = a->d_col;
@@ -391,8 +411,31 @@ static cudaError_t wgm_app_enqueue(wgm_app *a, const wgm_launch &L, int grid, in
       x.hub_threshold = a->hub_threshold;
       x.iterations = a->iterations;
       x.damping = a->damping;
-      return wgm_launch_pagerank(L, x, grid, block, stream);
+      x.dang0 = a->dang0;
+      return WGM_OK;
     }
+  }
+  return WGM_ERR_INVALID;
+}
+
+/* Enqueue the app's standalone persistent kernel on `stream`. */
+static cudaError_t wgm_app_enqueue(wgm_app *a, const wgm_launch &L, int grid, int block,
+                                   cudaStream_t stream) {
+  wgm_mega_args A;
+  std::memset(&A, 0, sizeof(A));
+  if (wgm_app_fill_mega(a, &A) != WGM_OK) return cudaErrorInvalidValue;
+  switch (a->kind) {
+    case WGM_APP_LONESTAR_BFS:
+    case WGM_APP_LONESTAR_SSSP:
+      return wgm_launch_lonestar(a->kind == WGM_APP_LONESTAR_SSSP, L, A.ls, grid, block, stream);
+    case WGM_APP_PANNOTIA_COLOR:
+      return wgm_launch_color(L, A.color, grid, block, stream);
+    case WGM_APP_PANNOTIA_MIS:
+      return wgm_launch_mis(L, A.mis, grid, block, stream);
+    case WGM_APP_PANNOTIA_SSSP:
+      return wgm_launch_psssp(L, A.psssp, grid, block, stream);
+    case WGM_APP_PAGERANK:
+      return wgm_launch_pagerank(L, A.pr, grid, block, stream);
   }
   return cudaErrorInvalidValue;
 }

@@ -1,0 +1,617 @@
+/*
+ * Batched form (include/wgm.h "batched form"): the discovery-free job-queue
+ * kernel of wgm_batch.cuh, its CUDA-graph capture, the per-graph baseline
+ * (one standalone persistent launch per job, the plain form) and the
+ * autotuner over block size, blocks per SM and worklist piece size.
+ */
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <new>
+#include <numeric>
+#include <vector>
+
+#include "../../include/wgm.h"
+#include "wgm_batch.cuh"
+#include "wgm_internal.h"
+#include "wgm_kernels.cuh"
+
+__global__ void __launch_bounds__(1024) wgm_k_batch(wgm_batch_args B) {
+  __shared__ wgm_warp_smem sm;
+  __shared__ int s_cnt[4];
+  __shared__ int s_slot;
+  for (;;) {
+    if (threadIdx.x == 0) s_slot = atomicAdd(&B.ctl[0], 1);
+    __syncthreads();
+    const int slot = s_slot;
+    if (slot >= B.nslots) break;
+    const int2 sr = B.slots[slot];
+    const wgm_batch_job j = B.jobs[sr.x];
+    if (sr.y == 0 && threadIdx.x == 0) B.times[2 * sr.x] = wgm_globaltimer();
+    if (j.team <= 1) {
+      if (j.algo == 0)
+        wgm_cta_lonestar<false>(B, j, sr.x, s_cnt, &sm);
+      else
+        wgm_cta_lonestar<true>(B, j, sr.x, s_cnt, &sm);
+    } else {
+      if (j.algo == 0)
+        wgm_team_lonestar<false>(B, j, sr.x, sr.y, &sm);
+      else
+        wgm_team_lonestar<true>(B, j, sr.x, sr.y, &sm);
+    }
+    if (sr.y == 0 && threadIdx.x == 0) B.times[2 * sr.x + 1] = wgm_globaltimer();
+    __syncthreads();
+  }
+}
+
+struct wgm_batch {
+  wgm_runtime *rt = nullptr;
+  int ngraphs = 0, njobs = 0;
+  std::vector<int> gV;
+  std::vector<long long> gE, g_row_off, g_col_off;
+  std::vector<wgm_batch_job> jobs; /* queue order (largest first) */
+  std::vector<int> queue_of;       /* caller's job index -> queue position */
+  int *d_rows = nullptr, *d_cols = nullptr;
+  unsigned *d_wts = nullptr, *d_dist = nullptr;
+  int *d_scratch = nullptr, *d_stamp = nullptr, *d_levels = nullptr;
+  int *d_ctl = nullptr;  /* control block: queue head + 4 lines per job */
+  int *d_err = nullptr;  /* first device error of a batched launch, its site */
+  int *d_cnt = nullptr;  /* level counters of the per-graph launches */
+  int2 *d_slots = nullptr;
+  unsigned long long *d_times = nullptr; /* per queue position: start, end ns */
+  int nslots = 0;
+  long long team_edges = 0; /* edges per team member; 0 = total edges / grid */
+  int max_team = 0;         /* 0 = a quarter of the grid */
+  wgm_batch_job *d_jobs = nullptr;
+  long long rows_total = 0, cols_total = 0, dist_total = 0, scratch_total = 0,
+            stamp_total = 0;
+  bool has_weights = false;
+  int threads = 256, ctas_per_sm = 0, piece = 0;
+  int teams_grid = 0; /* grid the team sizes were computed for (0 = stale) */
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+static void wgm_batch_free_graph(wgm_batch *b) {
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  b->exec = nullptr;
+  b->graph = nullptr;
+}
+
+extern "C" int wgm_batch_destroy(wgm_batch *b) {
+  if (!b) return WGM_ERR_INVALID;
+  cudaSetDevice(b->rt->device);
+  cudaStreamSynchronize(b->rt->stream);
+  wgm_batch_free_graph(b);
+  void *ptrs[] = {b->d_rows, b->d_cols, b->d_wts, b->d_dist, b->d_scratch, b->d_stamp,
+                  b->d_levels, b->d_ctl, b->d_err, b->d_slots, b->d_jobs, b->d_cnt,
+                  b->d_times};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  delete b;
+  return WGM_OK;
+}
+
+/* Piece size of a job: the configured one, else max(32, ceil(E/V)); the
+ * worklist capacity V + E/piece + 64 then bounds every level. */
+static void wgm_batch_layout(wgm_batch *b) {
+  long long wl = 0;
+  for (auto &j : b->jobs) {
+    const int g = j.graph;
+    long long V = b->gV[g], E = b->gE[g];
+    long long p = b->piece > 0 ? b->piece : std::max(32LL, (E + V - 1) / std::max(V, 1LL));
+    j.piece = (int)p;
+    j.cap = (int)(V + (E + p - 1) / p + 64);
+    j.wl_off = wl;
+    wl += 3LL * 2 * j.cap;
+  }
+  b->scratch_total = wl;
+}
+
+extern "C" int wgm_batch_create(wgm_runtime *rt, int num_graphs, const wgm_graph_desc *graphs,
+                                int num_jobs, const int32_t *job_graph, const int32_t *job_algo,
+                                const int32_t *job_source, wgm_batch **out) {
+  if (!rt || !out || num_graphs < 1 || !graphs || num_jobs < 1 || !job_graph || !job_algo ||
+      !job_source)
+    return WGM_ERR_INVALID;
+  *out = nullptr;
+  wgm_batch *b = new (std::nothrow) wgm_batch();
+  if (!b) return WGM_ERR_OOM;
+  b->rt = rt;
+  b->ngraphs = num_graphs;
+  b->njobs = num_jobs;
+  b->threads = rt->cfg.threads_per_wg;
+  /* graph arena layout and validation (as wgm_app_create does) */
+  for (int g = 0; g < num_graphs; g++) {
+    const wgm_graph_desc &d = graphs[g];
+    if (d.num_nodes < 1 || !d.row_ptr || d.num_edges < 0 || (d.num_edges && !d.col) ||
+        d.row_ptr[0] != 0) {
+      delete b;
+      return WGM_ERR_INVALID;
+    }
+    for (int i = 0; i < d.num_nodes; i++)
+      if (d.row_ptr[i + 1] < d.row_ptr[i] && i + 1 < d.num_nodes) {
+        delete b;
+        return WGM_ERR_INVALID;
+      }
+    if (d.row_ptr[d.num_nodes] > d.num_edges) {
+      delete b;
+      return WGM_ERR_INVALID;
+    }
+    b->gV.push_back(d.num_nodes);
+    b->gE.push_back(d.num_edges);
+    b->g_row_off.push_back(b->rows_total);
+    b->g_col_off.push_back(b->cols_total);
+    b->rows_total += d.num_nodes + 1;
+    b->cols_total += d.num_edges;
+    if (d.weights) b->has_weights = true;
+  }
+  /* jobs, queued largest first (edges, then vertices) */
+  std::vector<int> order(num_jobs);
+  std::iota(order.begin(), order.end(), 0);
+  for (int k = 0; k < num_jobs; k++) {
+    int g = job_graph[k];
+    if (g < 0 || g >= num_graphs || job_source[k] < 0 || job_source[k] >= b->gV[g] ||
+        (job_algo[k] != 0 && job_algo[k] != 1) || (job_algo[k] == 1 && !graphs[g].weights &&
+                                                   graphs[g].num_edges > 0)) {
+      delete b;
+      return WGM_ERR_INVALID;
+    }
+  }
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+    long long ex = b->gE[job_graph[x]], ey = b->gE[job_graph[y]];
+    if (ex != ey) return ex > ey;
+    return b->gV[job_graph[x]] > b->gV[job_graph[y]];
+  });
+  b->queue_of.assign(num_jobs, 0);
+  long long dist_off = 0, stamp_off = 0;
+  for (int q = 0; q < num_jobs; q++) {
+    int k = order[q], g = job_graph[k];
+    wgm_batch_job j;
+    std::memset(&j, 0, sizeof(j));
+    j.V = b->gV[g];
+    j.algo = job_algo[k];
+    j.source = job_source[k];
+    j.row_off = b->g_row_off[g];
+    j.col_off = b->g_col_off[g];
+    j.graph = g;
+    j.team = 1;
+    j.dist_off = dist_off;
+    dist_off += j.V;
+    if (j.algo == 1) {
+      j.stamp_off = stamp_off;
+      stamp_off += j.V;
+    }
+    b->jobs.push_back(j);
+    b->queue_of[k] = q;
+  }
+  b->dist_total = dist_off;
+  b->stamp_total = stamp_off;
+  wgm_batch_layout(b);
+  cudaSetDevice(rt->device);
+  cudaError_t e = cudaSuccess;
+  auto alloc = [&](void **p, size_t bytes) {
+    if (e == cudaSuccess) e = cudaMalloc(p, std::max<size_t>(bytes, 4));
+  };
+  alloc((void **)&b->d_rows, b->rows_total * 4);
+  alloc((void **)&b->d_cols, b->cols_total * 4);
+  alloc((void **)&b->d_wts, b->has_weights ? b->cols_total * 4 : 4);
+  alloc((void **)&b->d_dist, b->dist_total * 4);
+  alloc((void **)&b->d_stamp, b->stamp_total * 4);
+  alloc((void **)&b->d_levels, (size_t)num_jobs * 4);
+  alloc((void **)&b->d_ctl, (size_t)(1 + WGM_BATCH_CTL_LINES_PER_JOB * num_jobs) * WGM_LINE * 4);
+  alloc((void **)&b->d_err, 2 * 4);
+  alloc((void **)&b->d_times, (size_t)num_jobs * 16);
+  if (e == cudaSuccess) e = cudaMemset(b->d_err, 0, 2 * 4);
+  alloc((void **)&b->d_cnt, 3 * WGM_LINE * 4);
+  alloc((void **)&b->d_jobs, sizeof(wgm_batch_job) * (size_t)num_jobs);
+  alloc((void **)&b->d_scratch, b->scratch_total * 4);
+  if (e != cudaSuccess) {
+    int s = wgm_cuda_fail(rt, e);
+    wgm_batch_destroy(b);
+    return s;
+  }
+  int s = wgm_batch_upload(b, graphs);
+  if (s) {
+    wgm_batch_destroy(b);
+    return s;
+  }
+  *out = b;
+  return WGM_OK;
+}
+
+extern "C" int wgm_batch_upload(wgm_batch *b, const wgm_graph_desc *graphs) {
+  if (!b || !graphs) return WGM_ERR_INVALID;
+  cudaSetDevice(b->rt->device);
+  cudaStream_t s = b->rt->stream;
+  cudaError_t e = cudaSuccess;
+  for (int g = 0; g < b->ngraphs && e == cudaSuccess; g++) {
+    const wgm_graph_desc &d = graphs[g];
+    if (d.num_nodes != b->gV[g] || d.num_edges != b->gE[g]) return WGM_ERR_INVALID;
+    e = cudaMemcpyAsync(b->d_rows + b->g_row_off[g], d.row_ptr, (size_t)(d.num_nodes + 1) * 4,
+                        cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && d.num_edges)
+      e = cudaMemcpyAsync(b->d_cols + b->g_col_off[g], d.col, (size_t)d.num_edges * 4,
+                          cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && d.num_edges && d.weights && b->has_weights)
+      e = cudaMemcpyAsync(b->d_wts + b->g_col_off[g], d.weights, (size_t)d.num_edges * 4,
+                          cudaMemcpyHostToDevice, s);
+  }
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(b->d_jobs, b->jobs.data(), sizeof(wgm_batch_job) * b->jobs.size(),
+                        cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return wgm_cuda_fail(b->rt, e);
+  return WGM_OK;
+}
+
+static wgm_batch_args wgm_batch_kargs(wgm_batch *b) {
+  wgm_batch_args B;
+  B.jobs = b->d_jobs;
+  B.slots = b->d_slots;
+  B.nslots = b->nslots;
+  B.ctl = b->d_ctl;
+  B.err = b->d_err;
+  B.times = b->d_times;
+  B.spin_ns = b->rt->cfg.spin_timeout_ns ? b->rt->cfg.spin_timeout_ns : 2000000000ull;
+  B.rows = b->d_rows;
+  B.cols = b->d_cols;
+  B.wts = b->d_wts;
+  B.dist = b->d_dist;
+  B.scratch = b->d_scratch;
+  B.stamp = b->d_stamp;
+  B.levels = b->d_levels;
+  return B;
+}
+
+static int wgm_batch_grid(wgm_batch *b, int *grid) {
+  int per_sm = 0;
+  cudaError_t e =
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wgm_k_batch, b->threads, 0);
+  if (e != cudaSuccess) return wgm_cuda_fail(b->rt, e);
+  if (per_sm < 1) return WGM_ERR_INVALID;
+  int k = b->ctas_per_sm > 0 ? std::min(b->ctas_per_sm, per_sm) : per_sm;
+  *grid = k * b->rt->prop.multiProcessorCount;
+  return WGM_OK;
+}
+
+/* Team sizes and the slot queue for a grid of `grid` CTAs: a job of E edges
+ * gets ceil(E / team_edges) CTAs, at most max_team; its slots (job, rank)
+ * follow each other in the queue, largest job first. */
+static int wgm_batch_teams(wgm_batch *b, int grid) {
+  long long etot = 0;
+  for (auto &j : b->jobs) etot += b->gE[j.graph];
+  long long te = b->team_edges > 0 ? b->team_edges
+                                   : std::max(1LL << 15, (etot + grid - 1) / std::max(grid, 1));
+  int mt = b->max_team > 0 ? std::min(b->max_team, grid) : std::max(1, grid / 4);
+  std::vector<int2> slots;
+  for (int q = 0; q < b->njobs; q++) {
+    wgm_batch_job &j = b->jobs[q];
+    long long g = (b->gE[j.graph] + te - 1) / te;
+    j.team = (int)std::max(1LL, std::min<long long>(g, mt));
+    for (int r = 0; r < j.team; r++) slots.push_back(make_int2(q, r));
+  }
+  cudaError_t e = cudaSuccess;
+  if ((int)slots.size() > b->nslots || !b->d_slots) {
+    if (b->d_slots) cudaFree(b->d_slots);
+    b->d_slots = nullptr;
+    e = cudaMalloc((void **)&b->d_slots, slots.size() * sizeof(int2));
+  }
+  b->nslots = (int)slots.size();
+  if (e == cudaSuccess)
+    e = cudaMemcpy(b->d_slots, slots.data(), slots.size() * sizeof(int2), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(b->d_jobs, b->jobs.data(), sizeof(wgm_batch_job) * b->jobs.size(),
+                   cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return wgm_cuda_fail(b->rt, e);
+  return WGM_OK;
+}
+
+/* First device error of the batched launches since the last check. */
+static int wgm_batch_check(wgm_batch *b) {
+  int h[2] = {0, 0};
+  cudaError_t e = cudaMemcpy(h, b->d_err, sizeof(h), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return wgm_cuda_fail(b->rt, e);
+  if (h[0] == 0) return WGM_OK;
+  b->rt->last_status = h[0];
+  b->rt->last_site = h[1];
+  b->rt->last_detail = 0;
+  cudaMemset(b->d_err, 0, sizeof(h));
+  return wgm_status_from_device(h[0]);
+}
+
+/* Enqueue one batched launch: clear the control block, launch. */
+static cudaError_t wgm_batch_enqueue(wgm_batch *b, int grid, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(
+      b->d_ctl, 0, (size_t)(1 + WGM_BATCH_CTL_LINES_PER_JOB * b->njobs) * WGM_LINE * 4, s);
+  if (e != cudaSuccess) return e;
+  wgm_k_batch<<<grid, b->threads, 0, s>>>(wgm_batch_kargs(b));
+  return cudaGetLastError();
+}
+
+extern "C" int wgm_batch_configure(wgm_batch *b, int threads_per_cta, int ctas_per_sm,
+                                   int piece) {
+  if (!b || threads_per_cta < 32 || threads_per_cta > 1024 || threads_per_cta % 32 ||
+      ctas_per_sm < 0 || piece < 0 || (piece > 0 && piece < 1))
+    return WGM_ERR_INVALID;
+  cudaSetDevice(b->rt->device);
+  cudaStreamSynchronize(b->rt->stream);
+  bool relayout = piece != b->piece;
+  b->threads = threads_per_cta;
+  b->ctas_per_sm = ctas_per_sm;
+  b->piece = piece;
+  if (relayout) {
+    wgm_batch_layout(b);
+    cudaFree(b->d_scratch);
+    b->d_scratch = nullptr;
+    cudaError_t e = cudaMalloc((void **)&b->d_scratch, std::max<long long>(b->scratch_total, 1) * 4);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(b->d_jobs, b->jobs.data(), sizeof(wgm_batch_job) * b->jobs.size(),
+                     cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return wgm_cuda_fail(b->rt, e);
+  }
+  b->teams_grid = 0;
+  wgm_batch_free_graph(b);
+  return WGM_OK;
+}
+
+extern "C" int wgm_batch_configure_teams(wgm_batch *b, int64_t team_edges, int max_team) {
+  if (!b || team_edges < 0 || max_team < 0) return WGM_ERR_INVALID;
+  cudaSetDevice(b->rt->device);
+  cudaStreamSynchronize(b->rt->stream);
+  b->team_edges = team_edges;
+  b->max_team = max_team;
+  b->teams_grid = 0;
+  wgm_batch_free_graph(b);
+  return WGM_OK;
+}
+
+extern "C" int wgm_batch_launch(wgm_batch *b, int use_cuda_graph) {
+  if (!b) return WGM_ERR_INVALID;
+  cudaSetDevice(b->rt->device);
+  cudaStream_t s = b->rt->stream;
+  int grid = 0;
+  int st = wgm_batch_grid(b, &grid);
+  if (st) return st;
+  if (b->teams_grid != grid) {
+    cudaStreamSynchronize(s);
+    wgm_batch_free_graph(b);
+    st = wgm_batch_teams(b, grid);
+    if (st) return st;
+    b->teams_grid = grid;
+  }
+  cudaError_t e;
+  if (use_cuda_graph) {
+    if (!b->exec) {
+      /* capture once: queue reset + batched kernel */
+      e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+      if (e == cudaSuccess) e = wgm_batch_enqueue(b, grid, s);
+      cudaError_t e2 = cudaStreamEndCapture(s, &b->graph);
+      if (e == cudaSuccess) e = e2;
+      if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, b->graph, 0);
+      if (e != cudaSuccess) {
+        wgm_batch_free_graph(b);
+        return wgm_cuda_fail(b->rt, e);
+      }
+    }
+    e = cudaGraphLaunch(b->exec, s);
+  } else {
+    e = wgm_batch_enqueue(b, grid, s);
+  }
+  if (e != cudaSuccess) return wgm_cuda_fail(b->rt, e);
+  return WGM_OK;
+}
+
+extern "C" int wgm_batch_run(wgm_batch *b, int use_cuda_graph, double *device_ms) {
+  if (!b) return WGM_ERR_INVALID;
+  int s = wgm_timer_start(b->rt);
+  if (!s) s = wgm_batch_launch(b, use_cuda_graph);
+  double ms = 0;
+  int t = wgm_timer_stop(b->rt, &ms);
+  if (!s) s = t;
+  if (!s) s = wgm_batch_check(b);
+  if (device_ms) *device_ms = ms;
+  return s;
+}
+
+/* The plain form: one standalone persistent launch (discovery, barrier per
+ * level) per job, each on the whole GPU. */
+extern "C" int wgm_batch_launch_per_graph(wgm_batch *b) {
+  if (!b) return WGM_ERR_INVALID;
+  wgm_runtime *rt = b->rt;
+  cudaSetDevice(rt->device);
+  int block = rt->cfg.threads_per_wg;
+  if (block < 32 || block > 1024 || block % 32) block = 256;
+  int hw[2] = {0, 0};
+  int s = wgm_hw_bound_for(rt, WGM_K_BFS, block, &hw[0]);
+  if (!s) s = wgm_hw_bound_for(rt, WGM_K_SSSP, block, &hw[1]);
+  if (s) return s;
+  for (int q = 0; q < b->njobs; q++) {
+    const wgm_batch_job &j = b->jobs[q];
+    wgm_lonestar_args a;
+    std::memset(&a, 0, sizeof(a));
+    a.V = j.V;
+    a.row = b->d_rows + j.row_off;
+    a.col = b->d_cols + j.col_off;
+    a.wt = j.algo ? b->d_wts + j.col_off : nullptr;
+    a.dist = b->d_dist + j.dist_off;
+    a.wl_start = b->d_scratch + j.wl_off;
+    a.wl_cnt = a.wl_start + 2 * (size_t)j.cap;
+    a.wl_u = j.algo ? a.wl_cnt + 2 * (size_t)j.cap : nullptr;
+    a.cap = j.cap;
+    a.piece = j.piece;
+    a.cnt = b->d_cnt;
+    a.stamp = j.algo ? b->d_stamp + j.stamp_off : nullptr;
+    a.source = j.source;
+    a.levels_out = b->d_levels + q;
+    int grid = hw[j.algo];
+    wgm_launch L = wgm_make_launch(rt, grid, 0, 0);
+    cudaError_t e = wgm_launch_lonestar(j.algo == 1, L, a, grid, block, rt->stream);
+    if (e != cudaSuccess) return wgm_cuda_fail(rt, e);
+  }
+  return WGM_OK;
+}
+
+extern "C" int wgm_batch_run_per_graph(wgm_batch *b, double *device_ms) {
+  if (!b) return WGM_ERR_INVALID;
+  int s = wgm_timer_start(b->rt);
+  if (!s) s = wgm_batch_launch_per_graph(b);
+  double ms = 0;
+  int t = wgm_timer_stop(b->rt, &ms);
+  if (!s) s = t;
+  if (device_ms) *device_ms = ms;
+  return s;
+}
+
+extern "C" int wgm_batch_read(wgm_batch *b, int job, uint32_t *out, int64_t n) {
+  if (!b || !out || job < 0 || job >= b->njobs) return WGM_ERR_INVALID;
+  const wgm_batch_job &j = b->jobs[b->queue_of[job]];
+  if (n < j.V) return WGM_ERR_INVALID;
+  cudaSetDevice(b->rt->device);
+  cudaError_t e = cudaMemcpyAsync(out, b->d_dist + j.dist_off, (size_t)j.V * 4,
+                                  cudaMemcpyDeviceToHost, b->rt->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(b->rt->stream);
+  if (e != cudaSuccess) return wgm_cuda_fail(b->rt, e);
+  return wgm_batch_check(b);
+}
+
+/* All results, in the caller's job order, concatenated. */
+extern "C" int wgm_batch_read_all(wgm_batch *b, uint32_t *out, int64_t n) {
+  if (!b || !out || n < b->dist_total) return WGM_ERR_INVALID;
+  cudaSetDevice(b->rt->device);
+  cudaStream_t s = b->rt->stream;
+  int64_t pos = 0;
+  for (int k = 0; k < b->njobs; k++) {
+    const wgm_batch_job &j = b->jobs[b->queue_of[k]];
+    cudaError_t e = cudaMemcpyAsync(out + pos, b->d_dist + j.dist_off, (size_t)j.V * 4,
+                                    cudaMemcpyDeviceToHost, s);
+    if (e != cudaSuccess) return wgm_cuda_fail(b->rt, e);
+    pos += j.V;
+  }
+  cudaError_t e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return wgm_cuda_fail(b->rt, e);
+  return wgm_batch_check(b);
+}
+
+extern "C" int wgm_batch_info(wgm_batch *b, int64_t *total_nodes, int64_t *total_edges,
+                              int *threads, int *ctas_per_sm, int *piece) {
+  if (!b) return WGM_ERR_INVALID;
+  if (total_nodes) *total_nodes = b->dist_total;
+  if (total_edges) {
+    long long e = 0;
+    for (auto &j : b->jobs) e += b->gE[j.graph];
+    *total_edges = e;
+  }
+  if (threads) *threads = b->threads;
+  if (ctas_per_sm) *ctas_per_sm = b->ctas_per_sm;
+  if (piece) *piece = b->piece;
+  return WGM_OK;
+}
+
+/* Autotuner: block size x blocks per SM x worklist piece first, then the
+ * team size (edges per team member as a multiple of total edges / grid), each
+ * point the best of `reps` CUDA-graph replays; leaves the batch configured
+ * with the winner. */
+static int wgm_batch_time(wgm_batch *b, int reps, double *out) {
+  double ms = 0, mn = 1e300;
+  int s = wgm_batch_run(b, 1, &ms); /* warm-up and capture */
+  if (s) return s;
+  for (int r = 0; r < reps; r++) {
+    s = wgm_batch_run(b, 1, &ms);
+    if (s) return s;
+    mn = std::min(mn, ms);
+  }
+  *out = mn;
+  return WGM_OK;
+}
+
+extern "C" int wgm_batch_autotune(wgm_batch *b, int reps, int *best_threads,
+                                  int *best_ctas_per_sm, int *best_piece, double *best_ms) {
+  if (!b || reps < 1) return WGM_ERR_INVALID;
+  const int threads_set[3] = {128, 256, 512};
+  const int piece_set[3] = {16, 32, 64};
+  const long long saved_te = b->team_edges;
+  const int saved_mt = b->max_team;
+  double best = 1e300;
+  int bt = b->threads, bc = b->ctas_per_sm, bp = b->piece;
+  for (int t : threads_set) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wgm_k_batch, t, 0) !=
+            cudaSuccess ||
+        per_sm < 1)
+      continue;
+    std::vector<int> ctas;
+    for (int c = 1; c < per_sm; c *= 2) ctas.push_back(c);
+    ctas.push_back(per_sm);
+    for (int c : ctas) {
+      for (int p : piece_set) {
+        int s = wgm_batch_configure(b, t, c, p);
+        double mn = 0;
+        if (!s) s = wgm_batch_time(b, reps, &mn);
+        if (s) return s;
+        if (mn < best) {
+          best = mn;
+          bt = t;
+          bc = c;
+          bp = p;
+        }
+      }
+    }
+  }
+  int s = wgm_batch_configure(b, bt, bc, bp);
+  if (s) return s;
+  /* team sizes at the winning shape */
+  int grid = 0;
+  s = wgm_batch_grid(b, &grid);
+  if (s) return s;
+  long long etot = 0;
+  for (auto &j : b->jobs) etot += b->gE[j.graph];
+  const long long base = std::max(1LL, etot / std::max(grid, 1));
+  long long bte = saved_te;
+  const double factors[5] = {0.125, 0.25, 0.5, 1.0, 2.0};
+  for (double f : factors) {
+    long long te = std::max(1LL << 12, (long long)(base * f));
+    s = wgm_batch_configure_teams(b, te, saved_mt);
+    double mn = 0;
+    if (!s) s = wgm_batch_time(b, reps, &mn);
+    if (s) return s;
+    if (mn < best) {
+      best = mn;
+      bte = te;
+    }
+  }
+  s = wgm_batch_configure_teams(b, bte, saved_mt);
+  if (best_threads) *best_threads = bt;
+  if (best_ctas_per_sm) *best_ctas_per_sm = bc;
+  if (best_piece) *best_piece = bp;
+  if (best_ms) *best_ms = best;
+  return s;
+}
+
+/* Device timestamps of the last batched launch, in the caller's job order:
+ * start and end of each job (ns, relative to the earliest start), its team
+ * size and its level count. */
+extern "C" int wgm_batch_job_stats(wgm_batch *b, int64_t *start_ns, int64_t *end_ns,
+                                   int32_t *team, int32_t *levels) {
+  if (!b) return WGM_ERR_INVALID;
+  cudaSetDevice(b->rt->device);
+  std::vector<unsigned long long> t(2 * (size_t)b->njobs);
+  std::vector<int> lv(b->njobs);
+  cudaError_t e = cudaStreamSynchronize(b->rt->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(t.data(), b->d_times, t.size() * 8, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(lv.data(), b->d_levels, lv.size() * 4, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return wgm_cuda_fail(b->rt, e);
+  unsigned long long t0 = ~0ull;
+  for (int q = 0; q < b->njobs; q++) t0 = std::min(t0, t[2 * q]);
+  for (int k = 0; k < b->njobs; k++) {
+    const int q = b->queue_of[k];
+    if (start_ns) start_ns[k] = (int64_t)(t[2 * q] - t0);
+    if (end_ns) end_ns[k] = (int64_t)(t[2 * q + 1] - t0);
+    if (team) team[k] = b->jobs[q].team;
+    if (levels) levels[k] = lv[q];
+  }
+  return WGM_OK;
+}

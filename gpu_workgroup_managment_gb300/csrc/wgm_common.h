@@ -68,6 +68,7 @@
 #define WGM_BARRIER_SENSE 0 /* counter + generation word (sense reversal) */
 #define WGM_BARRIER_XF 1    /* master/slave flags (iw_barrier.cl:63-109) */
 #define WGM_BARRIER_TREE 2  /* two-level counter tree, then generation word */
+#define WGM_BARRIER_COUNT 3 /* monotonic arrival counter, waiters poll it */
 
 #define WGM_POLL_CLOSED 0x40000000
 
@@ -126,6 +127,9 @@ typedef struct wgm_dev_state {
   int32_t bar_to_kill;
   int32_t pad_b2[WGM_LINE - 2];
   int32_t tree_count[128 * WGM_LINE]; /* leaf counters, one line each */
+  /* Counting barrier: arrivals of launch generation g on line g&1; the
+   * discovery closer of launch g zeroes line (g+1)&1 for the next launch. */
+  int32_t bar_arrivals[2 * WGM_LINE];
 
   /* Kernel contexts (kernel_ctx.h:6-11): [0] non-persistent, [1] persistent. */
   int32_t k_num_groups[2][WGM_LINE];

@@ -69,6 +69,9 @@ __device__ __forceinline__ int wgm_atom_cas_acqrel_gpu(int *p, int cmp, int v) {
                : "=r"(old) : "l"(p), "r"(cmp), "r"(v) : "memory");
   return old;
 }
+__device__ __forceinline__ void wgm_red_add_release_gpu(int *p, int v) {
+  asm volatile("red.release.gpu.global.add.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
 __device__ __forceinline__ void wgm_fence_acqrel_gpu() {
   asm volatile("fence.acq_rel.gpu;" ::: "memory");
 }
@@ -224,6 +227,7 @@ __device__ __forceinline__ bool wgm_discover_ticket(const wgm_launch &L, int *id
     int old = wgm_atom_or_acqrel_gpu(&L.st->poll_word[slot], WGM_POLL_CLOSED);
     int cnt = old & (WGM_POLL_CLOSED - 1);
     wgm_st_relaxed_gpu(&L.st->poll_word[slot ^ 1], 0);
+    wgm_st_relaxed_gpu(&L.st->bar_arrivals[(slot ^ 1) * WGM_LINE], 0);
     wgm_st_relaxed_gpu(&L.st->count[slot], cnt);
     wgm_st_release_gpu(&L.st->published, L.gen);
     *n = cnt;
@@ -247,7 +251,10 @@ __device__ __forceinline__ bool wgm_discover_reference(const wgm_launch &L, int 
   bool open = wgm_ld_relaxed_gpu(&L.st->closed_gen) != L.gen;
   if (open) {
     *id = wgm_ld_relaxed_gpu(&L.st->count[slot]);
-    if (*id == 0) wgm_st_relaxed_gpu(&L.st->count[slot ^ 1], 0);
+    if (*id == 0) {
+      wgm_st_relaxed_gpu(&L.st->count[slot ^ 1], 0);
+      wgm_st_relaxed_gpu(&L.st->bar_arrivals[(slot ^ 1) * WGM_LINE], 0);
+    }
     wgm_st_relaxed_gpu(&L.st->count[slot], *id + 1);
   }
   wgm_tl_unlock(L);
@@ -286,6 +293,7 @@ __device__ __forceinline__ bool wgm_discover(const wgm_launch &L, wgm_cta *c) {
      * (no barrier can complete before every CTA has arrived). */
     c->gen = wgm_ld_relaxed_gpu(&L.st->bar_gen);
     c->tmp[0] = 0;
+    c->tmp[2] = 0; /* counting barrier: arrivals expected so far */
   }
   __syncthreads();
   if (!c->ok) return false;
@@ -321,6 +329,35 @@ __device__ __forceinline__ bool wgm_barrier_sense(const wgm_launch &L, wgm_cta *
       }
     }
     c->gen = g + 1;
+  }
+  __syncthreads();
+  return c->ok;
+}
+
+/* Counting barrier.  The launch's arrival counter (zeroed by the previous
+ * launch's discovery closer, so it starts at 0) only grows: barrier k of the
+ * launch completes when it reaches (k+1)*ngroups.  An arrival is one
+ * fire-and-forget red.release (this CTA's writes before the barrier are
+ * published by it); the waiters poll the counter itself and then fence, so
+ * the last arriver needs neither a returned value nor a second store - one
+ * L2 hop shorter than the generation barrier.  Differences are taken modulo
+ * 2^32, which keeps the test right across wrap-around. */
+__device__ __forceinline__ bool wgm_barrier_count(const wgm_launch &L, wgm_cta *c,
+                                                  int ngroups) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int *ctr = &L.st->bar_arrivals[(L.gen & 1) * WGM_LINE];
+    const unsigned target = (unsigned)c->tmp[2] + (unsigned)ngroups;
+    c->tmp[2] = (int)target;
+    wgm_red_add_release_gpu(ctr, 1);
+    wgm_spin s = wgm_spin_start(L);
+    while ((int)((unsigned)wgm_ld_relaxed_gpu(ctr) - target) < 0) {
+      if (wgm_spin_giveup(L, s, WGM_SITE_BARRIER)) {
+        c->ok = 0;
+        break;
+      }
+    }
+    wgm_fence_acqrel_gpu();
   }
   __syncthreads();
   return c->ok;
@@ -412,6 +449,8 @@ __device__ __forceinline__ bool wgm_barrier(const wgm_launch &L, wgm_cta *c) {
       return wgm_barrier_xf(L, c, c->ngroups);
     case WGM_BARRIER_TREE:
       return wgm_barrier_tree(L, c, c->ngroups);
+    case WGM_BARRIER_COUNT:
+      return wgm_barrier_count(L, c, c->ngroups);
     default:
       return wgm_barrier_sense(L, c, c->ngroups);
   }

@@ -123,11 +123,16 @@ struct wgm_lonestar_args {
   const int *col;
   const unsigned *wt; /* SSSP weights, nullptr for BFS */
   unsigned *dist;     /* [V] output */
-  int *wl;            /* [2][V]: small items grow up, hub items grow down */
-  int *cnt;           /* [6 lines]: small[3], big[3] counters (line each) */
-  int *stamp;         /* SSSP: level a vertex was last queued at */
+  /* Two worklists of `cap` pieces each, structure of arrays: a piece is up
+   * to `piece` consecutive edges of one vertex. */
+  int *wl_start; /* [2][cap] first edge of the piece */
+  int *wl_cnt;   /* [2][cap] number of edges */
+  int *wl_u;     /* [2][cap] the vertex (SSSP reads its distance); may be null for BFS */
+  int cap;       /* >= V + E/piece, so no level can overflow */
+  int piece;     /* edges per piece (>= 32) */
+  int *cnt;      /* [3 lines]: pieces queued for each level, by level mod 3 */
+  int *stamp;    /* SSSP: level a vertex was last queued at */
   int source;
-  int hub_threshold;
   int *levels_out; /* number of levels run (written by group 0) */
 };
 
@@ -137,34 +142,205 @@ __device__ __forceinline__ int wgm_ls_degree(const int *row, int v) {
   return max(__ldg(&row[v + 1]) - __ldg(&row[v]), 0);
 }
 
-/* One relaxation of edge e from a vertex at distance dsrc, at level L.
+/* Relaxation rules of one edge from a vertex at distance dsrc, at level L
+ * (applied by wgm_ls_chunk):
  * BFS (bfs.cl:115-125): dist[dst]==MYINFINITY -> dist[dst]=level; the
  *   reference's unsynchronised store becomes a CAS so each vertex is queued
  *   exactly once (the stored value is identical: the level).
  * SSSP (sssp.cl:115-131): altdist = dist[src]+wt; if smaller, atomic_min and
  *   queue dst; a per-level stamp queues a vertex at most once per level (its
  *   next visit reads the final dist of the level, so the fixpoint - the
- *   shortest-path vector - is unchanged). */
-template <bool SSSP>
-__device__ __forceinline__ bool wgm_ls_relax(const wgm_lonestar_args &a, int e, unsigned dsrc,
-                                             int L, int *u_out) {
-  int u = __ldg(&a.col[e]);
-  *u_out = u;
-  if ((unsigned)u >= (unsigned)a.V) return false; /* bfs.cl:116 */
-  if (!SSSP) {
-    if (__ldcg(&a.dist[u]) != WGM_LONESTAR_INF) return false;
-    return atomicCAS(&a.dist[u], WGM_LONESTAR_INF, (unsigned)L) == WGM_LONESTAR_INF;
-  } else {
-    unsigned w = __ldg(&a.wt[e]);
-    if (w >= WGM_LONESTAR_INF) return false; /* sssp.cl:120 */
-    unsigned alt = dsrc + w;
-    if (alt >= __ldcg(&a.dist[u])) return false;
-    unsigned old = atomicMin(&a.dist[u], alt);
-    if (alt >= old) return false;
-    return atomicExch(&a.stamp[u], L) != L;
+ *   shortest-path vector - is unchanged).
+ * Destinations outside [0, V) and weights >= MYINFINITY are skipped
+ * (bfs.cl:116, sssp.cl:120). */
+
+/* Queue the flagged lanes' vertices as pieces (warp-aggregated: one atomic
+ * per warp, __ballot_sync/__popc/__shfl_sync inside the scan and window
+ * walk).  A vertex with no out-edges is not queued: its level or distance is
+ * already written and it has nothing to relax.  Pieces are written by the
+ * whole warp, one piece per lane per window, so the stores are coalesced. */
+__device__ __forceinline__ bool wgm_ls_push(const wgm_lonestar_args &a, bool flag, int u,
+                                            int *counter, int *o_start, int *o_cnt, int *o_u,
+                                            int *tab) {
+  int start = 0, deg = 0, np = 0;
+  if (flag) {
+    start = __ldg(&a.row[u]);
+    deg = wgm_ls_degree(a.row, u);
+    np = (deg + a.piece - 1) / a.piece;
   }
+  int incl = wgm_warp_incl_scan(np);
+  int total = __shfl_sync(WGM_FULL, incl, 31);
+  if (total == 0) return true;
+  int base = 0;
+  if (wgm_lane() == 0) base = atomicAdd(counter, total);
+  base = __shfl_sync(WGM_FULL, base, 0);
+  if (base + total > a.cap) return false;
+  int off = incl - np;
+  const int P = a.piece;
+  wgm_for_each_edge(off, np, -off, total, 0, 32, tab, [&](bool valid, int k, int owner) {
+    /* k: piece index of `owner`'s vertex; slot = its position in the list */
+    int s = __shfl_sync(WGM_FULL, start, owner);
+    int d = __shfl_sync(WGM_FULL, deg, owner);
+    int v = __shfl_sync(WGM_FULL, u, owner);
+    int o = __shfl_sync(WGM_FULL, off, owner);
+    if (valid) {
+      int slot = base + o + k;
+      o_start[slot] = s + k * P;
+      o_cnt[slot] = min(P, d - k * P);
+      if (o_u) o_u[slot] = v;
+    }
+  });
+  return true;
 }
 
+/* Owner lane of edge slot s in a warp's concatenated ranges: the last lane
+ * whose exclusive offset is <= s, by binary search over shuffles.  A lane with
+ * no edges shares its successor's offset, so the search always lands on the
+ * lane whose range [off, off+deg) holds s (for 0 <= s < total). */
+__device__ __forceinline__ int wgm_owner_of(int off, int s) {
+  int j = 0;
+#pragma unroll
+  for (int step = 16; step > 0; step >>= 1) {
+    int o = __shfl_sync(WGM_FULL, off, j + step);
+    if (o <= s) j += step;
+  }
+  return j;
+}
+
+/* Worklist a chunk pushes to. */
+struct wgm_ls_out {
+  int *counter; /* pieces queued so far (global or shared memory) */
+  int *o_start, *o_cnt, *o_u;
+  int cap;
+};
+
+/* Edges per lane per batch of the chunk walker: a warp relaxes 32*K edges
+ * with every memory step of the K windows issued together, so K chains of
+ * loads and atomics are in flight per lane instead of one. */
+#ifndef WGM_LS_K
+#define WGM_LS_K 4
+#endif
+/* A pushed vertex with more pieces than this is written by the whole warp. */
+#define WGM_LS_LANE_PIECES 4
+
+/* Relax the edges of one chunk (one piece per lane: first edge `start`,
+ * `deg` edges, source distance `dv` for SSSP) and queue the improved
+ * vertices as pieces of the next level.  Per batch of 32*K edges:
+ *   col/wt loads -> dist pre-check -> atomic (CAS for BFS, min for SSSP)
+ *   with row[u], row[u+1] fetched beside it -> SSSP stamp exchange ->
+ *   one warp scan and one counter atomic for every piece of the batch.
+ * The relaxation rules are stated above wgm_ls_push; the order of
+ * relaxations inside a level does not change the fixpoint. */
+template <bool SSSP>
+__device__ __forceinline__ bool wgm_ls_chunk(const int *row, const int *col, const unsigned *wt,
+                                             unsigned *dist, int *stamp, int V, int P, int L,
+                                             int start, int deg, unsigned dv,
+                                             const wgm_ls_out &o) {
+  constexpr int K = WGM_LS_K;
+  const int lane = wgm_lane();
+  const int incl = wgm_warp_incl_scan(deg);
+  const int total = __shfl_sync(WGM_FULL, incl, 31);
+  const int off = incl - deg;
+  const int base = start - off;
+  bool ok = true;
+  for (int w = 0; w < total; w += 32 * K) {
+    int e[K], u[K], rs[K], d[K], np[K];
+    unsigned alt[K];
+    bool f[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      const int s = w + 32 * k + lane;
+      f[k] = s < total;
+      const int own = wgm_owner_of(off, min(s, total - 1));
+      e[k] = __shfl_sync(WGM_FULL, base, own) + s;
+      alt[k] = SSSP ? __shfl_sync(WGM_FULL, dv, own) : 0u;
+    }
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      u[k] = f[k] ? __ldg(&col[e[k]]) : -1;
+      if (SSSP) {
+        unsigned wk = f[k] ? __ldg(&wt[e[k]]) : WGM_LONESTAR_INF;
+        f[k] = f[k] && wk < WGM_LONESTAR_INF; /* sssp.cl:120 */
+        alt[k] += wk;
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      f[k] = f[k] && (unsigned)u[k] < (unsigned)V; /* bfs.cl:116 */
+      if (f[k]) {
+        unsigned cur = __ldcg(&dist[u[k]]);
+        f[k] = SSSP ? (alt[k] < cur) : (cur == WGM_LONESTAR_INF);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      rs[k] = 0;
+      d[k] = 0;
+      if (f[k]) {
+        if (SSSP)
+          f[k] = alt[k] < atomicMin(&dist[u[k]], alt[k]);
+        else
+          f[k] = atomicCAS(&dist[u[k]], WGM_LONESTAR_INF, (unsigned)L) == WGM_LONESTAR_INF;
+        rs[k] = __ldg(&row[u[k]]);
+        d[k] = __ldg(&row[u[k] + 1]);
+      }
+    }
+    int mine = 0;
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      if (SSSP && f[k]) f[k] = atomicExch(&stamp[u[k]], L) != L;
+      d[k] = f[k] ? max(d[k] - rs[k], 0) : 0; /* a vertex without edges is not queued */
+      np[k] = (d[k] + P - 1) / P;
+      mine += np[k];
+    }
+    const int pincl = wgm_warp_incl_scan(mine);
+    const int ptotal = __shfl_sync(WGM_FULL, pincl, 31);
+    if (ptotal == 0) continue;
+    int pbase = 0;
+    if (lane == 31) pbase = atomicAdd(o.counter, ptotal);
+    pbase = __shfl_sync(WGM_FULL, pbase, 31);
+    if (pbase + ptotal > o.cap) {
+      ok = false;
+      continue;
+    }
+    int slot = pbase + pincl - mine;
+    int sl[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      sl[k] = slot;
+      if (np[k] <= WGM_LS_LANE_PIECES) {
+        for (int q = 0; q < np[k]; q++) {
+          o.o_start[slot + q] = rs[k] + q * P;
+          o.o_cnt[slot + q] = min(P, d[k] - q * P);
+          if (o.o_u) o.o_u[slot + q] = u[k];
+        }
+      }
+      slot += np[k];
+    }
+    /* high-degree vertices: the whole warp writes their pieces */
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      unsigned big = __ballot_sync(WGM_FULL, np[k] > WGM_LS_LANE_PIECES);
+      while (big) {
+        const int j = __ffs(big) - 1;
+        big &= big - 1;
+        const int bs = __shfl_sync(WGM_FULL, rs[k], j), bd = __shfl_sync(WGM_FULL, d[k], j);
+        const int bu = __shfl_sync(WGM_FULL, u[k], j), bsl = __shfl_sync(WGM_FULL, sl[k], j);
+        const int bn = (bd + P - 1) / P;
+        for (int q = lane; q < bn; q += 32) {
+          o.o_start[bsl + q] = bs + q * P;
+          o.o_cnt[bsl + q] = min(P, bd - q * P);
+          if (o.o_u) o.o_u[bsl + q] = bu;
+        }
+      }
+    }
+  }
+  return ok;
+}
+
+/* One level: every warp takes 32 consecutive pieces of the input list (one
+ * per lane) and walks their edges with wgm_ls_chunk; a piece holds at most
+ * `piece` edges, so no warp ever holds more than 32*piece edges of a level. */
 template <bool SSSP>
 __device__ __forceinline__ bool wgm_ls_level(const wgm_launch &Lc, wgm_cta *c,
                                              const wgm_lonestar_args &a, int L,
@@ -172,109 +348,134 @@ __device__ __forceinline__ bool wgm_ls_level(const wgm_launch &Lc, wgm_cta *c,
   const int lane = wgm_lane(), warp = threadIdx.x >> 5;
   const int nwarps_cta = blockDim.x >> 5;
   const int gw = c->id * nwarps_cta + warp, NW = c->ngroups * nwarps_cta;
-  const int V = a.V;
-  int *cnt = a.cnt;
-  const int ns = __ldcg(&cnt[(L % 3) * WGM_LINE]);
-  const int nb = __ldcg(&cnt[(3 + L % 3) * WGM_LINE]);
-  int *cnt_small_out = &cnt[((L + 1) % 3) * WGM_LINE];
-  int *cnt_big_out = &cnt[(3 + (L + 1) % 3) * WGM_LINE];
-  const int *in = a.wl + (size_t)(L & 1) * V;
-  int *out = a.wl + (size_t)((L + 1) & 1) * V;
+  const int n = __ldcg(&a.cnt[(L % 3) * WGM_LINE]);
+  const size_t in_off = (size_t)(L & 1) * a.cap, out_off = (size_t)((L + 1) & 1) * a.cap;
+  const int *i_start = a.wl_start + in_off, *i_cnt = a.wl_cnt + in_off;
+  const int *i_u = a.wl_u ? a.wl_u + in_off : nullptr;
+  wgm_ls_out o;
+  o.counter = &a.cnt[((L + 1) % 3) * WGM_LINE];
+  o.o_start = a.wl_start + out_off;
+  o.o_cnt = a.wl_cnt + out_off;
+  o.o_u = a.wl_u ? a.wl_u + out_off : nullptr;
+  o.cap = a.cap;
   bool ok = true;
-  auto edge_fn = [&](bool valid, int e, int owner, unsigned dsrc_lane) {
-    unsigned dsrc = SSSP ? __shfl_sync(WGM_FULL, dsrc_lane, owner) : 0u;
-    int u = 0;
-    bool push = valid && wgm_ls_relax<SSSP>(a, e, dsrc, L, &u);
-    bool big = push && (wgm_ls_degree(a.row, u) > a.hub_threshold);
-    ok &= wgm_warp_push(push && !big, u, cnt_small_out, out, V, false);
-    ok &= wgm_warp_push(big, u, cnt_big_out, out, V, true);
-  };
-  /* Small items: each warp takes 32 consecutive worklist entries. */
-  for (int b = gw * 32; b < ns; b += NW * 32) {
-    int i = b + lane, v = -1, deg = 0, start = 0;
+  for (int b = gw * 32; b < n; b += NW * 32) {
+    int i = b + lane, deg = 0, start = 0;
     unsigned dv = 0;
-    if (i < ns) {
-      v = __ldcg(&in[i]);
-      start = __ldg(&a.row[v]);
-      deg = wgm_ls_degree(a.row, v);
-      if (SSSP) dv = __ldcg(&a.dist[v]);
+    if (i < n) {
+      start = __ldcg(&i_start[i]);
+      deg = __ldcg(&i_cnt[i]);
+      if (SSSP) dv = __ldcg(&a.dist[__ldcg(&i_u[i])]);
     }
-    int incl = wgm_warp_incl_scan(deg);
-    int total = __shfl_sync(WGM_FULL, incl, 31);
-    int off = incl - deg;
-    wgm_for_each_edge(off, deg, start - off, total, 0, 32, sm->tab[warp],
-                      [&](bool valid, int e, int owner) { edge_fn(valid, e, owner, dv); });
+    ok &= wgm_ls_chunk<SSSP>(a.row, a.col, a.wt, a.dist, a.stamp, a.V, a.piece, L, start, deg,
+                             dv, o);
   }
-  /* Hub items (stored at the back of the list): every warp of the grid
-   * takes a share of the windows of each batch of 32 hubs. */
-  for (int hb = 0; hb < nb; hb += 32) {
-    int i = hb + lane, v = -1, deg = 0, start = 0;
-    unsigned dv = 0;
-    if (i < nb) {
-      v = __ldcg(&in[V - 1 - i]);
-      start = __ldg(&a.row[v]);
-      deg = wgm_ls_degree(a.row, v);
-      if (SSSP) dv = __ldcg(&a.dist[v]);
-    }
-    int incl = wgm_warp_incl_scan(deg);
-    int total = __shfl_sync(WGM_FULL, incl, 31);
-    int off = incl - deg;
-    wgm_for_each_edge(off, deg, start - off, total, gw * 32, NW * 32, sm->tab[warp],
-                      [&](bool valid, int e, int owner) { edge_fn(valid, e, owner, dv); });
-  }
+  (void)sm;
   return ok;
 }
 
-/* Persistent BFS/SSSP loop.  One barrier per level (the reference uses two,
- * bfs.cl:282,295): worklist counters are triple-buffered by level, so the
- * counter a level fills was cleared two levels earlier and the swap/reset
- * step needs no barrier of its own. */
+/* Persistent BFS/SSSP phases: (0) device-side init; (1,L) level L.  One
+ * barrier per level (the reference uses two, bfs.cl:282,295): the piece
+ * counters are triple-buffered by level, so the counter a level fills was
+ * cleared two levels earlier and the swap/reset step needs no barrier. */
 template <bool SSSP>
-static __device__ void wgm_app_lonestar(const wgm_launch &Lc, wgm_cta *c,
-                                 const wgm_lonestar_args &a, wgm_warp_smem *sm) {
+static __device__ int wgm_phase_lonestar(const wgm_launch &Lc, wgm_cta *c,
+                                         const wgm_lonestar_args &a, wgm_warp_smem *sm,
+                                         int target, int Lv, int *next_target, int *next_round) {
   const int V = a.V;
-  const int tid = c->id * blockDim.x + threadIdx.x, nth = c->ngroups * blockDim.x;
-  /* Host init of the plugin (bfs.h:250-262) done on the device. */
-  for (int i = tid; i < V; i += nth) {
-    a.dist[i] = (i == a.source) ? 0u : WGM_LONESTAR_INF;
-    if (SSSP) a.stamp[i] = 0;
+  if (target == 0) {
+    const int tid = c->id * blockDim.x + threadIdx.x, nth = c->ngroups * blockDim.x;
+    /* Host init of the plugin (bfs.h:250-262) done on the device. */
+    for (int i = tid; i < V; i += nth) {
+      a.dist[i] = (i == a.source) ? 0u : WGM_LONESTAR_INF;
+      if (SSSP) a.stamp[i] = 0;
+    }
+    if (c->id == 0 && threadIdx.x < 32) {
+      /* Level 1 processes the source (bfs.cl:235-241 seeds it at iteration 0). */
+      if (threadIdx.x == 0)
+        for (int k = 0; k < 3; k++) a.cnt[k * WGM_LINE] = 0;
+      __syncwarp();
+      wgm_ls_push(a, threadIdx.x == 0, a.source, &a.cnt[1 * WGM_LINE], a.wl_start + a.cap,
+                  a.wl_cnt + a.cap, a.wl_u ? a.wl_u + a.cap : nullptr, sm->acc[0]);
+    }
+    *next_target = 1;
+    *next_round = 1;
+    return 1;
   }
-  if (c->id == 0 && threadIdx.x == 0) {
-    for (int k = 0; k < 6; k++) a.cnt[k * WGM_LINE] = 0;
-    /* Level 1 processes the source (bfs.cl:235-241 seeds it at iteration 0). */
-    bool big = wgm_ls_degree(a.row, a.source) > a.hub_threshold;
-    if (big) {
-      a.wl[1 * (size_t)V + V - 1] = a.source;
-      a.cnt[(3 + 1) * WGM_LINE] = 1;
-    } else {
-      a.wl[1 * (size_t)V] = a.source;
-      a.cnt[1 * WGM_LINE] = 1;
-    }
+  int n = __ldcg(&a.cnt[(Lv % 3) * WGM_LINE]);
+  if (n == 0) {
+    if (c->id == 0 && threadIdx.x == 0 && a.levels_out) *a.levels_out = Lv;
+    return 0;
   }
-  if (!wgm_barrier(Lc, c)) return;
-  int L = 1;
-  for (;;) {
-    int ns = __ldcg(&a.cnt[(L % 3) * WGM_LINE]);
-    int nb = __ldcg(&a.cnt[(3 + L % 3) * WGM_LINE]);
-    if (ns + nb == 0) break;
-    if (ns + nb > V) {
-      wgm_fail(Lc, WGM_DEV_OVERFLOW, WGM_SITE_QUEUE, L);
-      return;
-    }
-    if (L > V + 2) { /* Bellman-Ford bound; only a corrupt input gets here */
-      wgm_fail(Lc, WGM_DEV_BAD_INPUT, WGM_SITE_QUEUE, L);
-      return;
-    }
-    if (c->id == 0 && threadIdx.x == 0) {
-      a.cnt[((L + 2) % 3) * WGM_LINE] = 0;
-      a.cnt[(3 + (L + 2) % 3) * WGM_LINE] = 0;
-    }
-    if (!wgm_ls_level<SSSP>(Lc, c, a, L, sm)) wgm_fail(Lc, WGM_DEV_OVERFLOW, WGM_SITE_QUEUE, L);
-    if (!wgm_barrier(Lc, c)) return;
-    L++;
+  if (n > a.cap) {
+    wgm_fail(Lc, WGM_DEV_OVERFLOW, WGM_SITE_QUEUE, Lv);
+    return 0;
   }
-  if (c->id == 0 && threadIdx.x == 0 && a.levels_out) *a.levels_out = L;
+  if (Lv > V + 2) { /* Bellman-Ford bound; only a corrupt input gets here */
+    wgm_fail(Lc, WGM_DEV_BAD_INPUT, WGM_SITE_QUEUE, Lv);
+    return 0;
+  }
+  if (c->id == 0 && threadIdx.x == 0) a.cnt[((Lv + 2) % 3) * WGM_LINE] = 0;
+  if (!wgm_ls_level<SSSP>(Lc, c, a, Lv, sm)) wgm_fail(Lc, WGM_DEV_OVERFLOW, WGM_SITE_QUEUE, Lv);
+  *next_target = 1;
+  *next_round = Lv + 1;
+  return 1;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Resumable phases                                                          */
+/* ------------------------------------------------------------------------ */
+
+/* Every app runs as a sequence of phases separated by inter-CTA barriers.
+ * A phase is named by (target, round); target 0 is the device-side init.
+ * A phase function does its work, names the next phase and returns
+ * WGM_PHASE_NEXT (a barrier follows) or WGM_PHASE_DONE.  Everything a phase
+ * needs is in global memory or derivable from (target, round), so a group
+ * forked in at a resizing barrier starts at the next phase with nothing but
+ * that pair: the role of the reference's generated Restoration_ctx and its
+ * `switch (target)` resume points (lonestar/graph_apps/bfs/device/
+ * merged.cl:310-397, kernel_merge/src/ProcessPersistentKernelVisitor.cpp:
+ * 110-137,401-431). */
+struct wgm_step {
+  int target;
+  int round;
+};
+#define WGM_PHASE_DONE 0
+#define WGM_PHASE_NEXT 1
+
+/* Work split of the current phase: group id and group count can change at
+ * every resizing barrier, so each phase reads them afresh. */
+struct wgm_split {
+  int lane, warp, gw, NW, tid, nth;
+  __device__ __forceinline__ explicit wgm_split(const wgm_cta *c) {
+    lane = wgm_lane();
+    warp = threadIdx.x >> 5;
+    const int nw = blockDim.x >> 5;
+    gw = c->id * nw + warp;
+    NW = c->ngroups * nw;
+    tid = c->id * blockDim.x + threadIdx.x;
+    nth = c->ngroups * blockDim.x;
+  }
+};
+
+/* Run phases from `cur` until done, with `sync` between phases. */
+template <class Sync, class Phase>
+__device__ __forceinline__ void wgm_drive(const wgm_launch &L, wgm_cta *c, wgm_step cur,
+                                          Sync &&sync, Phase &&phase) {
+  for (;;) {
+    wgm_step nxt = cur;
+    if (phase(cur, &nxt) != WGM_PHASE_NEXT) return;
+    if (!sync(L, c, nxt)) return;
+    cur = nxt;
+  }
+}
+
+/* Plain barrier between phases (standalone persistent kernels). */
+struct wgm_plain_sync {
+  __device__ __forceinline__ bool operator()(const wgm_launch &L, wgm_cta *c, wgm_step) const {
+    return wgm_barrier(L, c);
+  }
+};
 
 /* ------------------------------------------------------------------------ */
 /* Pannotia colour                                                           */
@@ -301,104 +502,105 @@ __device__ __forceinline__ bool wgm_uncoloured_at(int cval, int r) {
   return cval == -1 || cval == r;
 }
 
-/* One barrier per round when no hub is uncoloured, two otherwise (the
- * reference uses two every round).  Round r fuses color1 and color2 for every
- * non-hub vertex: max over the neighbours uncoloured at round start (skipping
- * all neighbours of degree-1 vertices, color.cl:46), then colour r if the
- * vertex's value is larger (color.cl:78-81).  Hub maxima accumulate in
- * hub_acc across the grid and are decided after the first barrier. */
-static __device__ void wgm_app_color(const wgm_launch &Lc, wgm_cta *c, const wgm_color_args &a,
-                              wgm_warp_smem *sm) {
-  const int lane = wgm_lane(), warp = threadIdx.x >> 5;
-  const int nwarps_cta = blockDim.x >> 5;
-  const int gw = c->id * nwarps_cta + warp, NW = c->ngroups * nwarps_cta;
-  const int tid = c->id * blockDim.x + threadIdx.x, nth = c->ngroups * blockDim.x;
+/* Phases: (0) init; (1,r) round r for every non-hub vertex - colour1 and
+ * colour2 fused: max over the neighbours uncoloured at round start (skipping
+ * all neighbours of degree-1 vertices, color.cl:46), colour r if the vertex's
+ * value is larger (color.cl:78-81) - while hub maxima accumulate over the
+ * grid; (2,r) hub decisions.  One barrier per round when there are no hubs,
+ * two otherwise (the reference uses two every round).  Phase (1,r) first
+ * applies the reference's exit test to round r-1 (color.cl:85-87). */
+static __device__ int wgm_phase_color(const wgm_launch &Lc, wgm_cta *c, const wgm_color_args &a,
+                                      wgm_warp_smem *sm, wgm_step cur, wgm_step *nxt) {
+  const wgm_split s(c);
   const int V = a.V;
   const int NEG1 = __float_as_int(-1.0f);
-  for (int i = tid; i < V; i += nth) a.color[i] = -1; /* color.h:50 */
-  for (int h = tid; h < a.hubs.H; h += nth) a.hub_acc[h] = NEG1;
-  if (c->id == 0 && threadIdx.x == 0)
-    for (int k = 0; k < 3; k++) a.stop[k * WGM_LINE] = 0;
-  if (!wgm_barrier(Lc, c)) return;
-  int r = 1;
-  for (;;) {
-    if (r > V + 2) { /* every round settles at least one vertex of a valid input */
-      wgm_fail(Lc, WGM_DEV_BAD_INPUT, WGM_SITE_QUEUE, r);
-      return;
-    }
-    if (c->id == 0 && threadIdx.x == 0) a.stop[((r + 1) % 3) * WGM_LINE] = 0;
-    bool any = false;
-    /* Non-hub vertices. */
-    for (int b = gw * 32; b < V; b += NW * 32) {
-      int i = b + lane;
-      int deg = 0, start = 0;
-      bool unc = false;
-      if (i < V) {
-        unc = __ldcg(&a.color[i]) == -1;
-        start = __ldg(&a.row[i]);
-        int d = __ldg(&a.row[i + 1]) - start;
-        if (unc && d <= a.hub_threshold) deg = (d == 1) ? 0 : d;
-        if (d > a.hub_threshold) unc = false;
-      }
-      sm->acc[warp][lane] = NEG1;
-      int incl = wgm_warp_incl_scan(deg);
-      int total = __shfl_sync(WGM_FULL, incl, 31);
-      int off = incl - deg;
-      __syncwarp();
-      wgm_for_each_edge(off, deg, start - off, total, 0, 32, sm->tab[warp],
-                        [&](bool valid, int e, int owner) {
-                          if (valid) {
-                            int j = __ldg(&a.col[e]);
-                            if (wgm_uncoloured_at(__ldcg(&a.color[j]), r)) {
-                              any = true;
-                              atomicMax(&sm->acc[warp][owner],
-                                        __float_as_int(__ldg(&a.node_value[j])));
-                            }
-                          }
-                        });
-      __syncwarp();
-      if (unc && __ldg(&a.node_value[i]) > __int_as_float(sm->acc[warp][lane]))
-        a.color[i] = r;
-    }
-    /* Hubs still uncoloured: spread their edges over every warp. */
-    int nwin = (a.hubs.total + 31) >> 5;
-    for (int k = gw; k < nwin; k += NW) {
-      wgm_hub_window(a.hubs, a.row, k, [&](bool valid, int h, int e) {
-        int h0 = __shfl_sync(WGM_FULL, h, 0);
-        int val = INT_MIN;
-        if (valid && __ldcg(&a.color[__ldg(&a.hubs.ids[h])]) == -1) {
-          int j = __ldg(&a.col[e]);
-          if (wgm_uncoloured_at(__ldcg(&a.color[j]), r)) {
-            any = true;
-            val = __float_as_int(__ldg(&a.node_value[j]));
-          }
-        }
-        int m0, m1;
-        float f0, f1;
-        wgm_two_seg_reduce(h == h0, val, 0.f, 0, &m0, &m1, &f0, &f1);
-        if (lane == 0) {
-          if (m0 != INT_MIN) atomicMax(&a.hub_acc[h0], m0);
-          if (m1 != INT_MIN && h0 + 1 < a.hubs.H) atomicMax(&a.hub_acc[h0 + 1], m1);
-        }
-      });
-    }
-    if (__any_sync(WGM_FULL, any) && lane == 0) a.stop[(r % 3) * WGM_LINE] = 1;
-    if (!wgm_barrier(Lc, c)) return;
-    if (a.hubs.H > 0) {
-      /* Hub decisions (color.cl:77-81 for hubs), then reset the maxima. */
-      for (int h = tid; h < a.hubs.H; h += nth) {
-        int v = __ldg(&a.hubs.ids[h]);
-        if (__ldcg(&a.color[v]) == -1 &&
-            __ldg(&a.node_value[v]) > __int_as_float(__ldcg(&a.hub_acc[h])))
-          a.color[v] = r;
-        a.hub_acc[h] = NEG1;
-      }
-      if (!wgm_barrier(Lc, c)) return;
-    }
-    if (__ldcg(&a.stop[(r % 3) * WGM_LINE]) == 0) break; /* color.cl:85-87 */
-    r++;
+  if (cur.target == 0) {
+    for (int i = s.tid; i < V; i += s.nth) a.color[i] = -1; /* color.h:50 */
+    for (int h = s.tid; h < a.hubs.H; h += s.nth) a.hub_acc[h] = NEG1;
+    if (c->id == 0 && threadIdx.x == 0)
+      for (int k = 0; k < 3; k++) a.stop[k * WGM_LINE] = 0;
+    *nxt = {1, 1};
+    return WGM_PHASE_NEXT;
   }
-  if (c->id == 0 && threadIdx.x == 0 && a.rounds_out) *a.rounds_out = r;
+  const int r = cur.round;
+  if (cur.target == 2) {
+    /* Hub decisions (color.cl:77-81 for hubs), then reset the maxima. */
+    for (int h = s.tid; h < a.hubs.H; h += s.nth) {
+      int v = __ldg(&a.hubs.ids[h]);
+      if (__ldcg(&a.color[v]) == -1 &&
+          __ldg(&a.node_value[v]) > __int_as_float(__ldcg(&a.hub_acc[h])))
+        a.color[v] = r;
+      a.hub_acc[h] = NEG1;
+    }
+    *nxt = {1, r + 1};
+    return WGM_PHASE_NEXT;
+  }
+  if (r > 1 && __ldcg(&a.stop[((r - 1) % 3) * WGM_LINE]) == 0) {
+    if (c->id == 0 && threadIdx.x == 0 && a.rounds_out) *a.rounds_out = r - 1;
+    return WGM_PHASE_DONE;
+  }
+  if (r > V + 2) { /* every round colours at least one vertex of a valid input */
+    wgm_fail(Lc, WGM_DEV_BAD_INPUT, WGM_SITE_QUEUE, r);
+    return WGM_PHASE_DONE;
+  }
+  if (c->id == 0 && threadIdx.x == 0) a.stop[((r + 1) % 3) * WGM_LINE] = 0;
+  bool any = false;
+  const int lane = s.lane, warp = s.warp;
+  for (int b = s.gw * 32; b < V; b += s.NW * 32) {
+    int i = b + lane;
+    int deg = 0, start = 0;
+    bool unc = false;
+    if (i < V) {
+      unc = __ldcg(&a.color[i]) == -1;
+      start = __ldg(&a.row[i]);
+      int d = __ldg(&a.row[i + 1]) - start;
+      if (unc && d <= a.hub_threshold) deg = (d == 1) ? 0 : d;
+      if (d > a.hub_threshold) unc = false;
+    }
+    sm->acc[warp][lane] = NEG1;
+    int incl = wgm_warp_incl_scan(deg);
+    int total = __shfl_sync(WGM_FULL, incl, 31);
+    int off = incl - deg;
+    __syncwarp();
+    wgm_for_each_edge(off, deg, start - off, total, 0, 32, sm->tab[warp],
+                      [&](bool valid, int e, int owner) {
+                        if (valid) {
+                          int j = __ldg(&a.col[e]);
+                          if (wgm_uncoloured_at(__ldcg(&a.color[j]), r)) {
+                            any = true;
+                            atomicMax(&sm->acc[warp][owner],
+                                      __float_as_int(__ldg(&a.node_value[j])));
+                          }
+                        }
+                      });
+    __syncwarp();
+    if (unc && __ldg(&a.node_value[i]) > __int_as_float(sm->acc[warp][lane])) a.color[i] = r;
+  }
+  /* Hubs still uncoloured: spread their edges over every warp. */
+  int nwin = (a.hubs.total + 31) >> 5;
+  for (int k = s.gw; k < nwin; k += s.NW) {
+    wgm_hub_window(a.hubs, a.row, k, [&](bool valid, int h, int e) {
+      int h0 = __shfl_sync(WGM_FULL, h, 0);
+      int val = INT_MIN;
+      if (valid && __ldcg(&a.color[__ldg(&a.hubs.ids[h])]) == -1) {
+        int j = __ldg(&a.col[e]);
+        if (wgm_uncoloured_at(__ldcg(&a.color[j]), r)) {
+          any = true;
+          val = __float_as_int(__ldg(&a.node_value[j]));
+        }
+      }
+      int m0, m1;
+      float f0, f1;
+      wgm_two_seg_reduce(h == h0, val, 0.f, 0, &m0, &m1, &f0, &f1);
+      if (lane == 0) {
+        if (m0 != INT_MIN) atomicMax(&a.hub_acc[h0], m0);
+        if (m1 != INT_MIN && h0 + 1 < a.hubs.H) atomicMax(&a.hub_acc[h0 + 1], m1);
+      }
+    });
+  }
+  if (__any_sync(WGM_FULL, any) && lane == 0) a.stop[(r % 3) * WGM_LINE] = 1;
+  *nxt = (a.hubs.H > 0) ? wgm_step{2, r} : wgm_step{1, r + 1};
+  return WGM_PHASE_NEXT;
 }
 
 /* ------------------------------------------------------------------------ */
@@ -430,133 +632,139 @@ __device__ __forceinline__ bool wgm_active_at(int st, int r) {
   return st == -1 || (st >> 1) == r;
 }
 
-static __device__ void wgm_app_mis(const wgm_launch &Lc, wgm_cta *c, const wgm_mis_args &a,
-                            wgm_warp_smem *sm) {
-  const int lane = wgm_lane(), warp = threadIdx.x >> 5;
-  const int nwarps_cta = blockDim.x >> 5;
-  const int gw = c->id * nwarps_cta + warp, NW = c->ngroups * nwarps_cta;
-  const int tid = c->id * blockDim.x + threadIdx.x, nth = c->ngroups * blockDim.x;
+/* Phases: (0) init; (1,r) mis1+mis2 for non-hub vertices and hub minima over
+ * the grid; (2,r) mis2 for hubs.  (1,r) first applies the reference's exit
+ * test to round r-1 (mis.cl:106-108). */
+static __device__ int wgm_phase_mis(const wgm_launch &Lc, wgm_cta *c, const wgm_mis_args &a,
+                                    wgm_warp_smem *sm, wgm_step cur, wgm_step *nxt) {
+  const wgm_split s(c);
   const int V = a.V;
   const int BIG = __float_as_int((float)WGM_PANNOTIA_BIG);
-  for (int i = tid; i < V; i += nth) {
-    a.s_array[i] = 0; /* mis.h:58-92 */
-    a.status[i] = -1;
+  if (cur.target == 0) {
+    for (int i = s.tid; i < V; i += s.nth) {
+      a.s_array[i] = 0; /* mis.h:58-92 */
+      a.status[i] = -1;
+    }
+    for (int h = s.tid; h < 2 * a.hubs.H; h += s.nth) a.hub_acc[h] = BIG;
+    if (c->id == 0 && threadIdx.x == 0)
+      for (int k = 0; k < 3; k++) a.stop[k * WGM_LINE] = 0;
+    *nxt = {1, 1};
+    return WGM_PHASE_NEXT;
   }
-  for (int h = tid; h < 2 * a.hubs.H; h += nth) a.hub_acc[h] = BIG;
-  if (c->id == 0 && threadIdx.x == 0)
-    for (int k = 0; k < 3; k++) a.stop[k * WGM_LINE] = 0;
-  if (!wgm_barrier(Lc, c)) return;
-  int r = 1;
-  for (;;) {
-    if (r > V + 2) { /* every round settles at least one vertex of a valid input */
-      wgm_fail(Lc, WGM_DEV_BAD_INPUT, WGM_SITE_QUEUE, r);
-      return;
-    }
-    if (c->id == 0 && threadIdx.x == 0) a.stop[((r + 1) % 3) * WGM_LINE] = 0;
-    int *hacc = a.hub_acc + (size_t)(r & 1) * a.hubs.H;
-    bool any = false;
-    for (int b = gw * 32; b < V; b += NW * 32) {
-      int i = b + lane;
-      int deg = 0, start = 0;
-      bool act = false;
-      if (i < V) {
-        act = __ldcg(&a.status[i]) == -1; /* active: nothing else can stamp it yet */
-        start = __ldg(&a.row[i]);
-        int d = __ldg(&a.row[i + 1]) - start;
-        if (act) any = true; /* mis.cl:33 */
-        if (d > a.hub_threshold) act = false;
-        else if (act) deg = d;
+  const int r = cur.round;
+  int *hacc = a.hub_acc + (size_t)(r & 1) * a.hubs.H;
+  const int nwin = (a.hubs.total + 31) >> 5;
+  if (cur.target == 2) {
+    /* mis2 for hubs.  The join test is a pure function of the final hub
+     * minimum and the round-start status (a joined hub reads 2r+1, still
+     * "active at r"), so every warp re-derives it while marking neighbours
+     * and one thread per hub records the join.  The other parity's minima
+     * are reset here for the next round. */
+    int *hnext = a.hub_acc + (size_t)((r + 1) & 1) * a.hubs.H;
+    for (int h = s.tid; h < a.hubs.H; h += s.nth) {
+      int v = __ldg(&a.hubs.ids[h]);
+      if (__ldcg(&a.status[v]) == -1 &&
+          __ldg(&a.node_value[v]) < __int_as_float(__ldcg(&hacc[h]))) {
+        a.s_array[v] = 2;
+        a.status[v] = 2 * r + 1;
       }
-      sm->acc[warp][lane] = BIG;
-      int incl = wgm_warp_incl_scan(deg);
-      int total = __shfl_sync(WGM_FULL, incl, 31);
-      int off = incl - deg;
-      __syncwarp();
-      /* mis1: min over neighbours active at round start (mis.cl:44-51). */
-      wgm_for_each_edge(off, deg, start - off, total, 0, 32, sm->tab[warp],
-                        [&](bool valid, int e, int owner) {
-                          if (valid) {
-                            int j = __ldg(&a.col[e]);
-                            if (wgm_active_at(__ldcg(&a.status[j]), r))
-                              atomicMin(&sm->acc[warp][owner],
-                                        __float_as_int(__ldg(&a.node_value[j])));
-                          }
-                        });
-      __syncwarp();
-      /* mis2: join, then mark the neighbours removed (mis.cl:68-95). */
-      bool join = act && __ldg(&a.node_value[i]) < __int_as_float(sm->acc[warp][lane]);
-      if (join) {
-        a.s_array[i] = 2;
-        a.status[i] = 2 * r + 1;
-      }
-      int jdeg = join ? deg : 0;
-      int jincl = wgm_warp_incl_scan(jdeg);
-      int jtotal = __shfl_sync(WGM_FULL, jincl, 31);
-      int joff = jincl - jdeg;
-      wgm_for_each_edge(joff, jdeg, start - joff, jtotal, 0, 32, sm->tab[warp],
-                        [&](bool valid, int e, int owner) {
-                          if (valid) {
-                            int j = __ldg(&a.col[e]);
-                            if (wgm_active_at(__ldcg(&a.status[j]), r)) a.status[j] = 2 * r;
-                          }
-                        });
+      hnext[h] = BIG;
     }
-    /* Hub minima across the grid (mis1 for hubs). */
-    int nwin = (a.hubs.total + 31) >> 5;
-    for (int k = gw; k < nwin; k += NW) {
+    for (int k = s.gw; k < nwin; k += s.NW) {
       wgm_hub_window(a.hubs, a.row, k, [&](bool valid, int h, int e) {
-        int h0 = __shfl_sync(WGM_FULL, h, 0);
-        int val = INT_MAX;
-        if (valid && wgm_active_at(__ldcg(&a.status[__ldg(&a.hubs.ids[h])]), r)) {
+        if (!valid) return;
+        int v = __ldg(&a.hubs.ids[h]);
+        int stv = __ldcg(&a.status[v]);
+        if (wgm_active_at(stv, r) && stv != 2 * r &&
+            __ldg(&a.node_value[v]) < __int_as_float(__ldcg(&hacc[h]))) {
           int j = __ldg(&a.col[e]);
-          if (wgm_active_at(__ldcg(&a.status[j]), r))
-            val = __float_as_int(__ldg(&a.node_value[j]));
-        }
-        int m0, m1;
-        float f0, f1;
-        wgm_two_seg_reduce(h == h0, val, 0.f, 1, &m0, &m1, &f0, &f1);
-        if (lane == 0) {
-          if (m0 != INT_MAX) atomicMin(&hacc[h0], m0);
-          if (m1 != INT_MAX && h0 + 1 < a.hubs.H) atomicMin(&hacc[h0 + 1], m1);
+          if (wgm_active_at(__ldcg(&a.status[j]), r) && j != v) a.status[j] = 2 * r;
         }
       });
     }
-    if (__any_sync(WGM_FULL, any) && lane == 0) a.stop[(r % 3) * WGM_LINE] = 1;
-    if (!wgm_barrier(Lc, c)) return;
-    if (a.hubs.H > 0) {
-      /* mis2 for hubs.  The join test is a pure function of the final hub
-       * minimum and the round-start status (a joined hub reads 2r+1, still
-       * "active at r"), so every warp re-derives it while marking neighbours
-       * and one thread per hub records the join.  The other parity's minima
-       * are reset here for the next round. */
-      int *hnext = a.hub_acc + (size_t)((r + 1) & 1) * a.hubs.H;
-      for (int h = tid; h < a.hubs.H; h += nth) {
-        int v = __ldg(&a.hubs.ids[h]);
-        if (__ldcg(&a.status[v]) == -1 &&
-            __ldg(&a.node_value[v]) < __int_as_float(__ldcg(&hacc[h]))) {
-          a.s_array[v] = 2;
-          a.status[v] = 2 * r + 1;
-        }
-        hnext[h] = BIG;
-      }
-      for (int k = gw; k < nwin; k += NW) {
-        wgm_hub_window(a.hubs, a.row, k, [&](bool valid, int h, int e) {
-          if (!valid) return;
-          int v = __ldg(&a.hubs.ids[h]);
-          int stv = __ldcg(&a.status[v]);
-          if (wgm_active_at(stv, r) && stv != 2 * r &&
-              __ldg(&a.node_value[v]) < __int_as_float(__ldcg(&hacc[h]))) {
-            int j = __ldg(&a.col[e]);
-            if (wgm_active_at(__ldcg(&a.status[j]), r) && j != v) a.status[j] = 2 * r;
-          }
-        });
-      }
-      if (!wgm_barrier(Lc, c)) return;
-    }
-    if (__ldcg(&a.stop[(r % 3) * WGM_LINE]) == 0) break; /* mis.cl:106-108 */
-    r++;
+    *nxt = {1, r + 1};
+    return WGM_PHASE_NEXT;
   }
-  if (c->id == 0 && threadIdx.x == 0 && a.rounds_out) *a.rounds_out = r;
+  if (r > 1 && __ldcg(&a.stop[((r - 1) % 3) * WGM_LINE]) == 0) {
+    if (c->id == 0 && threadIdx.x == 0 && a.rounds_out) *a.rounds_out = r - 1;
+    return WGM_PHASE_DONE;
+  }
+  if (r > V + 2) {
+    wgm_fail(Lc, WGM_DEV_BAD_INPUT, WGM_SITE_QUEUE, r);
+    return WGM_PHASE_DONE;
+  }
+  if (c->id == 0 && threadIdx.x == 0) a.stop[((r + 1) % 3) * WGM_LINE] = 0;
+  bool any = false;
+  const int lane = s.lane, warp = s.warp;
+  for (int b = s.gw * 32; b < V; b += s.NW * 32) {
+    int i = b + lane;
+    int deg = 0, start = 0;
+    bool act = false;
+    if (i < V) {
+      act = __ldcg(&a.status[i]) == -1; /* active: nothing else can stamp it yet */
+      start = __ldg(&a.row[i]);
+      int d = __ldg(&a.row[i + 1]) - start;
+      if (act) any = true; /* mis.cl:33 */
+      if (d > a.hub_threshold)
+        act = false;
+      else if (act)
+        deg = d;
+    }
+    sm->acc[warp][lane] = BIG;
+    int incl = wgm_warp_incl_scan(deg);
+    int total = __shfl_sync(WGM_FULL, incl, 31);
+    int off = incl - deg;
+    __syncwarp();
+    /* mis1: min over neighbours active at round start (mis.cl:44-51). */
+    wgm_for_each_edge(off, deg, start - off, total, 0, 32, sm->tab[warp],
+                      [&](bool valid, int e, int owner) {
+                        if (valid) {
+                          int j = __ldg(&a.col[e]);
+                          if (wgm_active_at(__ldcg(&a.status[j]), r))
+                            atomicMin(&sm->acc[warp][owner],
+                                      __float_as_int(__ldg(&a.node_value[j])));
+                        }
+                      });
+    __syncwarp();
+    /* mis2: join, then mark the neighbours removed (mis.cl:68-95). */
+    bool join = act && __ldg(&a.node_value[i]) < __int_as_float(sm->acc[warp][lane]);
+    if (join) {
+      a.s_array[i] = 2;
+      a.status[i] = 2 * r + 1;
+    }
+    int jdeg = join ? deg : 0;
+    int jincl = wgm_warp_incl_scan(jdeg);
+    int jtotal = __shfl_sync(WGM_FULL, jincl, 31);
+    int joff = jincl - jdeg;
+    wgm_for_each_edge(joff, jdeg, start - joff, jtotal, 0, 32, sm->tab[warp],
+                      [&](bool valid, int e, int owner) {
+                        if (valid) {
+                          int j = __ldg(&a.col[e]);
+                          if (wgm_active_at(__ldcg(&a.status[j]), r)) a.status[j] = 2 * r;
+                        }
+                      });
+  }
+  /* Hub minima across the grid (mis1 for hubs). */
+  for (int k = s.gw; k < nwin; k += s.NW) {
+    wgm_hub_window(a.hubs, a.row, k, [&](bool valid, int h, int e) {
+      int h0 = __shfl_sync(WGM_FULL, h, 0);
+      int val = INT_MAX;
+      if (valid && wgm_active_at(__ldcg(&a.status[__ldg(&a.hubs.ids[h])]), r)) {
+        int j = __ldg(&a.col[e]);
+        if (wgm_active_at(__ldcg(&a.status[j]), r)) val = __float_as_int(__ldg(&a.node_value[j]));
+      }
+      int m0, m1;
+      float f0, f1;
+      wgm_two_seg_reduce(h == h0, val, 0.f, 1, &m0, &m1, &f0, &f1);
+      if (lane == 0) {
+        if (m0 != INT_MAX) atomicMin(&hacc[h0], m0);
+        if (m1 != INT_MAX && h0 + 1 < a.hubs.H) atomicMin(&hacc[h0 + 1], m1);
+      }
+    });
+  }
+  if (__any_sync(WGM_FULL, any) && lane == 0) a.stop[(r % 3) * WGM_LINE] = 1;
+  *nxt = (a.hubs.H > 0) ? wgm_step{2, r} : wgm_step{1, r + 1};
+  return WGM_PHASE_NEXT;
 }
 
 /* ------------------------------------------------------------------------ */
@@ -582,79 +790,82 @@ struct wgm_psssp_args {
  * iteration and this chaotic (in-place) iteration both stop at the fixpoint
  * of the min-plus system started from x = BIG_NUM except x[source] = 0, which
  * is unique (the shortest-path distances, BIG_NUM where unreachable), so the
- * returned vector is identical; only the round count can be smaller. */
-static __device__ void wgm_app_pannotia_sssp(const wgm_launch &Lc, wgm_cta *c,
-                                      const wgm_psssp_args &a, wgm_warp_smem *sm) {
-  const int lane = wgm_lane(), warp = threadIdx.x >> 5;
-  const int nwarps_cta = blockDim.x >> 5;
-  const int gw = c->id * nwarps_cta + warp, NW = c->ngroups * nwarps_cta;
-  const int tid = c->id * blockDim.x + threadIdx.x, nth = c->ngroups * blockDim.x;
+ * returned vector is identical; only the round count can be smaller.
+ * Phases: (0) init; (1,r) one relaxation pass (after the exit test of r-1). */
+static __device__ int wgm_phase_pannotia_sssp(const wgm_launch &Lc, wgm_cta *c,
+                                              const wgm_psssp_args &a, wgm_warp_smem *sm,
+                                              wgm_step cur, wgm_step *nxt) {
+  const wgm_split s(c);
   const int V = a.V;
-  for (int i = tid; i < V; i += nth) a.x[i] = (i == a.source) ? 0 : WGM_PANNOTIA_BIG;
-  if (c->id == 0 && threadIdx.x == 0)
-    for (int k = 0; k < 3; k++) a.stop[k * WGM_LINE] = 0;
-  if (!wgm_barrier(Lc, c)) return;
-  int r = 1;
-  for (;;) {
-    if (r > V + 2) { /* every round settles at least one vertex of a valid input */
-      wgm_fail(Lc, WGM_DEV_BAD_INPUT, WGM_SITE_QUEUE, r);
-      return;
-    }
-    if (c->id == 0 && threadIdx.x == 0) a.stop[((r + 1) % 3) * WGM_LINE] = 0;
-    bool changed = false;
-    for (int b = gw * 32; b < V; b += NW * 32) {
-      int i = b + lane, deg = 0, start = 0;
-      if (i < V) {
-        start = __ldg(&a.row[i]);
-        int d = __ldg(&a.row[i + 1]) - start;
-        deg = d > a.hub_threshold ? 0 : d;
-      }
-      sm->acc[warp][lane] = INT_MAX;
-      int incl = wgm_warp_incl_scan(deg);
-      int total = __shfl_sync(WGM_FULL, incl, 31);
-      int off = incl - deg;
-      __syncwarp();
-      wgm_for_each_edge(off, deg, start - off, total, 0, 32, sm->tab[warp],
-                        [&](bool valid, int e, int owner) {
-                          if (valid) {
-                            int cand = __ldg(&a.data[e]) + __ldcg(&a.x[__ldg(&a.col[e])]);
-                            atomicMin(&sm->acc[warp][owner], cand);
-                          }
-                        });
-      __syncwarp();
-      if (deg > 0) {
-        int cand = sm->acc[warp][lane];
-        if (cand < __ldcg(&a.x[i])) {
-          atomicMin(&a.x[i], cand);
-          changed = true;
-        }
-      }
-    }
-    int nwin = (a.hubs.total + 31) >> 5;
-    for (int k = gw; k < nwin; k += NW) {
-      wgm_hub_window(a.hubs, a.row, k, [&](bool valid, int h, int e) {
-        int h0 = __shfl_sync(WGM_FULL, h, 0);
-        int val = INT_MAX;
-        if (valid) val = __ldg(&a.data[e]) + __ldcg(&a.x[__ldg(&a.col[e])]);
-        int m0, m1;
-        float f0, f1;
-        wgm_two_seg_reduce(h == h0, val, 0.f, 1, &m0, &m1, &f0, &f1);
-        if (lane == 0) {
-          int v0 = __ldg(&a.hubs.ids[h0]);
-          if (m0 < __ldcg(&a.x[v0]) && atomicMin(&a.x[v0], m0) > m0) changed = true;
-          if (h0 + 1 < a.hubs.H && m1 != INT_MAX) {
-            int v1 = __ldg(&a.hubs.ids[h0 + 1]);
-            if (m1 < __ldcg(&a.x[v1]) && atomicMin(&a.x[v1], m1) > m1) changed = true;
-          }
-        }
-      });
-    }
-    if (__any_sync(WGM_FULL, changed) && lane == 0) a.stop[(r % 3) * WGM_LINE] = 1;
-    if (!wgm_barrier(Lc, c)) return;
-    if (__ldcg(&a.stop[(r % 3) * WGM_LINE]) == 0) break;
-    r++;
+  if (cur.target == 0) {
+    for (int i = s.tid; i < V; i += s.nth) a.x[i] = (i == a.source) ? 0 : WGM_PANNOTIA_BIG;
+    if (c->id == 0 && threadIdx.x == 0)
+      for (int k = 0; k < 3; k++) a.stop[k * WGM_LINE] = 0;
+    *nxt = {1, 1};
+    return WGM_PHASE_NEXT;
   }
-  if (c->id == 0 && threadIdx.x == 0 && a.rounds_out) *a.rounds_out = r;
+  const int r = cur.round;
+  if (r > 1 && __ldcg(&a.stop[((r - 1) % 3) * WGM_LINE]) == 0) {
+    if (c->id == 0 && threadIdx.x == 0 && a.rounds_out) *a.rounds_out = r - 1;
+    return WGM_PHASE_DONE;
+  }
+  if (r > V + 2) {
+    wgm_fail(Lc, WGM_DEV_BAD_INPUT, WGM_SITE_QUEUE, r);
+    return WGM_PHASE_DONE;
+  }
+  if (c->id == 0 && threadIdx.x == 0) a.stop[((r + 1) % 3) * WGM_LINE] = 0;
+  bool changed = false;
+  const int lane = s.lane, warp = s.warp;
+  for (int b = s.gw * 32; b < V; b += s.NW * 32) {
+    int i = b + lane, deg = 0, start = 0;
+    if (i < V) {
+      start = __ldg(&a.row[i]);
+      int d = __ldg(&a.row[i + 1]) - start;
+      deg = d > a.hub_threshold ? 0 : d;
+    }
+    sm->acc[warp][lane] = INT_MAX;
+    int incl = wgm_warp_incl_scan(deg);
+    int total = __shfl_sync(WGM_FULL, incl, 31);
+    int off = incl - deg;
+    __syncwarp();
+    wgm_for_each_edge(off, deg, start - off, total, 0, 32, sm->tab[warp],
+                      [&](bool valid, int e, int owner) {
+                        if (valid) {
+                          int cand = __ldg(&a.data[e]) + __ldcg(&a.x[__ldg(&a.col[e])]);
+                          atomicMin(&sm->acc[warp][owner], cand);
+                        }
+                      });
+    __syncwarp();
+    if (deg > 0) {
+      int cand = sm->acc[warp][lane];
+      if (cand < __ldcg(&a.x[i])) {
+        atomicMin(&a.x[i], cand);
+        changed = true;
+      }
+    }
+  }
+  int nwin = (a.hubs.total + 31) >> 5;
+  for (int k = s.gw; k < nwin; k += s.NW) {
+    wgm_hub_window(a.hubs, a.row, k, [&](bool valid, int h, int e) {
+      int h0 = __shfl_sync(WGM_FULL, h, 0);
+      int val = INT_MAX;
+      if (valid) val = __ldg(&a.data[e]) + __ldcg(&a.x[__ldg(&a.col[e])]);
+      int m0, m1;
+      float f0, f1;
+      wgm_two_seg_reduce(h == h0, val, 0.f, 1, &m0, &m1, &f0, &f1);
+      if (lane == 0) {
+        int v0 = __ldg(&a.hubs.ids[h0]);
+        if (m0 < __ldcg(&a.x[v0]) && atomicMin(&a.x[v0], m0) > m0) changed = true;
+        if (h0 + 1 < a.hubs.H && m1 != INT_MAX) {
+          int v1 = __ldg(&a.hubs.ids[h0 + 1]);
+          if (m1 < __ldcg(&a.x[v1]) && atomicMin(&a.x[v1], m1) > m1) changed = true;
+        }
+      }
+    });
+  }
+  if (__any_sync(WGM_FULL, changed) && lane == 0) a.stop[(r % 3) * WGM_LINE] = 1;
+  *nxt = {1, r + 1};
+  return WGM_PHASE_NEXT;
 }
 
 /* ------------------------------------------------------------------------ */
@@ -673,110 +884,110 @@ struct wgm_pr_args {
   int hub_threshold;
   int iterations;
   float damping;
+  float dang0;     /* initial dangling mass: (zero-degree vertices)/V */
 };
 
-/* pr' = (1-d)/V + d*(sum_{u in N(v)} pr[u]/deg(u) + dangling/V); one barrier
- * per iteration (two when hubs exist: hub sums accumulate over the grid and
- * are finalised after the first).  Per-vertex sums run in a fixed order (a
+/* pr' = (1-d)/V + d*(sum_{u in N(v)} pr[u]/deg(u) + dangling/V).  Phases:
+ * (0) init; (1,t) iteration t for non-hub vertices, hub sums accumulated over
+ * the grid; (2,t) hub finalisation.  Per-vertex sums run in a fixed order (a
  * segmented warp scan per window), so only the dangling mass and hub sums
  * depend on atomic order. */
-static __device__ void wgm_app_pagerank(const wgm_launch &Lc, wgm_cta *c, const wgm_pr_args &a,
-                                 wgm_warp_smem *sm) {
-  const int lane = wgm_lane(), warp = threadIdx.x >> 5;
-  const int nwarps_cta = blockDim.x >> 5;
-  const int gw = c->id * nwarps_cta + warp, NW = c->ngroups * nwarps_cta;
-  const int tid = c->id * blockDim.x + threadIdx.x, nth = c->ngroups * blockDim.x;
+static __device__ int wgm_phase_pagerank(const wgm_launch &Lc, wgm_cta *c, const wgm_pr_args &a,
+                                         wgm_warp_smem *sm, wgm_step cur, wgm_step *nxt) {
+  const wgm_split s(c);
   const int V = a.V;
   const float d = a.damping;
-  float *acc = reinterpret_cast<float *>(sm->acc[warp]);
-  {
-    float dl = 0.f;
-    for (int i = tid; i < V; i += nth) {
+  if (cur.target == 0) {
+    for (int i = s.tid; i < V; i += s.nth) {
       int deg = __ldg(&a.row[i + 1]) - __ldg(&a.row[i]);
       float p = 1.0f / (float)V;
+      a.pr[i] = p;
       a.contrib[i] = deg > 0 ? p / (float)deg : 0.f;
-      if (deg == 0) dl += p;
     }
-    for (int h = tid; h < a.hubs.H; h += nth) a.hub_sum[h] = 0.f;
-    if (c->id == 0 && threadIdx.x == 0)
-      for (int k = 0; k < 3; k++) a.dang[k * WGM_LINE] = 0.f;
-    if (!wgm_barrier(Lc, c)) return;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) dl += __shfl_xor_sync(WGM_FULL, dl, o);
-    if (lane == 0 && dl != 0.f) atomicAdd(&a.dang[0], dl);
-    if (!wgm_barrier(Lc, c)) return;
+    for (int h = s.tid; h < a.hubs.H; h += s.nth) a.hub_sum[h] = 0.f;
+    if (c->id == 0 && threadIdx.x == 0) {
+      a.dang[0] = a.dang0;
+      a.dang[1 * WGM_LINE] = 0.f;
+      a.dang[2 * WGM_LINE] = 0.f;
+    }
+    *nxt = {1, 0};
+    return WGM_PHASE_NEXT;
   }
-  for (int t = 0; t < a.iterations; t++) {
-    const float *cin = a.contrib + (size_t)(t & 1) * V;
-    float *cout = a.contrib + (size_t)((t + 1) & 1) * V;
-    const float base = (1.0f - d) / (float)V + d * __ldcg(&a.dang[(t % 3) * WGM_LINE]) / (float)V;
-    if (c->id == 0 && threadIdx.x == 0) a.dang[((t + 2) % 3) * WGM_LINE] = 0.f;
-    float dl = 0.f;
-    for (int b = gw * 32; b < V; b += NW * 32) {
-      int i = b + lane, deg = 0, start = 0, dfull = 0;
-      if (i < V) {
-        start = __ldg(&a.row[i]);
-        dfull = __ldg(&a.row[i + 1]) - start;
-        deg = dfull > a.hub_threshold ? 0 : dfull;
-      }
-      acc[lane] = 0.f;
-      int incl = wgm_warp_incl_scan(deg);
-      int total = __shfl_sync(WGM_FULL, incl, 31);
-      int off = incl - deg;
-      __syncwarp();
-      wgm_for_each_edge(off, deg, start - off, total, 0, 32, sm->tab[warp],
-                        [&](bool valid, int e, int owner) {
-                          float v = valid ? __ldcg(&cin[__ldg(&a.col[e])]) : 0.f;
-                          /* segmented inclusive scan over lanes with equal owner */
-                          int own = valid ? owner : -1;
-#pragma unroll
-                          for (int o = 1; o < 32; o <<= 1) {
-                            float y = __shfl_up_sync(WGM_FULL, v, o);
-                            int oy = __shfl_up_sync(WGM_FULL, own, o);
-                            if (lane >= o && oy == own) v += y;
-                          }
-                          int nxt = __shfl_down_sync(WGM_FULL, own, 1);
-                          if (own >= 0 && (lane == 31 || nxt != own)) acc[own] += v;
-                          __syncwarp();
-                        });
-      __syncwarp();
-      if (i < V && dfull <= a.hub_threshold) {
-        float p = base + d * acc[lane];
-        a.pr[i] = p;
-        cout[i] = dfull > 0 ? p / (float)dfull : 0.f;
-        if (dfull == 0) dl += p;
-      }
+  const int t = cur.round;
+  const float *cin = a.contrib + (size_t)(t & 1) * V;
+  float *cout = a.contrib + (size_t)((t + 1) & 1) * V;
+  const float base = (1.0f - d) / (float)V + d * __ldcg(&a.dang[(t % 3) * WGM_LINE]) / (float)V;
+  if (cur.target == 2) {
+    for (int h = s.tid; h < a.hubs.H; h += s.nth) {
+      int v = __ldg(&a.hubs.ids[h]);
+      int dg = __ldg(&a.row[v + 1]) - __ldg(&a.row[v]);
+      float p = base + d * __ldcg(&a.hub_sum[h]);
+      a.pr[v] = p;
+      cout[v] = p / (float)dg;
+      a.hub_sum[h] = 0.f;
     }
-    int nwin = (a.hubs.total + 31) >> 5;
-    for (int k = gw; k < nwin; k += NW) {
-      wgm_hub_window(a.hubs, a.row, k, [&](bool valid, int h, int e) {
-        int h0 = __shfl_sync(WGM_FULL, h, 0);
-        float v = valid ? __ldcg(&cin[__ldg(&a.col[e])]) : 0.f;
-        int m0, m1;
-        float f0, f1;
-        wgm_two_seg_reduce(h == h0, 0, v, 2, &m0, &m1, &f0, &f1);
-        if (lane == 0) {
-          atomicAdd(&a.hub_sum[h0], f0);
-          if (h0 + 1 < a.hubs.H && f1 != 0.f) atomicAdd(&a.hub_sum[h0 + 1], f1);
-        }
-      });
+    *nxt = {1, t + 1};
+    return WGM_PHASE_NEXT;
+  }
+  if (t >= a.iterations) return WGM_PHASE_DONE;
+  if (c->id == 0 && threadIdx.x == 0) a.dang[((t + 2) % 3) * WGM_LINE] = 0.f;
+  const int lane = s.lane, warp = s.warp;
+  float *acc = reinterpret_cast<float *>(sm->acc[warp]);
+  float dl = 0.f;
+  for (int b = s.gw * 32; b < V; b += s.NW * 32) {
+    int i = b + lane, deg = 0, start = 0, dfull = 0;
+    if (i < V) {
+      start = __ldg(&a.row[i]);
+      dfull = __ldg(&a.row[i + 1]) - start;
+      deg = dfull > a.hub_threshold ? 0 : dfull;
     }
+    acc[lane] = 0.f;
+    int incl = wgm_warp_incl_scan(deg);
+    int total = __shfl_sync(WGM_FULL, incl, 31);
+    int off = incl - deg;
+    __syncwarp();
+    wgm_for_each_edge(off, deg, start - off, total, 0, 32, sm->tab[warp],
+                      [&](bool valid, int e, int owner) {
+                        float v = valid ? __ldcg(&cin[__ldg(&a.col[e])]) : 0.f;
+                        /* segmented inclusive scan over lanes with equal owner */
+                        int own = valid ? owner : -1;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) dl += __shfl_xor_sync(WGM_FULL, dl, o);
-    if (lane == 0 && dl != 0.f) atomicAdd(&a.dang[((t + 1) % 3) * WGM_LINE], dl);
-    if (!wgm_barrier(Lc, c)) return;
-    if (a.hubs.H > 0) {
-      for (int h = tid; h < a.hubs.H; h += nth) {
-        int v = __ldg(&a.hubs.ids[h]);
-        int dg = __ldg(&a.row[v + 1]) - __ldg(&a.row[v]);
-        float p = base + d * __ldcg(&a.hub_sum[h]);
-        a.pr[v] = p;
-        cout[v] = p / (float)dg;
-        a.hub_sum[h] = 0.f;
-      }
-      if (!wgm_barrier(Lc, c)) return;
+                        for (int o = 1; o < 32; o <<= 1) {
+                          float y = __shfl_up_sync(WGM_FULL, v, o);
+                          int oy = __shfl_up_sync(WGM_FULL, own, o);
+                          if (lane >= o && oy == own) v += y;
+                        }
+                        int nx = __shfl_down_sync(WGM_FULL, own, 1);
+                        if (own >= 0 && (lane == 31 || nx != own)) acc[own] += v;
+                        __syncwarp();
+                      });
+    __syncwarp();
+    if (i < V && dfull <= a.hub_threshold) {
+      float p = base + d * acc[lane];
+      a.pr[i] = p;
+      cout[i] = dfull > 0 ? p / (float)dfull : 0.f;
+      if (dfull == 0) dl += p;
     }
   }
+  int nwin = (a.hubs.total + 31) >> 5;
+  for (int k = s.gw; k < nwin; k += s.NW) {
+    wgm_hub_window(a.hubs, a.row, k, [&](bool valid, int h, int e) {
+      int h0 = __shfl_sync(WGM_FULL, h, 0);
+      float v = valid ? __ldcg(&cin[__ldg(&a.col[e])]) : 0.f;
+      int m0, m1;
+      float f0, f1;
+      wgm_two_seg_reduce(h == h0, 0, v, 2, &m0, &m1, &f0, &f1);
+      if (lane == 0) {
+        atomicAdd(&a.hub_sum[h0], f0);
+        if (h0 + 1 < a.hubs.H && f1 != 0.f) atomicAdd(&a.hub_sum[h0 + 1], f1);
+      }
+    });
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) dl += __shfl_xor_sync(WGM_FULL, dl, o);
+  if (lane == 0 && dl != 0.f) atomicAdd(&a.dang[((t + 1) % 3) * WGM_LINE], dl);
+  *nxt = (a.hubs.H > 0) ? wgm_step{2, t} : wgm_step{1, t + 1};
+  return WGM_PHASE_NEXT;
 }
 
 #endif

@@ -26,6 +26,7 @@ struct wgm_runtime {
   cudaEvent_t tev0 = nullptr, tev1 = nullptr; /* wgm_timer_* */
   int gen = 1;                        /* launch generation */
   int last_cuda = 0;
+  int last_status = 0, last_site = 0, last_detail = 0; /* last device failure */
 };
 
 /* Static hub layout on the device (see wgm_hubs in wgm_graph.cuh). */
@@ -48,12 +49,15 @@ struct wgm_app {
   /* outputs and scratch */
   void *d_out = nullptr;
   size_t out_bytes = 0;
-  int *d_wl = nullptr, *d_cnt = nullptr, *d_stamp = nullptr, *d_stop = nullptr;
+  int *d_wl_start = nullptr, *d_wl_cnt = nullptr, *d_wl_u = nullptr; /* Lonestar pieces */
+  int wl_cap = 0, piece = 32;
+  int *d_cnt = nullptr, *d_stamp = nullptr, *d_stop = nullptr;
   int *d_hub_acc = nullptr, *d_status = nullptr;
   float *d_contrib = nullptr, *d_dang = nullptr, *d_hub_sum = nullptr;
   int *d_rounds = nullptr;
   int source = 0;
   float damping = 0.85f;
+  float dang0 = 0.f;
   int iterations = 20;
   bool has_node_values = false;
 };
@@ -66,5 +70,7 @@ int wgm_finish_launch(wgm_runtime *rt, int *dev_status, int *dev_site);
 bool wgm_host_wait(const volatile int32_t *p, int want, bool equal, uint64_t timeout_ns);
 int wgm_kind_to_kernel(int app_kind);
 int wgm_stream_wait(wgm_runtime *rt, cudaStream_t stream);
+struct wgm_mega_args;
+int wgm_app_fill_mega(wgm_app *a, wgm_mega_args *A);
 
 #endif

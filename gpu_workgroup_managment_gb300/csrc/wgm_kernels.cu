@@ -16,39 +16,52 @@
 #define WGM_PERSISTENT_EPILOGUE \
   if (L.handshake) wgm_standalone_exit(L);
 
+/* Run a phase function from its init phase with plain barriers between. */
+#define WGM_DRIVE(PHASE_CALL)                                                        \
+  wgm_drive(L, &c, wgm_step{0, 0}, wgm_plain_sync(),                                \
+            [&](wgm_step cur, wgm_step *nxt) { return PHASE_CALL; })
+
+template <bool SSSP>
+__device__ __forceinline__ int wgm_lonestar_step(const wgm_launch &L, wgm_cta *c,
+                                                 const wgm_lonestar_args &a, wgm_warp_smem *sm,
+                                                 wgm_step cur, wgm_step *nxt) {
+  return wgm_phase_lonestar<SSSP>(L, c, a, sm, cur.target, cur.round, &nxt->target,
+                                  &nxt->round);
+}
+
 __global__ void __launch_bounds__(1024) wgm_k_bfs(wgm_launch L, wgm_lonestar_args a) {
   WGM_PERSISTENT_PROLOGUE
-  wgm_app_lonestar<false>(L, &c, a, &sm);
+  WGM_DRIVE(wgm_lonestar_step<false>(L, &c, a, &sm, cur, nxt));
   WGM_PERSISTENT_EPILOGUE
 }
 
 __global__ void __launch_bounds__(1024) wgm_k_sssp(wgm_launch L, wgm_lonestar_args a) {
   WGM_PERSISTENT_PROLOGUE
-  wgm_app_lonestar<true>(L, &c, a, &sm);
+  WGM_DRIVE(wgm_lonestar_step<true>(L, &c, a, &sm, cur, nxt));
   WGM_PERSISTENT_EPILOGUE
 }
 
 __global__ void __launch_bounds__(1024) wgm_k_color(wgm_launch L, wgm_color_args a) {
   WGM_PERSISTENT_PROLOGUE
-  wgm_app_color(L, &c, a, &sm);
+  WGM_DRIVE(wgm_phase_color(L, &c, a, &sm, cur, nxt));
   WGM_PERSISTENT_EPILOGUE
 }
 
 __global__ void __launch_bounds__(1024) wgm_k_mis(wgm_launch L, wgm_mis_args a) {
   WGM_PERSISTENT_PROLOGUE
-  wgm_app_mis(L, &c, a, &sm);
+  WGM_DRIVE(wgm_phase_mis(L, &c, a, &sm, cur, nxt));
   WGM_PERSISTENT_EPILOGUE
 }
 
 __global__ void __launch_bounds__(1024) wgm_k_psssp(wgm_launch L, wgm_psssp_args a) {
   WGM_PERSISTENT_PROLOGUE
-  wgm_app_pannotia_sssp(L, &c, a, &sm);
+  WGM_DRIVE(wgm_phase_pannotia_sssp(L, &c, a, &sm, cur, nxt));
   WGM_PERSISTENT_EPILOGUE
 }
 
 __global__ void __launch_bounds__(1024) wgm_k_pagerank(wgm_launch L, wgm_pr_args a) {
   WGM_PERSISTENT_PROLOGUE
-  wgm_app_pagerank(L, &c, a, &sm);
+  WGM_DRIVE(wgm_phase_pagerank(L, &c, a, &sm, cur, nxt));
   WGM_PERSISTENT_EPILOGUE
 }
 

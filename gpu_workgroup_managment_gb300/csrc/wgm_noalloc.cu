@@ -33,13 +33,18 @@
 
 namespace {
 
+/* Worklist capacity per level: V + E/piece pieces with piece >= E/V, so at
+ * most 2V (plus slack) for any graph of WGM_NOALLOC_MAX_NODES vertices. */
+constexpr int kCap = 2 * WGM_NOALLOC_MAX_NODES + 64;
+
 struct wgm_noalloc_scratch {
   wgm_dev_state st;      /* discovery + barrier state */
   wgm_host_flags flags;  /* status words (device-resident here) */
-  int cnt[6 * WGM_LINE]; /* level counters */
+  int cnt[3 * WGM_LINE]; /* piece counters by level mod 3 */
   int levels;
   int pad[WGM_LINE - 1];
-  int wl[2 * WGM_NOALLOC_MAX_NODES]; /* two worklists */
+  int wl_start[2 * kCap]; /* two worklists of pieces (first edge, count) */
+  int wl_cnt[2 * kCap];
 };
 
 constexpr int kMaxDevices = 64;
@@ -125,11 +130,15 @@ extern "C" int wgm_bfs_noalloc(const int32_t *d_row_ptr, const int32_t *d_col,
   a.col = d_col;
   a.wt = nullptr;
   a.dist = d_dist;
-  a.wl = sc->wl;
+  int64_t avg = (num_edges + num_nodes - 1) / num_nodes;
+  a.piece = (int)(avg > 32 ? avg : 32);
+  a.cap = kCap;
+  a.wl_start = sc->wl_start;
+  a.wl_cnt = sc->wl_cnt;
+  a.wl_u = nullptr;
   a.cnt = sc->cnt;
   a.stamp = nullptr;
   a.source = source;
-  a.hub_threshold = 256;
   a.levels_out = &sc->levels;
   if (wgm_launch_lonestar(false, L, a, d->grid, 256, s) != cudaSuccess) return WGM_ERR_CUDA;
 

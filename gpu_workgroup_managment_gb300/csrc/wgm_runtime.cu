@@ -160,9 +160,16 @@ extern "C" int wgm_last_cuda_error(const wgm_runtime *rt) { return rt ? rt->last
 
 extern "C" int wgm_device_status(const wgm_runtime *rt, int *status, int *site, int *detail) {
   if (!rt) return WGM_ERR_INVALID;
-  if (status) *status = __atomic_load_n(&rt->hf->status, __ATOMIC_ACQUIRE);
-  if (site) *site = rt->hf->status_site;
-  if (detail) *detail = rt->hf->status_detail;
+  int cur = __atomic_load_n(&rt->hf->status, __ATOMIC_ACQUIRE);
+  if (cur) {
+    if (status) *status = cur;
+    if (site) *site = rt->hf->status_site;
+    if (detail) *detail = rt->hf->status_detail;
+  } else {
+    if (status) *status = rt->last_status;
+    if (site) *site = rt->last_site;
+    if (detail) *detail = rt->last_detail;
+  }
   return WGM_OK;
 }
 
@@ -231,9 +238,10 @@ int wgm_finish_launch(wgm_runtime *rt, int *dev_status, int *dev_site) {
   if (dev == WGM_DEV_OK) return WGM_OK;
   int st = wgm_status_from_device(dev);
   int site = rt->hf->status_site, detail = rt->hf->status_detail;
+  rt->last_status = dev;
+  rt->last_site = site;
+  rt->last_detail = detail;
   wgm_reset(rt);
-  rt->hf->status_site = site;
-  rt->hf->status_detail = detail;
   return st;
 }
 

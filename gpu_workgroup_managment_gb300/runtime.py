@@ -89,6 +89,10 @@ class Runtime:
         check(lib.wgm_sm_count(self._h, C.byref(n)))
         return n.value
 
+    def last_failure(self) -> str:
+        s, site, det = self.device_status()
+        return f"device status {s} at site {site} (detail {det})" if s else "no device failure"
+
     def device_status(self) -> tuple[int, int, int]:
         s, site, det = C.c_int(), C.c_int(), C.c_int()
         check(lib.wgm_device_status(self._h, C.byref(s), C.byref(site), C.byref(det)))

@@ -46,6 +46,7 @@ extern "C" {
 #define WGM_BARRIER_SENSE 0
 #define WGM_BARRIER_XF 1
 #define WGM_BARRIER_TREE 2
+#define WGM_BARRIER_COUNT 3 /* monotonic arrival counter, waiters poll it */
 
 /* ---- persistent apps (the reference selects them by macro, skel.cpp:50-77) */
 #define WGM_APP_LONESTAR_BFS 1
@@ -113,8 +114,9 @@ int wgm_runtime_destroy(wgm_runtime *rt);
  * (rt_host/cl_scheduler.h:35-50, skel.cpp:127-155). */
 int wgm_reset(wgm_runtime *rt);
 int wgm_last_cuda_error(const wgm_runtime *rt);
-/* First device-side failure recorded since the last reset (no reference
- * counterpart: the reference spins forever). */
+/* The device-side failure of the current launch, else the last one recorded
+ * (status WGM_DEV_*, the WGM_SITE_* of the wait that gave up, a detail word);
+ * no reference counterpart: the reference spins forever. */
 int wgm_device_status(const wgm_runtime *rt, int *status, int *site, int *detail);
 /* Raise/clear the host abort word every device wait polls. */
 int wgm_set_abort(wgm_runtime *rt, int value);
@@ -170,6 +172,93 @@ int wgm_app_rounds(wgm_app *app, int *rounds);
 /* clean_persistent_task (bfs.h:330-334). */
 int wgm_app_destroy(wgm_app *app);
 
+/* ---- megakernel and communicator --------------------------------------- */
+/* One persistent launch in which discovered group 0 runs the device-side
+ * scheduler (cl_scheduler.cl:54-308) and the other groups take either slices
+ * of the resident persistent app (grown and shrunk at every barrier by
+ * offer_fork/offer_kill, iw_barrier.cl:165-305, scheduler_1.cl:10-81) or the
+ * non-persistent task.  The host drives it with the reference's
+ * CL_Communicator protocol (cl_communicator.h:19-465). */
+#define WGM_NP_NONE 0
+#define WGM_NP_MATMULT_I32 1 /* matmult.cl: int32, djb2 hash of the diagonal */
+#define WGM_NP_REDUCE_I32 2  /* reduce.cl: int32 min */
+#define WGM_NP_MATMULT_F32 3 /* FP32 n x n product (no reference counterpart) */
+#define WGM_NP_REDUCE_F32 4  /* FP32 min (no reference counterpart) */
+typedef struct wgm_comm wgm_comm;
+/* Communicator for a persistent app (may be NULL) plus one non-persistent
+ * task kind of size np_size (matmult: n, reduce: elements):
+ * CL_Communicator's constructor + init_non_persistent_app (matmult.h:163-231,
+ * reduce.h:330-348). */
+int wgm_comm_create(wgm_runtime *rt, wgm_app *persistent, int np_kind, int np_size,
+                    wgm_comm **out);
+int wgm_comm_destroy(wgm_comm *comm);
+/* launch_mega_kernel (cl_communicator.h:71-95); num_wgs <= 0: all co-resident. */
+int wgm_comm_launch_mega_kernel(wgm_comm *comm, int num_wgs);
+/* number_of_discovered_groups (cl_communicator.h:97-99): groups available to
+ * tasks (the scheduler's group excluded). */
+int wgm_comm_number_of_discovered_groups(wgm_comm *comm, int *groups);
+/* send_persistent_task (cl_communicator.h:207-224): starts the monitor thread. */
+int wgm_comm_send_persistent_task(wgm_comm *comm, int groups);
+/* send_task_synchronous (cl_communicator.h:123-166). */
+int wgm_comm_send_task_synchronous(wgm_comm *comm, int groups, uint64_t *exec_ns,
+                                   uint64_t *resp_ns);
+int wgm_comm_is_executing_persistent(wgm_comm *comm, int *executing);
+int wgm_comm_get_persistent_time(wgm_comm *comm, uint64_t *ns);
+int wgm_comm_send_quit(wgm_comm *comm);
+/* Wait for the megakernel to exit (the reference's exec_queue.finish()). */
+int wgm_comm_finish(wgm_comm *comm);
+int wgm_comm_reset(wgm_comm *comm);              /* cl_communicator.h:376-393 */
+int wgm_comm_add_redline(wgm_comm *comm);        /* cl_communicator.h:67-69 */
+int wgm_comm_summary(wgm_comm *comm, char *buf, size_t len); /* :296-336 */
+int wgm_comm_task_times(wgm_comm *comm, uint64_t *resp_ns, uint64_t *exec_ns, int capacity,
+                        int *count);
+int wgm_comm_average_persistent_groups(wgm_comm *comm, double *avg);
+int wgm_comm_reset_non_persistent(wgm_comm *comm);              /* reset_non_persistent */
+int wgm_comm_check_non_persistent(wgm_comm *comm, int *ok);     /* check_non_persistent_task */
+int wgm_comm_get_occupancy_bound(wgm_comm *comm, int *groups);  /* :350-374 */
+/* execute_merged_iteration (skel.cpp:405-463). */
+int wgm_run_merged_iteration(wgm_comm *comm, int num_wgs, int np_groups, int frequency_ms,
+                             int skip_tasks, int *np_errors, int *np_tasks);
+
+/* ---- batched form ------------------------------------------------------- */
+/* Many graphs and many (graph, algorithm, source) jobs in one persistent
+ * launch: CTAs pull team slots largest job first from a device queue; a job
+ * runs its Lonestar BFS (algo 0) or SSSP (algo 1) on a team of CTAs sized by
+ * its edges (one CTA and a CTA barrier per level for most jobs, a team
+ * counting barrier for the large ones).  No counterpart in the reference,
+ * which runs one graph per launch. */
+typedef struct wgm_batch wgm_batch;
+int wgm_batch_create(wgm_runtime *rt, int num_graphs, const wgm_graph_desc *graphs,
+                     int num_jobs, const int32_t *job_graph, const int32_t *job_algo,
+                     const int32_t *job_source, wgm_batch **out);
+/* Re-upload graphs of the same shapes. */
+int wgm_batch_upload(wgm_batch *b, const wgm_graph_desc *graphs);
+/* threads per CTA, CTAs per SM (0: occupancy maximum), piece (0: per graph). */
+int wgm_batch_configure(wgm_batch *b, int threads_per_cta, int ctas_per_sm, int piece);
+/* Team sizing: a job of E edges runs on ceil(E / team_edges) CTAs, at most
+ * max_team.  0 selects the defaults: total edges / grid, a quarter of the grid. */
+int wgm_batch_configure_teams(wgm_batch *b, int64_t team_edges, int max_team);
+/* Queue one batched launch on the runtime's stream (use_cuda_graph: replay a
+ * captured CUDA graph of the queue reset and the launch). */
+int wgm_batch_launch(wgm_batch *b, int use_cuda_graph);
+int wgm_batch_run(wgm_batch *b, int use_cuda_graph, double *device_ms);
+/* The plain form for comparison: one standalone persistent launch per job. */
+int wgm_batch_launch_per_graph(wgm_batch *b);
+int wgm_batch_run_per_graph(wgm_batch *b, double *device_ms);
+int wgm_batch_read(wgm_batch *b, int job, uint32_t *out, int64_t n);
+int wgm_batch_read_all(wgm_batch *b, uint32_t *out, int64_t n);
+/* Per job (caller's order) of the last batched launch: device start and end
+ * (ns from the earliest start), team size, levels run. */
+int wgm_batch_job_stats(wgm_batch *b, int64_t *start_ns, int64_t *end_ns, int32_t *team,
+                        int32_t *levels);
+int wgm_batch_info(wgm_batch *b, int64_t *total_nodes, int64_t *total_edges, int *threads,
+                   int *ctas_per_sm, int *piece);
+/* Sweep block size {128,256,512} x CTAs per SM x piece {16,32,64}, then the
+ * team size at the winner. */
+int wgm_batch_autotune(wgm_batch *b, int reps, int *best_threads, int *best_ctas_per_sm,
+                       int *best_piece, double *best_ms);
+int wgm_batch_destroy(wgm_batch *b);
+
 /* ---- device timing on the runtime's stream (CUDA events) --------------- */
 /* os_freq.cpp:311-328 reads CL profiling events; here a pair of CUDA events
  * brackets everything queued on the runtime's stream in between. */
@@ -191,7 +280,7 @@ int wgm_timer_stop(wgm_runtime *rt, double *elapsed_ms);
  * cudaStream_t (NULL: the default stream); the call returns when the BFS has
  * finished.  d_row_ptr must be a valid CSR (row_ptr[V] may be one short of
  * num_edges, as the Lonestar loader produces). */
-#define WGM_NOALLOC_MAX_NODES (1 << 20)
+#define WGM_NOALLOC_MAX_NODES (1 << 18)
 int wgm_bfs_noalloc(const int32_t *d_row_ptr, const int32_t *d_col, int32_t num_nodes,
                     int64_t num_edges, int32_t source, uint32_t *d_dist, void *stream);
 

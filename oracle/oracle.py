@@ -52,6 +52,7 @@ def lib() -> C.CDLL:
             "oracle_matmult_i32": [P, I, I, P, I, P],
             "oracle_hash_diag": [P, I, I],
             "oracle_matmult_f32": [P, I, I, P, I, P],
+            "oracle_batch_lonestar": [I, P, P, P, P, P, P, P, P, P, P],
         }
         for name, args in protos.items():
             fn = getattr(_lib, name)
@@ -76,6 +77,45 @@ def _p(a: np.ndarray) -> int:
 
 def threads() -> int:
     return lib().oracle_omp_threads()
+
+
+class BatchArena:
+    """Graphs and jobs of a batch packed for oracle_batch_lonestar."""
+
+    def __init__(self, graphs: list, jobs: list):
+        rows, cols, wts, roff, coff = [], [], [], [], []
+        r = c = 0
+        for g in graphs:
+            roff.append(r)
+            coff.append(c)
+            rows.append(g.row_ptr)
+            cols.append(g.col)
+            wts.append(g.weights if g.weights is not None else np.zeros(g.num_edges, np.uint32))
+            r += g.num_nodes + 1
+            c += g.num_edges
+        self.rows = np.concatenate(rows).astype(np.int32)
+        self.cols = np.concatenate(cols).astype(np.int32) if c else np.zeros(1, np.int32)
+        self.wts = np.concatenate(wts).astype(np.uint32) if c else np.zeros(1, np.uint32)
+        self.graph_roff = np.array(roff, np.int64)
+        self.graph_coff = np.array(coff, np.int64)
+        self.graphs = graphs
+        self.set_jobs(jobs)
+
+    def set_jobs(self, jobs: list) -> None:
+        gi = np.array([j[0] for j in jobs], np.int64)
+        self.V = np.array([self.graphs[i].num_nodes for i in gi], np.int32)
+        self.row_off = self.graph_roff[gi]
+        self.col_off = self.graph_coff[gi]
+        self.dist_off = np.concatenate([[0], np.cumsum(self.V.astype(np.int64))[:-1]])
+        self.algo = np.array([0 if j[1] == "bfs" else 1 for j in jobs], np.int32)
+        self.source = np.array([j[2] for j in jobs], np.int32)
+        self.dist = np.empty(int(self.V.astype(np.int64).sum()), np.uint32)
+
+    def run(self) -> np.ndarray:
+        lib().oracle_batch_lonestar(len(self.V), _p(self.V), _p(self.row_off), _p(self.col_off),
+                                    _p(self.dist_off), _p(self.algo), _p(self.source),
+                                    _p(self.rows), _p(self.cols), _p(self.wts), _p(self.dist))
+        return self.dist
 
 
 def lonestar_bfs(g, source: int = 0, omp: bool = False) -> np.ndarray:

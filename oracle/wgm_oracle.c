@@ -589,3 +589,19 @@ float oracle_reduce_min_f32(const float *buf, int64_t n) {
     if (buf[i] < m) m = buf[i];
   return m;
 }
+
+void oracle_batch_lonestar(int32_t njobs, const int32_t *V, const int64_t *row_off,
+                           const int64_t *col_off, const int64_t *dist_off,
+                           const int32_t *algo, const int32_t *source, const int32_t *rows,
+                           const int32_t *cols, const uint32_t *wts, uint32_t *dist) {
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int32_t k = 0; k < njobs; k++) {
+    const int32_t *rp = rows + row_off[k];
+    const int32_t *cl = cols + col_off[k];
+    uint32_t *d = dist + dist_off[k];
+    if (algo[k] == 0)
+      oracle_lonestar_bfs(V[k], rp, cl, source[k], d);
+    else
+      oracle_lonestar_sssp(V[k], rp, cl, wts + col_off[k], source[k], d);
+  }
+}

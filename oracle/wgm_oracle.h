@@ -106,6 +106,16 @@ void oracle_matmult_f32(const float *A, int32_t M, int32_t K, const float *B,
                         int32_t N, float *C);
 float oracle_reduce_min_f32(const float *buf, int64_t n);
 
+/* Batched CPU baseline: njobs Lonestar BFS (algo 0) / SSSP (algo 1) jobs,
+ * spread over the OpenMP threads (dynamic schedule, in the order given),
+ * each job the serial restatement above.  Job k reads graph rows at
+ * rows + row_off[k] (V[k]+1 entries), cols/wts at col_off[k], writes
+ * dist + dist_off[k]. */
+void oracle_batch_lonestar(int32_t njobs, const int32_t *V, const int64_t *row_off,
+                           const int64_t *col_off, const int64_t *dist_off,
+                           const int32_t *algo, const int32_t *source, const int32_t *rows,
+                           const int32_t *cols, const uint32_t *wts, uint32_t *dist);
+
 int oracle_omp_threads(void);
 
 #ifdef __cplusplus

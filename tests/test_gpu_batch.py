@@ -1,0 +1,109 @@
+"""Batched form on the GPU: every job's result must equal the plain per-graph
+launch and the oracle, bit for bit, whatever the block size, CTAs per SM,
+worklist piece size, and whether the launch is replayed from a CUDA graph."""
+import numpy as np
+import pytest
+
+from gpu_workgroup_managment_gb300 import Runtime, graphs
+from gpu_workgroup_managment_gb300.batch import Batch, batch_workload
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def small_batch():
+    gs, jobs, _ = batch_workload(n_graphs=40, seed=7, mu=10.0, sigma=2.0, lo=8, hi=13)
+    return gs, jobs
+
+
+def _oracle(gs, jobs):
+    out = []
+    for gi, algo, src in jobs:
+        g = gs[gi]
+        out.append(oracle.lonestar_bfs(g, src) if algo == "bfs" else oracle.lonestar_sssp(g, src))
+    return out
+
+
+def test_batch_matches_oracle_and_per_graph(small_batch):
+    gs, jobs = small_batch
+    want = _oracle(gs, jobs)
+    with Runtime() as rt, Batch(rt, gs, jobs) as b:
+        b.run(use_cuda_graph=False)
+        got = [b.result(k) for k in range(len(jobs))]
+        for k in range(len(jobs)):
+            assert np.array_equal(got[k], want[k]), k
+        b.run_per_graph()
+        for k in range(len(jobs)):
+            assert np.array_equal(b.result(k), want[k]), ("per-graph", k)
+        b.run(use_cuda_graph=True)
+        b.run(use_cuda_graph=True)  # replay of the captured graph
+        allres = b.results()
+        for k in range(len(jobs)):
+            assert np.array_equal(allres[b.offsets[k]:b.offsets[k + 1]], want[k])
+
+
+@pytest.mark.parametrize("threads,ctas,piece", [(128, 1, 16), (512, 2, 64), (1024, 0, 32),
+                                                (256, 3, 0)])
+def test_batch_configurations(small_batch, threads, ctas, piece):
+    gs, jobs = small_batch
+    want = _oracle(gs, jobs)
+    with Runtime() as rt, Batch(rt, gs, jobs) as b:
+        b.configure(threads, ctas, piece)
+        b.run(use_cuda_graph=True)
+        for k in range(len(jobs)):
+            assert np.array_equal(b.result(k), want[k]), k
+
+
+@pytest.mark.parametrize("team_edges,max_team,threads", [(2000, 8, 256), (500, 64, 128),
+                                                         (4000, 3, 512)])
+def test_batch_teams(small_batch, team_edges, max_team, threads):
+    """Large jobs on teams of CTAs (team counting barrier, global level
+    counters): results stay identical, across replays of the CUDA graph."""
+    gs, jobs = small_batch
+    want = _oracle(gs, jobs)
+    with Runtime() as rt, Batch(rt, gs, jobs) as b:
+        b.configure(threads, 0, 0)
+        b.configure_teams(team_edges, max_team)
+        for rep in range(3):
+            b.run(use_cuda_graph=rep > 0)
+            allres = b.results()
+            for k in range(len(jobs)):
+                assert np.array_equal(allres[b.offsets[k]:b.offsets[k + 1]], want[k]), (rep, k)
+
+
+def test_batch_edge_cases():
+    # single vertex, isolated source, star hub, the Lonestar loader view
+    one = graphs.Graph(np.array([0, 0], np.int32), np.zeros(0, np.int32), np.zeros(0, np.uint32))
+    rows = [list(range(1, 3000))] + [[0]] * 2999
+    rp = np.zeros(3001, np.int32)
+    rp[1:] = np.cumsum([len(r) for r in rows])
+    star = graphs.Graph(rp, np.array([c for r in rows for c in r], np.int32))
+    star.weights = graphs.uniform_weights(star, 1)
+    gridv = graphs.grid(20, 30)
+    gridv.weights = graphs.uniform_weights(gridv, 2)
+    lv = graphs.lonestar_view(gridv)
+    gs = [one, star, lv]
+    jobs = [(0, "bfs", 0), (0, "sssp", 0), (1, "bfs", 0), (1, "sssp", 17), (2, "bfs", 599),
+            (2, "sssp", 0), (1, "bfs", 2999)]
+    want = _oracle(gs, jobs)
+    with Runtime() as rt, Batch(rt, gs, jobs) as b:
+        b.run()
+        for k in range(len(jobs)):
+            assert np.array_equal(b.result(k), want[k]), k
+        b.configure_teams(100, 4)  # the star and the grid on teams
+        b.run()
+        for k in range(len(jobs)):
+            assert np.array_equal(b.result(k), want[k]), ("teams", k)
+
+
+def test_batch_autotune_picks_a_valid_config(small_batch):
+    gs, jobs = small_batch
+    gs, jobs = gs[:12], [j for j in jobs if j[0] < 12]
+    want = _oracle(gs, jobs)
+    with Runtime() as rt, Batch(rt, gs, jobs) as b:
+        best = b.autotune(reps=1)
+        assert best["threads"] in (128, 256, 512) and best["piece"] in (16, 32, 64)
+        b.run()
+        for k in range(len(jobs)):
+            assert np.array_equal(b.result(k), want[k]), k

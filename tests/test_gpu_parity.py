@@ -86,6 +86,7 @@ def test_few_groups(rt, num_wgs):
 
 @pytest.mark.parametrize("cfg", [
     dict(barrier_kind=1), dict(barrier_kind=2), dict(barrier_kind=2, tree_fanin=3),
+    dict(barrier_kind=3), dict(barrier_kind=3, threads_per_wg=128),
     dict(discovery_mode=1, discovery_extra_rounds=2), dict(threads_per_wg=128),
     dict(threads_per_wg=512), dict(threads_per_wg=1024), dict(hub_threshold=32),
     dict(hub_threshold=100000), dict(host_handshake=1),

@@ -13,10 +13,11 @@ pytestmark = pytest.mark.gpu
 
 def test_occupancy_bound(rt):
     sms = rt.sm_count()
-    hw = rt.hw_occupancy_bound("lonestar_bfs", 256)
+    hw = rt.hw_occupancy_bound(0, 256)  # the discovery probe's own kernel
     found = rt.get_occupancy_bound(256)
     assert sms >= 1 and hw >= sms
     assert 1 <= found <= hw
+    assert rt.hw_occupancy_bound("lonestar_bfs", 256) >= sms
 
 
 def test_reference_mode_discovery(rt):
@@ -27,7 +28,7 @@ def test_reference_mode_discovery(rt):
         assert res["groups"] >= 1
 
 
-@pytest.mark.parametrize("kind", [0, 1, 2])
+@pytest.mark.parametrize("kind", [0, 1, 2, 3])
 def test_barrier_bench(kind):
     with Runtime() as r:
         res = r.barrier_bench(iterations=1000, threads_per_wg=256, barrier_kind=kind)

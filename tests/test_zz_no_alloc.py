@@ -18,7 +18,7 @@ from gpu_workgroup_managment_gb300._lib import STATUS_CODE, lib
 
 pytestmark = pytest.mark.gpu
 
-MAX_NODES = 1 << 20  # WGM_NOALLOC_MAX_NODES in include/wgm.h
+MAX_NODES = 1 << 18  # WGM_NOALLOC_MAX_NODES in include/wgm.h
 
 
 def _regular_bfs(g, source):
