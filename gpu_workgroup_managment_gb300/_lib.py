@@ -46,6 +46,25 @@ class WgmRunStats(C.Structure):
                 ("device_site", C.c_int), ("kernel_ms", C.c_double), ("host_ms", C.c_double)]
 
 
+class WgmServeConfig(C.Structure):
+    _fields_ = [("rate_per_s", C.c_double), ("duration_s", C.c_double), ("seed", C.c_uint64),
+                ("frac_bfs", C.c_double), ("frac_reduce", C.c_double), ("reps", C.c_int),
+                ("persist_groups", C.c_int), ("reserve", C.c_int), ("bfs_groups", C.c_int),
+                ("reduce_groups", C.c_int), ("matmul_groups", C.c_int),
+                ("max_in_flight", C.c_int), ("keep_results", C.c_int),
+                ("threads_per_wg", C.c_int)]
+
+
+class WgmServeStats(C.Structure):
+    _fields_ = [("arrived", C.c_int64), ("completed", C.c_int64),
+                ("waited_for_memory", C.c_int64), ("stream_s", C.c_double),
+                ("achieved_rate", C.c_double), ("lat_p50_us", C.c_double),
+                ("lat_p99_us", C.c_double), ("lat_mean_us", C.c_double),
+                ("lat_max_us", C.c_double), ("persist_ms", C.c_double),
+                ("persist_reps", C.c_int), ("kills", C.c_int), ("forks", C.c_int),
+                ("groups", C.c_int), ("run_ms", C.c_double)]
+
+
 class WgmGraphDesc(C.Structure):
     _fields_ = [("num_nodes", C.c_int32), ("num_edges", C.c_int64),
                 ("row_ptr", C.c_void_p), ("col", C.c_void_p), ("weights", C.c_void_p)]
@@ -106,6 +125,12 @@ _PROTOS = {
     "wgm_batch_configure": (_I, [_P, _I, _I, _I]),
     "wgm_batch_configure_teams": (_I, [_P, C.c_int64, _I]),
     "wgm_batch_job_stats": (_I, [_P, _P, _P, _P, _P]),
+    "wgm_batch_reorder_by_last_run": (_I, [_P]),
+    "wgm_serve_create": (_I, [_P, _P, _P, _I, _P, _I, _I, _P, _I, _I, _P, C.c_int64, _P]),
+    "wgm_serve_run": (_I, [_P, _P, _P]),
+    "wgm_serve_requests": (_I, [_P, _P, _P, _P, _P, _P, _P]),
+    "wgm_serve_result": (_I, [_P, C.c_int64, _P, C.c_int64]),
+    "wgm_serve_destroy": (_I, [_P]),
     "wgm_batch_launch": (_I, [_P, _I]),
     "wgm_batch_run": (_I, [_P, _I, C.POINTER(C.c_double)]),
     "wgm_batch_launch_per_graph": (_I, [_P]),

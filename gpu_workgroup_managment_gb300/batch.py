@@ -99,6 +99,11 @@ class Batch:
                                       lv.ctypes.data), "wgm_batch_job_stats")
         return {"start_ns": st, "end_ns": en, "team": tm, "levels": lv}
 
+    def reorder_by_last_run(self) -> None:
+        """Queue the jobs longest first by their device time in the last
+        batched launch."""
+        check(lib.wgm_batch_reorder_by_last_run(self._h), "wgm_batch_reorder_by_last_run")
+
     def autotune(self, reps: int = 3) -> dict:
         t, c, p, ms = C.c_int(), C.c_int(), C.c_int(), C.c_double()
         check(lib.wgm_batch_autotune(self._h, reps, C.byref(t), C.byref(c), C.byref(p),

@@ -18,7 +18,7 @@ ROOT = os.path.dirname(PKG)
 LIB = os.path.join(PKG, "libwgm.so")
 OBJ = os.path.join(PKG, "_build")
 
-SOURCES = ["wgm_kernels.cu", "wgm_runtime.cu", "wgm_apps.cu", "wgm_graphgen.cpp",
+SOURCES = ["wgm_kernels.cu", "wgm_runtime.cu", "wgm_apps.cu", "wgm_graphgen.cpp", "wgm_serve.cu",
            "wgm_noalloc.cu", "wgm_mega.cu", "wgm_batch.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -510,9 +510,9 @@ extern "C" int wgm_batch_info(wgm_batch *b, int64_t *total_nodes, int64_t *total
 }
 
 /* Autotuner: block size x blocks per SM x worklist piece first, then the
- * team size (edges per team member as a multiple of total edges / grid), each
- * point the best of `reps` CUDA-graph replays; leaves the batch configured
- * with the winner. */
+ * team size (edges per team member as a multiple of total edges / grid) with
+ * the queue ordered by a run at that size, each point the best of `reps`
+ * CUDA-graph replays; leaves the batch configured with the winner. */
 static int wgm_batch_time(wgm_batch *b, int reps, double *out) {
   double ms = 0, mn = 1e300;
   int s = wgm_batch_run(b, 1, &ms); /* warm-up and capture */
@@ -569,11 +569,14 @@ extern "C" int wgm_batch_autotune(wgm_batch *b, int reps, int *best_threads,
   for (auto &j : b->jobs) etot += b->gE[j.graph];
   const long long base = std::max(1LL, etot / std::max(grid, 1));
   long long bte = saved_te;
-  const double factors[5] = {0.125, 0.25, 0.5, 1.0, 2.0};
+  const double factors[6] = {1.0 / 32, 1.0 / 16, 0.125, 0.25, 0.5, 1.0};
   for (double f : factors) {
     long long te = std::max(1LL << 12, (long long)(base * f));
     s = wgm_batch_configure_teams(b, te, saved_mt);
-    double mn = 0;
+    double mn = 0, ms = 0;
+    /* one run at these team sizes, then the queue ordered by its job times */
+    if (!s) s = wgm_batch_run(b, 1, &ms);
+    if (!s) s = wgm_batch_reorder_by_last_run(b);
     if (!s) s = wgm_batch_time(b, reps, &mn);
     if (s) return s;
     if (mn < best) {
@@ -582,6 +585,9 @@ extern "C" int wgm_batch_autotune(wgm_batch *b, int reps, int *best_threads,
     }
   }
   s = wgm_batch_configure_teams(b, bte, saved_mt);
+  double ms = 0;
+  if (!s) s = wgm_batch_run(b, 1, &ms);
+  if (!s) s = wgm_batch_reorder_by_last_run(b);
   if (best_threads) *best_threads = bt;
   if (best_ctas_per_sm) *best_ctas_per_sm = bc;
   if (best_piece) *best_piece = bp;
@@ -613,5 +619,37 @@ extern "C" int wgm_batch_job_stats(wgm_batch *b, int64_t *start_ns, int64_t *end
     if (team) team[k] = b->jobs[q].team;
     if (levels) levels[k] = lv[q];
   }
+  return WGM_OK;
+}
+
+/* Profile-guided queue order: sort the jobs by their device duration in the
+ * last batched launch, longest first (longest-processing-time-first list
+ * scheduling), so the jobs on the critical path - high-diameter graphs run
+ * level after level - start at once instead of behind jobs with more edges
+ * but fewer levels.  Outputs and offsets do not move; the next launch
+ * recaptures its CUDA graph. */
+extern "C" int wgm_batch_reorder_by_last_run(wgm_batch *b) {
+  if (!b) return WGM_ERR_INVALID;
+  cudaSetDevice(b->rt->device);
+  std::vector<unsigned long long> t(2 * (size_t)b->njobs);
+  cudaError_t e = cudaStreamSynchronize(b->rt->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(t.data(), b->d_times, t.size() * 8, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return wgm_cuda_fail(b->rt, e);
+  std::vector<int> order(b->njobs);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+    return t[2 * x + 1] - t[2 * x] > t[2 * y + 1] - t[2 * y];
+  });
+  std::vector<wgm_batch_job> jobs(b->njobs);
+  std::vector<int> new_pos(b->njobs);
+  for (int q = 0; q < b->njobs; q++) {
+    jobs[q] = b->jobs[order[q]];
+    new_pos[order[q]] = q;
+  }
+  for (int k = 0; k < b->njobs; k++) b->queue_of[k] = new_pos[b->queue_of[k]];
+  b->jobs.swap(jobs);
+  b->teams_grid = 0;
+  wgm_batch_free_graph(b);
   return WGM_OK;
 }

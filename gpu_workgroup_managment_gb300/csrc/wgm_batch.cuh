@@ -152,9 +152,10 @@ __device__ void wgm_cta_lonestar(const wgm_batch_args &B, const wgm_batch_job &j
 
 /* Team barrier: a counting barrier on the job's arrival line.  `nb` holds
  * the arrivals this member has waited for so far.  Returns false when the
- * wait ran out or another CTA already failed. */
-__device__ __forceinline__ bool wgm_team_barrier(const wgm_batch_args &B, int *arr, int G,
-                                                 unsigned *nb) {
+ * wait ran out (err[0] = WGM_DEV_TIMEOUT, err[1] = site) or another CTA
+ * already failed. */
+__device__ __forceinline__ bool wgm_team_barrier(int *err, unsigned long long spin_ns, int *arr,
+                                                 int G, unsigned *nb) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -162,16 +163,16 @@ __device__ __forceinline__ bool wgm_team_barrier(const wgm_batch_args &B, int *a
     *nb = target;
     int ok = 1;
     wgm_red_add_release_gpu(arr, 1);
-    const unsigned long long deadline = wgm_globaltimer() + B.spin_ns;
+    const unsigned long long deadline = wgm_globaltimer() + spin_ns;
     unsigned it = 0;
     while ((int)((unsigned)wgm_ld_relaxed_gpu(arr) - target) < 0) {
       if ((++it & 63u) == 0) {
-        if (wgm_ld_relaxed_gpu(B.err) != 0) {
+        if (wgm_ld_relaxed_gpu(err) != 0) {
           ok = 0;
           break;
         }
         if (wgm_globaltimer() > deadline) {
-          if (atomicCAS(B.err, 0, WGM_DEV_TIMEOUT) == 0) B.err[1] = WGM_SITE_BARRIER;
+          if (atomicCAS(err, 0, WGM_DEV_TIMEOUT) == 0) err[1] = WGM_SITE_BARRIER;
           ok = 0;
           break;
         }
@@ -185,64 +186,92 @@ __device__ __forceinline__ bool wgm_team_barrier(const wgm_batch_args &B, int *a
   return s_ok != 0;
 }
 
-/* One job on a team of G > 1 CTAs; this CTA is member `rank`.  The level
- * loop is the persistent kernel's (wgm_phase_lonestar): device-side init,
- * then one barrier per level with the level counters triple-buffered in the
- * job's control lines. */
+/* One Lonestar BFS/SSSP job as seen by one member of its team. */
+struct wgm_ls_job {
+  int V, source, piece, cap;
+  int G, rank; /* team size, this CTA's rank */
+  const int *row, *col;
+  const unsigned *wt;
+  unsigned *dist;
+  int *stamp;
+  int *wl_start, *wl_cnt, *wl_u; /* [2][cap] each */
+  int *cnt;                      /* 3 level-counter lines, zero at start */
+  int *arr;                      /* team barrier arrival line, zero at start */
+};
+
+/* Run a job on a team of G > 1 CTAs.  The level loop is the persistent
+ * kernel's (wgm_phase_lonestar): device-side init, then one barrier per
+ * level with the level counters triple-buffered in the job's control lines.
+ * Returns the number of levels (the Lonestar iteration count), or -1 when a
+ * team wait failed. */
 template <bool SSSP>
-__device__ void wgm_team_lonestar(const wgm_batch_args &B, const wgm_batch_job &j, int job,
-                                  int rank, wgm_warp_smem *sm) {
-  const int V = j.V, G = j.team;
-  const int *row = B.rows + j.row_off;
-  const int *col = B.cols + j.col_off;
-  const unsigned *wt = SSSP ? B.wts + j.col_off : nullptr;
-  unsigned *dist = B.dist + j.dist_off;
-  int *stamp = SSSP ? B.stamp + j.stamp_off : nullptr;
-  const int cap = j.cap;
-  int *wl_start = B.scratch + j.wl_off;
-  int *wl_cnt = wl_start + 2 * (size_t)cap;
-  int *wl_u = SSSP ? wl_cnt + 2 * (size_t)cap : nullptr;
-  int *ctl = B.ctl + (size_t)(1 + job * WGM_BATCH_CTL_LINES_PER_JOB) * WGM_LINE;
-  int *cnt = ctl; /* 3 lines */
-  int *arr = ctl + 3 * WGM_LINE;
+__device__ int wgm_team_ls_run(const wgm_ls_job &J, wgm_warp_smem *sm, int *err,
+                               unsigned long long spin_ns) {
+  const int V = J.V, G = J.G, rank = J.rank, cap = J.cap;
   const int lane = wgm_lane(), warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   unsigned nb = 0;
   const int tid = rank * blockDim.x + threadIdx.x, nth = G * blockDim.x;
   for (int i = tid; i < V; i += nth) {
-    dist[i] = (i == j.source) ? 0u : WGM_LONESTAR_INF;
-    if (SSSP) stamp[i] = 0;
+    J.dist[i] = (i == J.source) ? 0u : WGM_LONESTAR_INF;
+    if (SSSP) J.stamp[i] = 0;
   }
   if (rank == 0 && threadIdx.x < 32)
-    wgm_cta_push(row, j.piece, threadIdx.x == 0, j.source, &cnt[1 * WGM_LINE], wl_start + cap,
-                 wl_cnt + cap, wl_u ? wl_u + cap : nullptr, sm->acc[0]);
-  if (!wgm_team_barrier(B, arr, G, &nb)) return;
+    wgm_cta_push(J.row, J.piece, threadIdx.x == 0, J.source, &J.cnt[1 * WGM_LINE],
+                 J.wl_start + cap, J.wl_cnt + cap, J.wl_u ? J.wl_u + cap : nullptr, sm->acc[0]);
+  if (!wgm_team_barrier(err, spin_ns, J.arr, G, &nb)) return -1;
   const int gw = rank * nw + warp, NW = G * nw;
   int L = 1;
   for (;;) {
-    const int n = __ldcg(&cnt[(L % 3) * WGM_LINE]);
+    const int n = __ldcg(&J.cnt[(L % 3) * WGM_LINE]);
     if (n == 0 || L > V + 2) break;
-    if (rank == 0 && threadIdx.x == 0) cnt[((L + 2) % 3) * WGM_LINE] = 0;
+    if (rank == 0 && threadIdx.x == 0) J.cnt[((L + 2) % 3) * WGM_LINE] = 0;
     wgm_ls_out o;
-    o.counter = &cnt[((L + 1) % 3) * WGM_LINE];
+    o.counter = &J.cnt[((L + 1) % 3) * WGM_LINE];
     const size_t io = (size_t)(L & 1) * cap, oo = (size_t)((L + 1) & 1) * cap;
-    o.o_start = wl_start + oo;
-    o.o_cnt = wl_cnt + oo;
-    o.o_u = wl_u ? wl_u + oo : nullptr;
+    o.o_start = J.wl_start + oo;
+    o.o_cnt = J.wl_cnt + oo;
+    o.o_u = J.wl_u ? J.wl_u + oo : nullptr;
     o.cap = cap;
     for (int b = gw * 32; b < n; b += NW * 32) {
       int i = b + lane, deg = 0, start = 0;
       unsigned dv = 0;
       if (i < n) {
-        start = __ldcg(&wl_start[io + i]);
-        deg = __ldcg(&wl_cnt[io + i]);
-        if (SSSP) dv = __ldcg(&dist[__ldcg(&wl_u[io + i])]);
+        start = __ldcg(&J.wl_start[io + i]);
+        deg = __ldcg(&J.wl_cnt[io + i]);
+        if (SSSP) dv = __ldcg(&J.dist[__ldcg(&J.wl_u[io + i])]);
       }
-      wgm_ls_chunk<SSSP>(row, col, wt, dist, stamp, V, j.piece, L, start, deg, dv, o);
+      wgm_ls_chunk<SSSP>(J.row, J.col, J.wt, J.dist, J.stamp, V, J.piece, L, start, deg, dv, o);
     }
-    if (!wgm_team_barrier(B, arr, G, &nb)) return;
+    if (!wgm_team_barrier(err, spin_ns, J.arr, G, &nb)) return -1;
     L++;
   }
-  if (rank == 0 && threadIdx.x == 0 && B.levels) B.levels[job] = L;
+  return L;
+}
+
+/* One batch job on a team of G > 1 CTAs; this CTA is member `rank`. */
+template <bool SSSP>
+__device__ void wgm_team_lonestar(const wgm_batch_args &B, const wgm_batch_job &j, int job,
+                                  int rank, wgm_warp_smem *sm) {
+  wgm_ls_job J;
+  J.V = j.V;
+  J.source = j.source;
+  J.piece = j.piece;
+  J.cap = j.cap;
+  J.G = j.team;
+  J.rank = rank;
+  J.row = B.rows + j.row_off;
+  J.col = B.cols + j.col_off;
+  J.wt = SSSP ? B.wts + j.col_off : nullptr;
+  J.dist = B.dist + j.dist_off;
+  J.stamp = SSSP ? B.stamp + j.stamp_off : nullptr;
+  J.wl_start = B.scratch + j.wl_off;
+  J.wl_cnt = J.wl_start + 2 * (size_t)j.cap;
+  J.wl_u = SSSP ? J.wl_cnt + 2 * (size_t)j.cap : nullptr;
+  int *ctl = B.ctl + (size_t)(1 + job * WGM_BATCH_CTL_LINES_PER_JOB) * WGM_LINE;
+  J.cnt = ctl;
+  J.arr = ctl + 3 * WGM_LINE;
+  const int L = wgm_team_ls_run<SSSP>(J, sm, B.err, B.spin_ns);
+  if (L > 0 && rank == 0 && threadIdx.x == 0 && B.levels) B.levels[job] = L;
 }
 
 #endif

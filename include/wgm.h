@@ -253,11 +253,74 @@ int wgm_batch_job_stats(wgm_batch *b, int64_t *start_ns, int64_t *end_ns, int32_
                         int32_t *levels);
 int wgm_batch_info(wgm_batch *b, int64_t *total_nodes, int64_t *total_edges, int *threads,
                    int *ctas_per_sm, int *piece);
+/* Queue the jobs longest first by their device time in the last batched
+ * launch (profile-guided order; results and offsets are unchanged). */
+int wgm_batch_reorder_by_last_run(wgm_batch *b);
 /* Sweep block size {128,256,512} x CTAs per SM x piece {16,32,64}, then the
  * team size at the winner. */
 int wgm_batch_autotune(wgm_batch *b, int reps, int *best_threads, int *best_ctas_per_sm,
                        int *best_piece, double *best_ms);
 int wgm_batch_destroy(wgm_batch *b);
+
+/* ---- served form -------------------------------------------------------- */
+/* One serving megakernel launch hosts a resident persistent job (Pannotia
+ * colour then Lonestar BFS on one graph, `reps` times, resizable at every
+ * barrier) while a Poisson stream of requests arrives: BFS queries on
+ * resident graphs, FP32 min reductions over resident vectors, FP32 n x n
+ * products of resident operand pairs.  A request is admitted when its state
+ * fits in the device arena (first fit), runs on a team of groups beside
+ * other requests, and the persistent job cedes groups to waiting requests at
+ * its resizing barriers (offer_kill) and takes free ones back (offer_fork).
+ * Generalises the reference's one-task-at-a-time CL_Communicator loop
+ * (cl_communicator.h:19-465, skel.cpp:387-463). */
+#define WGM_REQ_BFS 1
+#define WGM_REQ_REDUCE 2
+#define WGM_REQ_MATMUL 3
+typedef struct wgm_serve wgm_serve;
+typedef struct wgm_serve_config {
+  double rate_per_s;   /* Poisson arrival rate (0: no requests) */
+  double duration_s;   /* stream length; with reps > 0 the stream also stops when
+                          the persistent job ends */
+  uint64_t seed;
+  double frac_bfs;     /* request mix; the rest after frac_reduce are matmuls */
+  double frac_reduce;
+  int reps;            /* persistent job repetitions (0: no persistent job) */
+  int persist_groups;  /* groups the persistent job starts with (0: all) */
+  int reserve;         /* free groups the persistent job leaves to requests */
+  int bfs_groups, reduce_groups, matmul_groups; /* team sizes */
+  int max_in_flight;   /* admitted and unfinished requests (<= 4000) */
+  int keep_results;    /* copy every request's output to the host (tests) */
+  int threads_per_wg;  /* 0: the runtime's */
+} wgm_serve_config;
+typedef struct wgm_serve_stats {
+  int64_t arrived, completed, waited_for_memory;
+  double stream_s;       /* from the first arrival to the last completion */
+  double achieved_rate;  /* completed / stream_s */
+  double lat_p50_us, lat_p99_us, lat_mean_us, lat_max_us;
+  double persist_ms;     /* launch to the persistent job's last repetition */
+  int persist_reps;
+  int kills, forks;      /* groups ceded and taken back by the persistent job */
+  int groups;            /* discovered groups (scheduler included) */
+  double run_ms;         /* whole launch, host clock */
+} wgm_serve_stats;
+/* color/bfs: the persistent job's apps (both NULL: requests only), created
+ * with wgm_app_create on the same graph.  graphs: BFS query graphs; vecs:
+ * num_vecs x vec_len floats (>= 0); mats: num_mats pairs (A, B) of mat_n x
+ * mat_n floats, mat_n a multiple of 32; arena_bytes: request-state memory. */
+int wgm_serve_create(wgm_runtime *rt, wgm_app *color, wgm_app *bfs, int num_graphs,
+                     const wgm_graph_desc *graphs, int num_vecs, int vec_len, const float *vecs,
+                     int num_mats, int mat_n, const float *mats, int64_t arena_bytes,
+                     wgm_serve **out);
+int wgm_serve_run(wgm_serve *s, const wgm_serve_config *cfg, wgm_serve_stats *stats);
+/* Requests of the last run, in arrival order: kind, arg0 (graph / vector /
+ * pair), arg1 (BFS source), latency (ns, arrival to completion seen by the
+ * host; -1 if not completed), team size. */
+int wgm_serve_requests(wgm_serve *s, int64_t *count, int32_t *kind, int32_t *arg0,
+                       int32_t *arg1, int64_t *latency_ns, int32_t *groups);
+/* Output of request i of the last run (keep_results): BFS dist (uint32 x V),
+ * reduce min (one float), matmul C (mat_n^2 floats). */
+int wgm_serve_result(wgm_serve *s, int64_t i, void *out, int64_t bytes);
+int wgm_serve_destroy(wgm_serve *s);
 
 /* ---- device timing on the runtime's stream (CUDA events) --------------- */
 /* os_freq.cpp:311-328 reads CL profiling events; here a pair of CUDA events

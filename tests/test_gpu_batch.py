@@ -65,11 +65,16 @@ def test_batch_teams(small_batch, team_edges, max_team, threads):
     with Runtime() as rt, Batch(rt, gs, jobs) as b:
         b.configure(threads, 0, 0)
         b.configure_teams(team_edges, max_team)
-        for rep in range(3):
+        for rep in range(4):
             b.run(use_cuda_graph=rep > 0)
             allres = b.results()
             for k in range(len(jobs)):
                 assert np.array_equal(allres[b.offsets[k]:b.offsets[k + 1]], want[k]), (rep, k)
+            if rep == 1:
+                b.reorder_by_last_run()  # profile-guided queue order
+        st = b.job_stats()
+        assert np.all(st["end_ns"] >= st["start_ns"]) and st["team"].max() > 1
+        assert np.all(st["levels"] >= 1)
 
 
 def test_batch_edge_cases():
