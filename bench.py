@@ -1,22 +1,29 @@
-"""Benchmark of the persistent graph path on one GB300 (or N replicas).
+"""Benchmark of the cooperative-kernel runtime on one GB300 (or N replicas).
 
-Default workload: persistent Lonestar SSSP on RMAT scale 20 (edge factor 16,
-(a,b,c) = (0.57,0.19,0.19), seeded, symmetrised, uint32 weights in [1,1000]),
-source = the highest-degree vertex.  A step = one persistent launch (discovery,
-device-side init, worklist levels) over the graph resident in HBM.
+Headline (default): the batched form.  512 seeded graphs, node counts
+lognormal between 2^8 and 2^18 (half RMAT (0.57,0.19,0.19) with average degree
+8-32, half near-square 2D grids), one BFS and one SSSP job per graph from
+seeded sources (uint32 weights U[1,1000]) - 1024 jobs in one persistent launch
+with a device work queue, replayed from a CUDA graph, shape and team size
+chosen by the autotuner.  A step = one batched launch over all 1024 jobs with
+the graphs resident in HBM (1.4 GB of CSR, larger than L2).
 
 JSON line keys (one line, rank 0):
-  value        GTEPS = traversed edges / device time per step (CUDA events on
-               the launching stream; inputs larger than L2)
+  value        batched GTEPS = sum over jobs of traversed edges (out-degree
+               summed over reached vertices) / device time per step (CUDA
+               events on the launching stream)
   e2e          the same metric through the public API with host buffers:
-               per step pinned H2D of the CSR + weights, the run, D2H of dist
-  roofline     achieved algorithmic GB/s of the SSSP kernel vs the HBM peak
-  cpu_baseline the OpenMP oracle (a restatement of the reference's kernel) on
-               the machine's host cores, on a bounded sample
-  extra        barrier ns (10^6 barriers over every co-resident CTA), grid BFS
+               per step pinned H2D of every graph, the launch, D2H of every
+               job's distances
+  roofline     algorithmic GB/s of the batched kernel vs the HBM peak
+  cpu_baseline the oracle (the reference's algorithm restated in C) over
+               the same 1024 jobs, jobs spread over the host cores
+  extra        plain per-graph launches of the same jobs and the speed-up,
+               ns per global barrier (10^6 barriers over every co-resident
+               CTA), persistent SSSP on RMAT-20, served-form latency
 `--impl reference` times the reference's algorithm on the host cores (the
 oracle port: the reference's OpenCL 2.0 program needs fine-grained SVM atomics,
-which no runtime on the box provides).
+which no runtime on the box provides) on the same jobs.
 """
 from __future__ import annotations
 
@@ -34,8 +41,11 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 INF = 1000000000
-RMAT_SCALE, RMAT_EF, RMAT_SEED = 20, 16, 1
 HBM_FALLBACK_GBS = 6800.0
+METRIC = "batched GTEPS vs per-graph launches, bit-exact; barrier ns; p99 task latency"
+WORKLOAD = ("batched Lonestar BFS+SSSP: 512 graphs (log2 V ~ N(13, 2.5) in [8, 18], "
+            "half RMAT (0.57,0.19,0.19) avg degree 8-32, half 2D grids), 1024 jobs, "
+            "seed 2024, weights U[1,1000]")
 
 
 def _peak_hbm() -> tuple[float, str]:
@@ -73,6 +83,7 @@ class Clocks:
     def __init__(self, device: int):
         self.device = device
         self.proc = None
+        self.out = ""
 
     def __enter__(self):
         try:
@@ -85,7 +96,6 @@ class Clocks:
         return self
 
     def __exit__(self, *exc):
-        self.out = ""
         if self.proc is not None:
             self.proc.terminate()
             try:
@@ -122,26 +132,171 @@ def _dist_env():
     return ws, rank, local
 
 
-def _traversed(g, dist) -> tuple[int, int]:
-    """E_t = out-degree summed over reached vertices, V_r = reached vertices."""
-    reached = dist != INF
-    return int(g.degrees()[reached].sum()), int(reached.sum())
+def _max_over_ranks(dist, x: float) -> float:
+    if not dist:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
 
 
-def _cpu_baseline(g, src, budget_s: float = 12.0) -> dict:
+def _job_edges(gs, jobs, res, offsets):
+    """Per job: traversed edges E_t and reached vertices V_r."""
+    et, vr = [], []
+    for k, (gi, _algo, _src) in enumerate(jobs):
+        d = res[offsets[k]:offsets[k + 1]]
+        reached = d != INF
+        et.append(int(gs[gi].degrees()[reached].sum()))
+        vr.append(int(reached.sum()))
+    return np.array(et, np.int64), np.array(vr, np.int64)
+
+
+def _alg_bytes(gs, jobs, et, vr) -> int:
+    """Algorithmic bytes of one batched launch, per job: per traversed edge
+    col (4) and dist[dst] (4), plus the weight (4) for SSSP; per reached
+    vertex its row pair (8), its worklist piece written and read once (start
+    and count, plus the vertex for SSSP: 16 or 24) and its distance (4); per
+    vertex the initialisation of dist (4), and of the SSSP stamp (4)."""
+    total = 0
+    for k, (gi, algo, _src) in enumerate(jobs):
+        V = gs[gi].num_nodes
+        if algo == "sssp":
+            total += 12 * int(et[k]) + 36 * int(vr[k]) + 8 * V
+        else:
+            total += 8 * int(et[k]) + 28 * int(vr[k]) + 4 * V
+    return total
+
+
+def _batch_inputs():
+    from gpu_workgroup_managment_gb300.batch import batch_workload
+    return batch_workload()
+
+
+def _reference_arm(args, ws, rank) -> int:
+    """The reference's algorithm on the host cores: the oracle's job-parallel
+    batched restatement of lonestar bfs.cl / sssp.cl over the same 1024 jobs,
+    every host thread busy.  One step = the whole batch."""
+    if rank != 0:
+        return 0
     from oracle import oracle
-    runs, t_tot, et = 0, 0.0, 0
-    while runs < 50 and t_tot < budget_s:
+    gs, jobs, meta = _batch_inputs()
+    arena = oracle.BatchArena(gs, jobs)
+    d = arena.run()
+    offsets = np.concatenate([[0], np.cumsum(arena.V.astype(np.int64))])
+    et, _ = _job_edges(gs, jobs, d, offsets)
+    E = int(et.sum())
+    warm = max(1, min(args.warmup, 3))
+    for _ in range(warm - 1):
+        arena.run()
+    times = []
+    for _ in range(args.steps):
         t0 = time.perf_counter()
-        d = oracle.lonestar_sssp(g, src, omp=True)
-        t_tot += time.perf_counter() - t0
-        runs += 1
-        if runs == 1:
-            et, _ = _traversed(g, d)
-    return {"value": et * runs / t_tot / 1e9, "unit": "GTEPS", "cores": oracle.threads(),
-            "kind": "port",
-            "sample": f"{runs} full SSSP runs on the same RMAT graph from the max-degree vertex "
-                      f"(OpenMP restatement of lonestar sssp.cl)"}
+        arena.run()
+        times.append(time.perf_counter() - t0)
+    mean = sum(times) / len(times)
+    v = E / mean / 1e9
+    sample = (f"{args.steps} runs of all {len(jobs)} jobs ({E} traversed edges each), jobs "
+              f"spread over {oracle.threads()} threads, each job the serial restatement "
+              "of the reference's bfs.cl/sssp.cl; the reference's OpenCL 2.0 SVM program "
+              "cannot run here")
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "GTEPS",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": warm, "ms_per_step": mean * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+            "data": "synthetic", "config": {"workload": WORKLOAD, "jobs": len(jobs),
+                                            "edges_traversed": E},
+            "cpu_baseline": {"value": v, "unit": "GTEPS", "cores": oracle.threads(),
+                             "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": "GTEPS", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def _barrier_sweep() -> int:
+    from gpu_workgroup_managment_gb300 import Runtime
+    kinds = {0: "sense", 1: "xf", 2: "tree", 3: "count"}
+    with Runtime() as rt:
+        for threads in (128, 256, 512, 1024):
+            for kind, name in kinds.items():
+                r = rt.barrier_bench(iterations=20000, threads_per_wg=threads, barrier_kind=kind)
+                print(json.dumps({"barrier": name, "threads_per_cta": threads,
+                                  "ctas": r["groups"], "barriers": r["barriers"],
+                                  "ns_per_barrier": r["ns_per_barrier"]}))
+    return 0
+
+
+def _sssp_rmat(rt, scale: int, steps: int, warmup: int) -> dict:
+    """Persistent Lonestar SSSP on RMAT scale `scale` (edge factor 16, seed 1,
+    weights U[1,1000]) from the max-degree vertex: one launch per step."""
+    from gpu_workgroup_managment_gb300 import PersistentApp, graphs
+    g = graphs.rmat(scale, 16, seed=1)
+    src = graphs.max_degree_vertex(g)
+    with PersistentApp(rt, "lonestar_sssp", g, source=src) as app:
+        st0 = app.run()
+        d = app.result()
+        reached = d != INF
+        et, vr = int(g.degrees()[reached].sum()), int(reached.sum())
+        for _ in range(warmup):
+            app.launch()
+        rt.synchronize()
+        rt.timer_start()
+        for _ in range(steps):
+            app.launch()
+        ms = rt.timer_stop() / steps
+    return {"gteps": et / (ms * 1e-3) / 1e9, "ms": ms, "levels": st0.rounds,
+            "groups": st0.groups, "edges_traversed": et, "vertices_reached": vr,
+            "bytes_alg": 12 * et + 36 * vr + 8 * g.num_nodes}
+
+
+def _sssp_kernel_only(args) -> int:
+    """The command profiled with ncu for the persistent SSSP kernel."""
+    from gpu_workgroup_managment_gb300 import Runtime
+    with Runtime() as rt:
+        r = _sssp_rmat(rt, args.scale, args.steps, max(args.warmup, 3))
+    print(json.dumps({"metric": "SSSP GTEPS", "workload": f"rmat{args.scale}_sssp", **r}))
+    return 0
+
+
+def _served(rt, rates=(1000, 5000, 20000), reps: int = 3, reserve: int = 48) -> dict:
+    """Served form: a resident colour+BFS job on RMAT scale 22 (edge factor
+    16, seed 1; BFS from the max-degree vertex), `reps` repetitions, alone and
+    beside a Poisson request stream at each rate: 40% BFS queries on RMAT
+    graphs of scale 12-16, 30% FP32 min reductions of 2^20 elements, 30% FP32
+    256x256 products; the stream lasts as long as the persistent job."""
+    from gpu_workgroup_managment_gb300 import PersistentApp, graphs
+    from gpu_workgroup_managment_gb300.serve import Serve, serve_datasets
+    g = graphs.rmat(22, 16, seed=1)
+    nv = graphs.seeded_node_values(g.num_nodes, 1)
+    src = graphs.max_degree_vertex(g)
+    qg, vecs, mats = serve_datasets(seed=7)
+    out = {"persistent": "colour + Lonestar BFS, RMAT-22", "reps": reps, "reserve": reserve,
+           "mix": "40% BFS (RMAT 12-16), 30% FP32 min 2^20, 30% FP32 256x256 matmul",
+           "teams": {"bfs": 8, "reduce": 4, "matmul": 4}}
+    with PersistentApp(rt, "color", g, node_values=nv) as ca, \
+            PersistentApp(rt, "lonestar_bfs", g, source=src) as ba, \
+            Serve(rt, ca, ba, graphs=qg, vecs=vecs, mats=mats, arena_bytes=1 << 30) as sv:
+        sv.run(reps=1)
+        alone = sv.run(reps=reps)
+        out["persist_ms_alone"] = alone["persist_ms"]
+        runs = []
+        for rate in rates:
+            st = sv.run(rate=rate, duration_s=60.0, reps=reps, seed=11, reserve=reserve,
+                        bfs_groups=8, reduce_groups=4, matmul_groups=4, max_in_flight=512)
+            runs.append({"rate_offered": rate, "achieved_rate": st["achieved_rate"],
+                         "completed": st["completed"], "p50_us": st["lat_p50_us"],
+                         "p99_us": st["lat_p99_us"], "mean_us": st["lat_mean_us"],
+                         "max_us": st["lat_max_us"], "persist_ms": st["persist_ms"],
+                         "persist_kept": alone["persist_ms"] / st["persist_ms"],
+                         "kills": st["kills"], "forks": st["forks"],
+                         "waited_for_memory": st["waited_for_memory"]})
+        out["runs"] = runs
+        # requests alone (no persistent job) at the lowest rate, for context
+        st = sv.run(rate=rates[0], duration_s=0.5, seed=11, bfs_groups=8, reduce_groups=4,
+                    matmul_groups=4)
+        out["requests_only"] = {"rate_offered": rates[0], "p50_us": st["lat_p50_us"],
+                                "p99_us": st["lat_p99_us"], "completed": st["completed"]}
+    return out
 
 
 def main() -> int:
@@ -150,177 +305,176 @@ def main() -> int:
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="wgm", choices=["wgm", "reference"])
-    ap.add_argument("--no-extra", action="store_true")
-    ap.add_argument("--scale", type=int, default=RMAT_SCALE)
+    ap.add_argument("--no-extra", action="store_true", help="skip the extra measurements")
     ap.add_argument("--kernel-only", action="store_true",
-                    help="time the device steps only (no e2e, extras or CPU baseline); "
-                         "the command profiled with ncu")
+                    help="batched launches only (the command profiled with ncu)")
+    ap.add_argument("--sssp-kernel-only", action="store_true",
+                    help="persistent SSSP on RMAT --scale only (profiled with ncu)")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="fixed shape (256 threads, teams of 50000 edges) instead of the autotuner")
+    ap.add_argument("--scale", type=int, default=20)
     ap.add_argument("--barrier-sweep", action="store_true",
-                    help="ns per barrier for every barrier kind and CTA size, one JSON line each")
+                    help="ns per barrier for every barrier kind and CTA size")
+    ap.add_argument("--served", action="store_true", help="served-form measurement only")
     args = ap.parse_args()
-    scale = args.scale
     if args.barrier_sweep:
-        from gpu_workgroup_managment_gb300 import Runtime
-        kinds = {0: "sense", 1: "xf", 2: "tree", 3: "count"}
-        with Runtime() as rt:
-            for threads in (128, 256, 512, 1024):
-                for kind, name in kinds.items():
-                    r = rt.barrier_bench(iterations=20000, threads_per_wg=threads,
-                                         barrier_kind=kind)
-                    print(json.dumps({"barrier": name, "threads_per_cta": threads,
-                                      "ctas": r["groups"], "barriers": r["barriers"],
-                                      "ns_per_barrier": r["ns_per_barrier"]}))
-        return 0
-    warmup = max(args.warmup, 3)
+        return _barrier_sweep()
+    if args.sssp_kernel_only:
+        return _sssp_kernel_only(args)
     ws, rank, local = _dist_env()
     dist = None
     if ws > 1:
         import torch.distributed as td
         td.init_process_group("gloo")
         dist = td
-
-    from gpu_workgroup_managment_gb300 import graphs
-
-    workload = f"rmat{scale}_sssp"
-    config = {"workload": f"persistent Lonestar SSSP, RMAT scale {scale} edge factor "
-                          f"{RMAT_EF} (0.57,0.19,0.19) seed {RMAT_SEED}, weights U[1,1000], "
-                          f"source = max-degree vertex",
-              "graph": f"rmat{scale}", "parallelism": f"replicas{args.gpus}",
-              "l2": "inputs larger than L2 (CSR+weights > 129 MB), no flush"}
-
     if args.impl == "reference":
-        if rank != 0:
-            return 0
-        g = graphs.rmat(scale, RMAT_EF, seed=RMAT_SEED)
-        src = graphs.max_degree_vertex(g)
-        from oracle import oracle
-        for _ in range(1):
-            oracle.lonestar_sssp(g, src, omp=True)
-        times, et = [], 0
-        for i in range(args.steps):
-            t0 = time.perf_counter()
-            d = oracle.lonestar_sssp(g, src, omp=True)
-            times.append(time.perf_counter() - t0)
-            if i == 0:
-                et, _ = _traversed(g, d)
-        mean = sum(times) / len(times)
-        v = et / mean / 1e9
-        line = {"impl": "reference", "metric": "SSSP GTEPS (persistent Lonestar, RMAT-20)",
-                "value": v, "unit": "GTEPS", "n_gpus": args.gpus, "steps": args.steps,
-                "warmup": 1, "ms_per_step": mean * 1e3, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-                "config": config,
-                "cpu_baseline": {"value": v, "unit": "GTEPS", "cores": oracle.threads(),
-                                 "kind": "port",
-                                 "sample": f"{args.steps} full SSSP runs (OpenMP restatement "
-                                           "of the reference's sssp.cl; the reference's OpenCL "
-                                           "2.0 SVM program cannot run here)"},
-                "e2e": {"value": v, "unit": "GTEPS", "h2d_bytes_per_step": 0,
-                        "d2h_bytes_per_step": 0}}
-        print(json.dumps(line))
+        rc = _reference_arm(args, ws, rank)
+        if dist:
+            dist.destroy_process_group()
+        return rc
+    if args.served:
+        from gpu_workgroup_managment_gb300 import Runtime
+        with Runtime(device=local) as rt:
+            print(json.dumps(_served(rt)))
         return 0
+    warmup = max(args.warmup, 3)
 
-    from gpu_workgroup_managment_gb300 import PersistentApp, Runtime
+    from gpu_workgroup_managment_gb300 import Runtime
     from gpu_workgroup_managment_gb300._lib import lib
+    from gpu_workgroup_managment_gb300.batch import Batch
     from gpu_workgroup_managment_gb300.runtime import pinned_copy
+    from gpu_workgroup_managment_gb300 import graphs as G
 
-    g = graphs.rmat(scale, RMAT_EF, seed=RMAT_SEED)
-    src = graphs.max_degree_vertex(g)
+    gs, jobs, meta = _batch_inputs()
     rt = Runtime(device=local)
-    app = PersistentApp(rt, "lonestar_sssp", g, source=src)
-    # correctness of the benchmarked kernel (checked once, outside the timing)
-    st0 = app.run()
-    d = app.result()
-    et, vr = _traversed(g, d)
-
+    b = Batch(rt, gs, jobs)
+    b.run(use_cuda_graph=False)
+    res = b.results()
+    et, vr = _job_edges(gs, jobs, res, b.offsets)
+    E = int(et.sum())
+    if args.no_tune:
+        b.configure(256, 0, 0)
+        b.configure_teams(50000, 0)
+        b.run()
+        b.reorder_by_last_run()
+        tuned = {"threads": 256, "ctas_per_sm": 0, "piece": 0, "team_edges": 50000}
+    else:
+        tuned = b.autotune(reps=2)
     for _ in range(warmup):
-        app.launch()
+        b.launch(True)
     rt.synchronize()
     if dist:
         dist.barrier()
     with Clocks(local) as clk:
         rt.timer_start()
         for _ in range(args.steps):
-            app.launch()
+            b.launch(True)
         ms_total = rt.timer_stop()
-    ms_step = ms_total / args.steps
-    if dist:
-        import torch
-        t = torch.tensor([ms_step], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_step = float(t.item())
-    value = et * ws / (ms_step * 1e-3) / 1e9
+    ms_step = _max_over_ranks(dist, ms_total / args.steps)
+    value = E * ws / (ms_step * 1e-3) / 1e9
+    if not np.array_equal(b.results(), res):
+        raise SystemExit("batched results changed between launches")
     if args.kernel_only:
         if rank == 0:
-            print(json.dumps({"metric": "SSSP GTEPS", "value": value, "ms_per_step": ms_step,
-                              "levels": st0.rounds, "groups": st0.groups,
-                              "edges_traversed": et, "workload": workload}))
-        app.close()
+            print(json.dumps({"metric": "batched GTEPS", "value": value, "ms_per_step": ms_step,
+                              "edges_traversed": E, "tuned": tuned}))
+        b.close()
         rt.close()
         return 0
 
-    # e2e through the public API with pinned host buffers
-    rp, p1 = pinned_copy(g.row_ptr)
-    cl, p2 = pinned_copy(g.col)
-    wt, p3 = pinned_copy(g.weights)
-    out, p4 = pinned_copy(np.empty(g.num_nodes, np.uint32))
-    hg = graphs.Graph(rp, cl, wt)
+    # e2e through the public API: pinned host graphs up, batched launch, results down
+    keep, hgs = [], []
+    for g in gs:
+        rp, p1 = pinned_copy(g.row_ptr)
+        cl, p2 = pinned_copy(g.col)
+        wt, p3 = pinned_copy(g.weights)
+        keep += [p1, p2, p3]
+        hgs.append(G.Graph(rp, cl, wt))
+    out, p4 = pinned_copy(np.empty(int(b.offsets[-1]), np.uint32))
+    keep.append(p4)
     for _ in range(2):
-        app.upload(hg)
-        app.launch()
-        app.result(out)
+        b.upload(hgs)
+        b.launch(True)
+        b.results(out)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        app.upload(hg)
-        app.launch()
-        app.result(out)
-    e2e_s = (time.perf_counter() - t0) / args.steps
-    assert np.array_equal(out, d)
-    h2d = rp.nbytes + cl.nbytes + wt.nbytes
+        b.upload(hgs)
+        b.launch(True)
+        b.results(out)
+    e2e_s = _max_over_ranks(dist, (time.perf_counter() - t0) / args.steps)
+    if not np.array_equal(out, res):
+        raise SystemExit("e2e results differ")
+    h2d = sum(g.row_ptr.nbytes + g.col.nbytes + g.weights.nbytes for g in gs)
     d2h = out.nbytes
+    for p in keep:
+        lib.wgm_host_free(p)
 
-    bytes_alg = 12 * et + 20 * vr  # SSSP algorithmic bytes per launch
+    bytes_alg = _alg_bytes(gs, jobs, et, vr)
     peak, peak_kind = _peak_hbm()
     achieved = bytes_alg / (ms_step * 1e-3) / 1e9
     line = {
-        "metric": "SSSP GTEPS (persistent Lonestar, RMAT-20)", "value": value, "unit": "GTEPS",
-        "n_gpus": args.gpus, "steps": args.steps, "warmup": warmup, "ms_per_step": ms_step,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
-        "data": "synthetic", "config": config,
-        "e2e": {"value": et / e2e_s / 1e9, "unit": "GTEPS", "h2d_bytes_per_step": h2d,
+        "metric": METRIC, "value": value, "unit": "GTEPS", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": warmup, "ms_per_step": ms_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "jobs": len(jobs), "graphs": meta["graphs"],
+                   "nodes_total": meta["nodes_total"], "edges_total": meta["edges_total"],
+                   "edges_traversed": E, "parallelism": f"replicas{args.gpus}",
+                   "cuda_graph": True, "tuned": tuned,
+                   "l2": "inputs larger than L2 (1.4 GB CSR + weights), no flush"},
+        "e2e": {"value": E * ws / e2e_s / 1e9, "unit": "GTEPS", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind,
-                     "traffic": _traffic("wgm_k_sssp", workload),
-                     "bytes_alg_per_launch": bytes_alg, "edges_traversed": et,
-                     "vertices_reached": vr, "levels": st0.rounds, "groups": st0.groups},
+                     "traffic": _traffic("wgm_k_batch", "batch512"),
+                     "bytes_alg_per_launch": bytes_alg, "kernel": "wgm_k_batch"},
         "clocks": clk.summary(),
         "gpu_launches": args.steps,
     }
-    for ptr in (p1, p2, p3, p4):
-        lib.wgm_host_free(ptr)
-
     if rank == 0 and not args.no_extra:
         extra = {}
+        pg = b.run_per_graph()
+        pg = min(pg, b.run_per_graph())
+        if not np.array_equal(b.results(), res):
+            raise SystemExit("per-graph results differ from the batched ones")
+        extra["per_graph_ms"] = pg
+        extra["per_graph_gteps"] = E / (pg * 1e-3) / 1e9
+        extra["speedup_vs_per_graph"] = pg / ms_step
+        st = b.job_stats()
+        extra["makespan_ms"] = float(st["end_ns"].max()) / 1e6
+        extra["max_team"] = int(st["team"].max())
         bb = rt.barrier_bench(iterations=100000, threads_per_wg=256)
         extra["barrier_ns"] = bb["ns_per_barrier"]
-        extra["barrier_groups"] = bb["groups"]
-        gg = graphs.lonestar_view(graphs.grid(256, 256))
-        with PersistentApp(rt, "lonestar_bfs", gg) as ga:
-            ga.run()
-            rt.timer_start()
-            for _ in range(5):
-                ga.launch()
-            ms = rt.timer_stop() / 5
-            lv = ga.result()
-        extra["grid256_bfs_ms"] = ms
-        extra["grid256_bfs_levels"] = int(lv.max())
-        extra["grid256_ns_per_level"] = ms * 1e6 / int(lv.max())
+        extra["barrier_ctas"] = bb["groups"]
+        extra["barrier_count"] = bb["barriers"]
+        bb = rt.barrier_bench(iterations=100000, threads_per_wg=1024)
+        extra["barrier_ns_1024_threads"] = bb["ns_per_barrier"]
+        extra["barrier_ctas_1024_threads"] = bb["groups"]
+        extra["sssp_rmat20"] = _sssp_rmat(rt, 20, 5, 3)
+        try:
+            extra["served"] = _served(rt)
+        except Exception as exc:  # reported, not hidden
+            extra["served"] = {"error": repr(exc)}
         line["extra"] = extra
+    b.close()
     if rank == 0:
-        line["cpu_baseline"] = _cpu_baseline(g, src)
+        from oracle import oracle
+        arena = oracle.BatchArena(gs, jobs)
+        d = arena.run()
+        if not np.array_equal(d, res):
+            raise SystemExit("batched results differ from the oracle")
+        line["config"]["oracle_checked"] = True
+        runs, t_tot = 0, 0.0
+        while runs < 20 and t_tot < 12.0:
+            t0 = time.perf_counter()
+            arena.run()
+            t_tot += time.perf_counter() - t0
+            runs += 1
+        line["cpu_baseline"] = {
+            "value": E * runs / t_tot / 1e9, "unit": "GTEPS", "cores": oracle.threads(),
+            "kind": "port",
+            "sample": f"{runs} runs of all {len(jobs)} jobs, jobs spread over the host "
+                      "threads, each the serial restatement of lonestar bfs.cl/sssp.cl"}
         print(json.dumps(line))
-    app.close()
     rt.close()
     if dist:
         dist.destroy_process_group()

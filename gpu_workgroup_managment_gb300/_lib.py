@@ -124,6 +124,7 @@ _PROTOS = {
     "wgm_batch_upload": (_I, [_P, _P]),
     "wgm_batch_configure": (_I, [_P, _I, _I, _I]),
     "wgm_batch_configure_teams": (_I, [_P, C.c_int64, _I]),
+    "wgm_batch_team_info": (_I, [_P, _P, _P]),
     "wgm_batch_job_stats": (_I, [_P, _P, _P, _P, _P]),
     "wgm_batch_reorder_by_last_run": (_I, [_P]),
     "wgm_serve_create": (_I, [_P, _P, _P, _I, _P, _I, _I, _P, _I, _I, _P, C.c_int64, _P]),
@@ -131,6 +132,7 @@ _PROTOS = {
     "wgm_serve_requests": (_I, [_P, _P, _P, _P, _P, _P, _P]),
     "wgm_serve_result": (_I, [_P, C.c_int64, _P, C.c_int64]),
     "wgm_serve_destroy": (_I, [_P]),
+    "wgm_serve_diag": (_I, [_P, C.c_char_p, C.c_size_t]),
     "wgm_batch_launch": (_I, [_P, _I]),
     "wgm_batch_run": (_I, [_P, _I, C.POINTER(C.c_double)]),
     "wgm_batch_launch_per_graph": (_I, [_P]),

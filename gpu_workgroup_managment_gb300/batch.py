@@ -108,7 +108,10 @@ class Batch:
         t, c, p, ms = C.c_int(), C.c_int(), C.c_int(), C.c_double()
         check(lib.wgm_batch_autotune(self._h, reps, C.byref(t), C.byref(c), C.byref(p),
                                      C.byref(ms)), "wgm_batch_autotune")
-        return {"threads": t.value, "ctas_per_sm": c.value, "piece": p.value, "ms": ms.value}
+        te, mt = C.c_int64(), C.c_int()
+        check(lib.wgm_batch_team_info(self._h, C.byref(te), C.byref(mt)))
+        return {"threads": t.value, "ctas_per_sm": c.value, "piece": p.value, "ms": ms.value,
+                "team_edges": te.value, "max_team": mt.value}
 
     def close(self):
         if self._h:

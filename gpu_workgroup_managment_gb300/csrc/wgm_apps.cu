@@ -552,8 +552,11 @@ extern "C" int wgm_app_result_device_ptr(wgm_app *a, void **p, size_t *bytes) {
 extern "C" int wgm_app_rounds(wgm_app *a, int *rounds) {
   if (!a || !rounds) return WGM_ERR_INVALID;
   cudaSetDevice(a->rt->device);
-  cudaError_t e = cudaMemcpy(rounds, a->d_rounds, 4, cudaMemcpyDeviceToHost);
+  int h = 0;
+  cudaError_t e = cudaMemcpyAsync(&h, a->d_rounds, 4, cudaMemcpyDeviceToHost, a->rt->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(a->rt->stream);
   if (e != cudaSuccess) return wgm_cuda_fail(a->rt, e);
+  *rounds = h;
   return WGM_OK;
 }
 

@@ -300,10 +300,13 @@ static int wgm_batch_teams(wgm_batch *b, int grid) {
   }
   b->nslots = (int)slots.size();
   if (e == cudaSuccess)
-    e = cudaMemcpy(b->d_slots, slots.data(), slots.size() * sizeof(int2), cudaMemcpyHostToDevice);
+    e = cudaMemcpyAsync(b->d_slots, slots.data(), slots.size() * sizeof(int2),
+                        cudaMemcpyHostToDevice, b->rt->stream);
   if (e == cudaSuccess)
-    e = cudaMemcpy(b->d_jobs, b->jobs.data(), sizeof(wgm_batch_job) * b->jobs.size(),
-                   cudaMemcpyHostToDevice);
+    e = cudaMemcpyAsync(b->d_jobs, b->jobs.data(), sizeof(wgm_batch_job) * b->jobs.size(),
+                        cudaMemcpyHostToDevice, b->rt->stream);
+  /* pageable sources: wait until the copies are done before they change */
+  if (e == cudaSuccess) e = cudaStreamSynchronize(b->rt->stream);
   if (e != cudaSuccess) return wgm_cuda_fail(b->rt, e);
   return WGM_OK;
 }
@@ -317,7 +320,7 @@ static int wgm_batch_check(wgm_batch *b) {
   b->rt->last_status = h[0];
   b->rt->last_site = h[1];
   b->rt->last_detail = 0;
-  cudaMemset(b->d_err, 0, sizeof(h));
+  cudaMemsetAsync(b->d_err, 0, sizeof(h), b->rt->stream);
   return wgm_status_from_device(h[0]);
 }
 
@@ -347,8 +350,9 @@ extern "C" int wgm_batch_configure(wgm_batch *b, int threads_per_cta, int ctas_p
     b->d_scratch = nullptr;
     cudaError_t e = cudaMalloc((void **)&b->d_scratch, std::max<long long>(b->scratch_total, 1) * 4);
     if (e == cudaSuccess)
-      e = cudaMemcpy(b->d_jobs, b->jobs.data(), sizeof(wgm_batch_job) * b->jobs.size(),
-                     cudaMemcpyHostToDevice);
+      e = cudaMemcpyAsync(b->d_jobs, b->jobs.data(), sizeof(wgm_batch_job) * b->jobs.size(),
+                          cudaMemcpyHostToDevice, b->rt->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->rt->stream);
     if (e != cudaSuccess) return wgm_cuda_fail(b->rt, e);
   }
   b->teams_grid = 0;
@@ -651,5 +655,12 @@ extern "C" int wgm_batch_reorder_by_last_run(wgm_batch *b) {
   b->jobs.swap(jobs);
   b->teams_grid = 0;
   wgm_batch_free_graph(b);
+  return WGM_OK;
+}
+
+extern "C" int wgm_batch_team_info(wgm_batch *b, int64_t *team_edges, int *max_team) {
+  if (!b) return WGM_ERR_INVALID;
+  if (team_edges) *team_edges = b->team_edges;
+  if (max_team) *max_team = b->max_team;
   return WGM_OK;
 }

@@ -280,6 +280,9 @@ static int wgm_np_init(wgm_comm *c) {
   } else if (kind != 0) {
     return WGM_ERR_INVALID;
   }
+  /* the copies above come from pageable memory and may still be in flight
+   * when cudaMemcpy returns; the megakernel runs on a non-blocking stream */
+  if ((e = cudaDeviceSynchronize()) != cudaSuccess) return wgm_comm_fail(c, e);
   return WGM_OK;
 }
 

@@ -19,6 +19,7 @@
 #include <map>
 #include <new>
 #include <random>
+#include <string>
 #include <thread>
 #include <vector>
 
@@ -195,7 +196,7 @@ struct wgm_serve {
   /* last run */
   std::vector<wgm_serve_req_log> log;
   std::vector<char> results;
-  int last_groups = 0;
+  std::string diag; /* where the last failed run stood */
 };
 
 static size_t wgm_req_bytes(const wgm_serve *s, int kind, int arg0) {
@@ -329,15 +330,51 @@ extern "C" int wgm_serve_create(wgm_runtime *rt, wgm_app *color, wgm_app *bfs, i
     wgm_serve_destroy(s);
     return st;
   }
+  /* pageable-source copies may still be in flight when cudaMemcpy returns;
+   * the serving kernel runs on the runtime's non-blocking stream */
+  if ((e = cudaDeviceSynchronize()) != cudaSuccess) {
+    int st = wgm_cuda_fail(rt, e);
+    wgm_serve_destroy(s);
+    return st;
+  }
   s->arena_bytes = (size_t)arena_bytes;
   *out = s;
   return WGM_OK;
 }
 
-static int wgm_serve_fail_run(wgm_serve *s, int status) {
+/* Where a failed run stood: host counters, then the serving and pool words
+ * after the kernel ended. */
+static void wgm_serve_diag_fill(wgm_serve *s, const char *why, int64_t head, size_t inflight,
+                                size_t waiting, size_t next, size_t narr) {
+  wgm_runtime *rt = s->rt;
+  wgm_serve_dev sd;
+  std::memset(&sd, 0, sizeof(sd));
+  int avail = -1, lock = -1, tk = -1, exe = -1, err[2] = {0, 0};
+  cudaMemcpy(&sd, s->d_sd, sizeof(sd), cudaMemcpyDeviceToHost);
+  cudaMemcpy(&avail, &rt->st->available_workgroups, 4, cudaMemcpyDeviceToHost);
+  cudaMemcpy(&lock, &rt->st->pool_lock, 4, cudaMemcpyDeviceToHost);
+  cudaMemcpy(&tk, &rt->st->groups_to_kill, 4, cudaMemcpyDeviceToHost);
+  cudaMemcpy(&exe, &rt->st->k_executing[1][0], 4, cudaMemcpyDeviceToHost);
+  cudaMemcpy(err, s->d_err, 8, cudaMemcpyDeviceToHost);
+  char buf[640];
+  std::snprintf(buf, sizeof(buf),
+                "%s: host head=%lld inflight=%zu waiting=%zu arrivals=%zu/%zu; device "
+                "seen=%d started=%d completed=%d pending=%d persist_reps=%d kills=%d forks=%d "
+                "available=%d pool_lock=%d to_kill=%d executing=%d discovered=%d; team err=%d "
+                "site=%d; device status=%d site=%d detail=%d",
+                why, (long long)head, inflight, waiting, next, narr, s->hs_h->seen,
+                s->hs_h->started, sd.completed, sd.pending, sd.persist_done, sd.kills, sd.forks,
+                avail, lock, tk, exe, rt->hf->discovered, err[0], err[1], rt->hf->status,
+                rt->hf->status_site, rt->hf->status_detail);
+  s->diag = buf;
+}
+
+static int wgm_serve_fail_run(wgm_serve *s, int status, const char *why, int64_t head,
+                              size_t inflight, size_t waiting, size_t next, size_t narr) {
   wgm_set_abort(s->rt, 1);
   __atomic_store_n(&s->hs_h->quit, 1, __ATOMIC_RELEASE);
   cudaStreamSynchronize(s->rt->stream);
+  wgm_serve_diag_fill(s, why, head, inflight, waiting, next, narr);
   wgm_set_abort(s->rt, 0);
   int ds = 0, site = 0;
   wgm_finish_launch(s->rt, &ds, &site);
@@ -407,13 +444,19 @@ extern "C" int wgm_serve_run(wgm_serve *s, const wgm_serve_config *cfg, wgm_serv
   std::memset(s->ring_h, 0, sizeof(wgm_req) * s->ring);
   std::memset(s->comp_h, 0, 4 * (size_t)s->ring);
   std::memset((void *)s->hs_h, 0, sizeof(wgm_serve_host));
-  e = cudaMemset(s->d_sd, 0, sizeof(wgm_serve_dev));
-  if (e == cudaSuccess) e = cudaMemset(s->d_err, 0, 8);
-  int reserve = std::max(0, cfg->reserve);
-  if (e == cudaSuccess)
-    e = cudaMemcpy(&s->d_sd->reserve, &reserve, 4, cudaMemcpyHostToDevice);
+  /* stream-ordered before the launch (the runtime's stream does not wait
+   * for the legacy stream): the serving words, the error word, and the pool
+   * words of the runtime state, which a previous megakernel may have left
+   * elsewhere */
+  cudaStream_t rs = rt->stream;
+  e = cudaMemsetAsync(s->d_sd, 0, sizeof(wgm_serve_dev), rs);
+  if (e == cudaSuccess) e = cudaMemsetAsync(&rt->st->available_workgroups, 0, 4, rs);
+  if (e == cudaSuccess) e = cudaMemsetAsync(&rt->st->pool_lock, 0, 4, rs);
+  if (e == cudaSuccess) e = cudaMemsetAsync(&rt->st->bar_count, 0, 4, rs);
+  if (e == cudaSuccess) e = cudaMemsetAsync(s->d_err, 0, 8, rs);
   if (e != cudaSuccess) return wgm_cuda_fail(rt, e);
   s->arena.init(s->arena_bytes);
+  s->diag.clear();
   s->log.clear();
   s->results.clear();
 
@@ -445,6 +488,7 @@ extern "C" int wgm_serve_run(wgm_serve *s, const wgm_serve_config *cfg, wgm_serv
   A.mats = s->d_mats;
   A.mat_n = s->mat_n;
   A.err = s->d_err;
+  A.reserve = std::max(0, cfg->reserve);
   const uint64_t run_budget = rt->cfg.run_timeout_ns ? rt->cfg.run_timeout_ns : 120000000000ull;
   A.idle_ns = run_budget;
   __atomic_store_n(&rt->hf->persistent_flag, 0, __ATOMIC_RELEASE);
@@ -465,9 +509,12 @@ extern "C" int wgm_serve_run(wgm_serve *s, const wgm_serve_config *cfg, wgm_serv
   const int reps = A.reps;
   for (;;) {
     const uint64_t now = wgm_serve_now() - t0;
-    if (now > run_budget) return wgm_serve_fail_run(s, WGM_ERR_TIMEOUT);
+    if (now > run_budget)
+      return wgm_serve_fail_run(s, WGM_ERR_TIMEOUT, "run budget", head, inflight.size(),
+                                waiting.size() - wait_head, next, arr.size());
     if (__atomic_load_n(&rt->hf->status, __ATOMIC_ACQUIRE) != 0)
-      return wgm_serve_fail_run(s, WGM_ERR_TIMEOUT);
+      return wgm_serve_fail_run(s, WGM_ERR_TIMEOUT, "device failure", head, inflight.size(),
+                                waiting.size() - wait_head, next, arr.size());
     if (reps > 0 && !persist_done_at &&
         __atomic_load_n(&s->hs_h->persist_reps, __ATOMIC_ACQUIRE) >= reps) {
       persist_done_at = now;
@@ -529,7 +576,9 @@ extern "C" int wgm_serve_run(wgm_serve *s, const wgm_serve_config *cfg, wgm_serv
                               s->d_arena + lg.state_off + wgm_req_result_off(lg.kind), rb,
                               cudaMemcpyDeviceToHost, s->side);
           if (e == cudaSuccess) e = cudaStreamSynchronize(s->side);
-          if (e != cudaSuccess) return wgm_serve_fail_run(s, wgm_cuda_fail(rt, e));
+          if (e != cudaSuccess)
+            return wgm_serve_fail_run(s, wgm_cuda_fail(rt, e), "result copy", head,
+                                      inflight.size(), 0, next, arr.size());
         }
         s->arena.release(lg.state_off, lg.state_bytes);
         inflight[k] = inflight.back();
@@ -542,6 +591,7 @@ extern "C" int wgm_serve_run(wgm_serve *s, const wgm_serve_config *cfg, wgm_serv
   }
   __atomic_store_n(&s->hs_h->quit, 1, __ATOMIC_RELEASE);
   int status = wgm_synchronize(rt);
+  if (status) wgm_serve_diag_fill(s, "after quit", head, inflight.size(), 0, next, arr.size());
   const uint64_t t_end = wgm_serve_now() - t0;
   int herr[2] = {0, 0};
   if (cudaMemcpy(herr, s->d_err, 8, cudaMemcpyDeviceToHost) == cudaSuccess && herr[0] && !status)
@@ -613,5 +663,11 @@ extern "C" int wgm_serve_result(wgm_serve *s, int64_t i, void *out, int64_t byte
   const size_t rb = wgm_req_result_bytes(s, lg.kind, lg.arg0);
   if (bytes < (int64_t)rb) return WGM_ERR_INVALID;
   std::memcpy(out, s->results.data() + lg.result_at, rb);
+  return WGM_OK;
+}
+
+extern "C" int wgm_serve_diag(wgm_serve *s, char *buf, size_t len) {
+  if (!s || !buf || len == 0) return WGM_ERR_INVALID;
+  std::snprintf(buf, len, "%s", s->diag.c_str());
   return WGM_OK;
 }

@@ -64,8 +64,7 @@ struct wgm_serve_dev {
   int slot_rank[WGM_MAX_GROUPS];      /* rank in that request's team */
   int pending;                        /* requests seen but not yet given groups */
   int pad0[WGM_LINE - 1];
-  int reserve;                        /* free groups the fork leaves for requests */
-  int pad1[WGM_LINE - 1];
+  int pad1[WGM_LINE];
   int persist_done;                   /* persistent repetitions completed */
   int pad2[WGM_LINE - 1];
   int kills;                          /* groups ceded by the persistent job */
@@ -107,6 +106,7 @@ struct wgm_serve_args {
   const float *mats; /* matmul operand pairs: A then B, mat_n^2 floats each */
   int mat_n;
   int *err;          /* team waits: first error, site */
+  int reserve;       /* free groups the fork leaves for requests */
   unsigned long long idle_ns;
 };
 
@@ -193,13 +193,19 @@ __device__ void wgm_req_reduce(const wgm_serve_args &A, const wgm_req &r, int ra
   const float *x = A.vecs + (size_t)r.arg0 * A.vec_len;
   const int gid = rank * blockDim.x + threadIdx.x, nth = r.groups * blockDim.x;
   int m = INT_MAX;
-  const int n4 = A.vec_len >> 2;
+  const int len = A.vec_len;
+  /* vectors start wherever vec_len puts them: scalar loads up to the first
+   * 16-byte boundary, float4 loads for the body, scalar loads for the tail */
+  const int pre = min(len, (int)(((16u - ((unsigned)(uintptr_t)x & 15u)) & 15u) >> 2));
+  const int n4 = (len - pre) >> 2;
+  const float4 *x4 = reinterpret_cast<const float4 *>(x + pre);
+  for (int i = gid; i < pre; i += nth) m = min(m, __float_as_int(__ldg(&x[i])));
   for (int i = gid; i < n4; i += nth) {
-    float4 v = __ldg(reinterpret_cast<const float4 *>(x) + i);
+    float4 v = __ldg(x4 + i);
     m = min(m, min(min(__float_as_int(v.x), __float_as_int(v.y)),
                    min(__float_as_int(v.z), __float_as_int(v.w))));
   }
-  for (int i = (n4 << 2) + gid; i < A.vec_len; i += nth) m = min(m, __float_as_int(__ldg(&x[i])));
+  for (int i = pre + (n4 << 2) + gid; i < len; i += nth) m = min(m, __float_as_int(__ldg(&x[i])));
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) m = min(m, __shfl_xor_sync(WGM_FULL, m, o));
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
@@ -337,8 +343,7 @@ static __device__ int wgm_serve_barrier(const wgm_launch &L, wgm_cta *c, wgm_ste
           wgm_st_relaxed_gpu(&st->bar_count, 0);
           n = wgm_ld_acquire_gpu(kng);
           if (wgm_ld_acquire_gpu(&A.sd->pending) == 0) {
-            int spare = wgm_ld_acquire_gpu(&st->available_workgroups) -
-                        wgm_ld_relaxed_gpu(&A.sd->reserve);
+            int spare = wgm_ld_acquire_gpu(&st->available_workgroups) - A.reserve;
             want = min(spare, WGM_SERVE_FORK_MAX);
             if (want > 0 && !wgm_try_lock(&st->pool_lock)) want = 0;
           }
@@ -436,6 +441,11 @@ static __device__ bool wgm_serve_scheduler(const wgm_launch &L, const wgm_serve_
   const int nslots = lpg + 1; /* worker slots 1..lpg; slot 0 (the scheduler) has no bit */
   wgm_rctx rc;
   for (int k = 0; k < WGM_RCTX_WORDS; k++) rc.w[k] = 0;
+  if (lane == 0) {
+    wgm_st_relaxed_gpu(&st->k_executing[1][0], 0);
+    wgm_st_relaxed_gpu(&st->k_num_groups[1][0], 0);
+    wgm_st_relaxed_gpu(&st->groups_to_kill, 0);
+  }
   /* every worker enters the pool first */
   int ok = 1;
   if (lane == 0)
@@ -468,8 +478,12 @@ static __device__ bool wgm_serve_scheduler(const wgm_launch &L, const wgm_serve_
   wgm_spin idle = wgm_idle_start(L, A.idle_ns);
   for (;;) {
     bool progress = false;
-    /* new descriptors: host ring (mapped) -> device ring */
-    const int head = wgm_bcast(lane == 0 ? wgm_ld_acquire_sys(&A.hs->head) : 0);
+    /* new descriptors: host ring (mapped) -> device ring.  Every lane takes
+     * the head with its own acquire load (and the warp the smallest value),
+     * so each lane's reads of the descriptor words are ordered after the
+     * host's writes of them. */
+    const int head = (int)__reduce_min_sync(
+        WGM_FULL, (unsigned)wgm_ld_acquire_sys(&A.hs->head));
     if (head != seen) {
       for (int idx = seen; idx != head; idx++) {
         const int ri = idx % A.ring_size;
@@ -477,9 +491,9 @@ static __device__ bool wgm_serve_scheduler(const wgm_launch &L, const wgm_serve_
         int *dst = reinterpret_cast<int *>(&A.dreq[ri]);
         if (lane < (int)(sizeof(wgm_req) / 4)) dst[lane] = wgm_ld_relaxed_sys(src + lane);
       }
+      __threadfence();
       __syncwarp();
       if (lane == 0) {
-        __threadfence();
         atomicAdd(&sd->pending, head - seen);
         wgm_st_relaxed_sys(&A.hs->seen, head);
       }

@@ -53,7 +53,11 @@ class Serve:
                            reserve, bfs_groups, reduce_groups, matmul_groups, max_in_flight,
                            int(keep_results), threads_per_wg)
         st = WgmServeStats()
-        check(lib.wgm_serve_run(self._h, C.byref(c), C.byref(st)), "wgm_serve_run")
+        rc = lib.wgm_serve_run(self._h, C.byref(c), C.byref(st))
+        if rc:
+            buf = C.create_string_buffer(1024)
+            lib.wgm_serve_diag(self._h, buf, 1024)
+            check(rc, "wgm_serve_run (" + buf.value.decode() + ")")
         return {k: getattr(st, k) for k, _ in WgmServeStats._fields_}
 
     def requests(self) -> dict:

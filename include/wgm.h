@@ -238,6 +238,7 @@ int wgm_batch_configure(wgm_batch *b, int threads_per_cta, int ctas_per_sm, int 
 /* Team sizing: a job of E edges runs on ceil(E / team_edges) CTAs, at most
  * max_team.  0 selects the defaults: total edges / grid, a quarter of the grid. */
 int wgm_batch_configure_teams(wgm_batch *b, int64_t team_edges, int max_team);
+int wgm_batch_team_info(wgm_batch *b, int64_t *team_edges, int *max_team);
 /* Queue one batched launch on the runtime's stream (use_cuda_graph: replay a
  * captured CUDA graph of the queue reset and the launch). */
 int wgm_batch_launch(wgm_batch *b, int use_cuda_graph);
@@ -320,6 +321,8 @@ int wgm_serve_requests(wgm_serve *s, int64_t *count, int32_t *kind, int32_t *arg
 /* Output of request i of the last run (keep_results): BFS dist (uint32 x V),
  * reduce min (one float), matmul C (mat_n^2 floats). */
 int wgm_serve_result(wgm_serve *s, int64_t i, void *out, int64_t bytes);
+/* Where the last failed run stood (host and device counters), "" if none. */
+int wgm_serve_diag(wgm_serve *s, char *buf, size_t len);
 int wgm_serve_destroy(wgm_serve *s);
 
 /* ---- device timing on the runtime's stream (CUDA events) --------------- */

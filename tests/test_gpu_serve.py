@@ -14,7 +14,7 @@ from oracle import oracle
 
 pytestmark = pytest.mark.gpu
 
-FAST = dict(run_timeout_ns=30_000_000_000)
+FAST = dict(run_timeout_ns=10_000_000_000)
 
 
 @pytest.fixture(scope="module")
