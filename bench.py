@@ -215,7 +215,7 @@ def _reference_arm(args, ws, rank) -> int:
 
 def _barrier_sweep() -> int:
     from gpu_workgroup_managment_gb300 import Runtime
-    kinds = {0: "sense", 1: "xf", 2: "tree", 3: "count"}
+    kinds = {0: "sense", 1: "xf", 2: "tree", 3: "count", 4: "spread"}
     with Runtime() as rt:
         for threads in (128, 256, 512, 1024):
             for kind, name in kinds.items():
@@ -258,7 +258,7 @@ def _sssp_kernel_only(args) -> int:
     return 0
 
 
-def _served(rt, rates=(1000, 5000, 20000), reps: int = 3, reserve: int = 48) -> dict:
+def _served(rt, rates=(1000, 5000, 20000), reps: int = 20, reserve: int = 96) -> dict:
     """Served form: a resident colour+BFS job on RMAT scale 22 (edge factor
     16, seed 1; BFS from the max-degree vertex), `reps` repetitions, alone and
     beside a Poisson request stream at each rate: 40% BFS queries on RMAT
@@ -272,7 +272,7 @@ def _served(rt, rates=(1000, 5000, 20000), reps: int = 3, reserve: int = 48) -> 
     qg, vecs, mats = serve_datasets(seed=7)
     out = {"persistent": "colour + Lonestar BFS, RMAT-22", "reps": reps, "reserve": reserve,
            "mix": "40% BFS (RMAT 12-16), 30% FP32 min 2^20, 30% FP32 256x256 matmul",
-           "teams": {"bfs": 8, "reduce": 4, "matmul": 4}}
+           "teams": {"bfs": "ceil(E / 65536), at most 32", "reduce": 4, "matmul": 4}}
     with PersistentApp(rt, "color", g, node_values=nv) as ca, \
             PersistentApp(rt, "lonestar_bfs", g, source=src) as ba, \
             Serve(rt, ca, ba, graphs=qg, vecs=vecs, mats=mats, arena_bytes=1 << 30) as sv:
@@ -282,7 +282,8 @@ def _served(rt, rates=(1000, 5000, 20000), reps: int = 3, reserve: int = 48) -> 
         runs = []
         for rate in rates:
             st = sv.run(rate=rate, duration_s=60.0, reps=reps, seed=11, reserve=reserve,
-                        bfs_groups=8, reduce_groups=4, matmul_groups=4, max_in_flight=512)
+                        bfs_groups=32, bfs_edges_per_group=1 << 16, reduce_groups=4,
+                        matmul_groups=4, max_in_flight=512)
             runs.append({"rate_offered": rate, "achieved_rate": st["achieved_rate"],
                          "completed": st["completed"], "p50_us": st["lat_p50_us"],
                          "p99_us": st["lat_p99_us"], "mean_us": st["lat_mean_us"],
@@ -292,8 +293,8 @@ def _served(rt, rates=(1000, 5000, 20000), reps: int = 3, reserve: int = 48) -> 
                          "waited_for_memory": st["waited_for_memory"]})
         out["runs"] = runs
         # requests alone (no persistent job) at the lowest rate, for context
-        st = sv.run(rate=rates[0], duration_s=0.5, seed=11, bfs_groups=8, reduce_groups=4,
-                    matmul_groups=4)
+        st = sv.run(rate=rates[0], duration_s=0.5, seed=11, bfs_groups=32,
+                    bfs_edges_per_group=1 << 16, reduce_groups=4, matmul_groups=4)
         out["requests_only"] = {"rate_offered": rates[0], "p50_us": st["lat_p50_us"],
                                 "p99_us": st["lat_p99_us"], "completed": st["completed"]}
     return out
@@ -383,28 +384,25 @@ def main() -> int:
         return 0
 
     # e2e through the public API: pinned host graphs up, batched launch, results down
-    keep, hgs = [], []
-    for g in gs:
-        rp, p1 = pinned_copy(g.row_ptr)
-        cl, p2 = pinned_copy(g.col)
-        wt, p3 = pinned_copy(g.weights)
-        keep += [p1, p2, p3]
-        hgs.append(G.Graph(rp, cl, wt))
+    rows, cols, wts = b.pack(gs)
+    rows, p1 = pinned_copy(rows)
+    cols, p2 = pinned_copy(cols)
+    wts, p3 = pinned_copy(wts)
     out, p4 = pinned_copy(np.empty(int(b.offsets[-1]), np.uint32))
-    keep.append(p4)
+    keep = [p1, p2, p3, p4]
     for _ in range(2):
-        b.upload(hgs)
+        b.upload_packed(rows, cols, wts)
         b.launch(True)
         b.results(out)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        b.upload(hgs)
+        b.upload_packed(rows, cols, wts)
         b.launch(True)
         b.results(out)
     e2e_s = _max_over_ranks(dist, (time.perf_counter() - t0) / args.steps)
     if not np.array_equal(out, res):
         raise SystemExit("e2e results differ")
-    h2d = sum(g.row_ptr.nbytes + g.col.nbytes + g.weights.nbytes for g in gs)
+    h2d = rows.nbytes + cols.nbytes + wts.nbytes
     d2h = out.nbytes
     for p in keep:
         lib.wgm_host_free(p)

@@ -24,7 +24,7 @@ STATUS_CODE = {v: k for k, v in STATUS.items()}
 APP_LONESTAR_BFS, APP_LONESTAR_SSSP, APP_PANNOTIA_COLOR = 1, 2, 3
 APP_PANNOTIA_MIS, APP_PANNOTIA_SSSP, APP_PAGERANK = 4, 5, 6
 DISCOVERY_TICKET, DISCOVERY_REFERENCE = 0, 1
-BARRIER_SENSE, BARRIER_XF, BARRIER_TREE, BARRIER_COUNT = 0, 1, 2, 3
+BARRIER_SENSE, BARRIER_XF, BARRIER_TREE, BARRIER_COUNT, BARRIER_SPREAD = 0, 1, 2, 3, 4
 NP_NONE, NP_MATMULT_I32, NP_REDUCE_I32, NP_MATMULT_F32, NP_REDUCE_F32 = 0, 1, 2, 3, 4
 
 
@@ -52,7 +52,7 @@ class WgmServeConfig(C.Structure):
                 ("persist_groups", C.c_int), ("reserve", C.c_int), ("bfs_groups", C.c_int),
                 ("reduce_groups", C.c_int), ("matmul_groups", C.c_int),
                 ("max_in_flight", C.c_int), ("keep_results", C.c_int),
-                ("threads_per_wg", C.c_int)]
+                ("threads_per_wg", C.c_int), ("bfs_edges_per_group", C.c_int64)]
 
 
 class WgmServeStats(C.Structure):
@@ -125,6 +125,8 @@ _PROTOS = {
     "wgm_batch_configure": (_I, [_P, _I, _I, _I]),
     "wgm_batch_configure_teams": (_I, [_P, C.c_int64, _I]),
     "wgm_batch_team_info": (_I, [_P, _P, _P]),
+    "wgm_batch_upload_packed": (_I, [_P, _P, _P, _P]),
+    "wgm_batch_graph_offsets": (_I, [_P, _P, _P]),
     "wgm_batch_job_stats": (_I, [_P, _P, _P, _P, _P]),
     "wgm_batch_reorder_by_last_run": (_I, [_P]),
     "wgm_serve_create": (_I, [_P, _P, _P, _I, _P, _I, _I, _P, _I, _I, _P, C.c_int64, _P]),

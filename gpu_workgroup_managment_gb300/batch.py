@@ -47,6 +47,32 @@ class Batch:
         self._fill(graphs)
         check(lib.wgm_batch_upload(self._h, self._descs), "wgm_batch_upload")
 
+    def graph_offsets(self) -> tuple[np.ndarray, np.ndarray]:
+        """Where each graph's rows and cols/weights sit in the packed layout."""
+        ro = np.empty(len(self.graphs), np.int64)
+        co = np.empty(len(self.graphs), np.int64)
+        check(lib.wgm_batch_graph_offsets(self._h, ro.ctypes.data, co.ctypes.data))
+        return ro, co
+
+    def pack(self, graphs: list, out: tuple | None = None) -> tuple:
+        """Concatenate graphs' rows, cols and weights in the packed layout
+        (into `out` = (rows, cols, weights) arrays when given)."""
+        ro, co = self.graph_offsets()
+        nr = int(ro[-1] + graphs[-1].num_nodes + 1)
+        ne = int(co[-1] + graphs[-1].num_edges)
+        rows, cols, wts = out if out is not None else (
+            np.empty(nr, np.int32), np.empty(max(ne, 1), np.int32), np.empty(max(ne, 1), np.uint32))
+        for g, r0, c0 in zip(graphs, ro, co):
+            rows[r0:r0 + g.num_nodes + 1] = g.row_ptr
+            cols[c0:c0 + g.num_edges] = g.col
+            if g.weights is not None:
+                wts[c0:c0 + g.num_edges] = g.weights
+        return rows, cols, wts
+
+    def upload_packed(self, rows: np.ndarray, cols: np.ndarray, wts: np.ndarray) -> None:
+        check(lib.wgm_batch_upload_packed(self._h, rows.ctypes.data, cols.ctypes.data,
+                                          wts.ctypes.data), "wgm_batch_upload_packed")
+
     def configure(self, threads: int = 256, ctas_per_sm: int = 0, piece: int = 0) -> None:
         check(lib.wgm_batch_configure(self._h, threads, ctas_per_sm, piece), "batch_configure")
 

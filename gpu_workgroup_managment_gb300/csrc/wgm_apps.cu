@@ -126,7 +126,7 @@ static void wgm_app_free_buffers(wgm_app *a) {
                   a->d_wl_start, a->d_wl_cnt,   a->d_wl_u,
                   a->d_cnt,       a->d_stamp,   a->d_stop,       a->d_hub_acc,
                   a->d_status,  a->d_contrib,   a->d_dang,    a->d_hub_sum,    a->d_rounds,
-                  a->hubs.ids,  a->hubs.prefix, a->hubs.wmap};
+                  a->hubs.ids,  a->hubs.prefix, a->hubs.wmap, a->d_trow, a->d_tcol};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   a->hubs = wgm_dev_hubs();
@@ -178,6 +178,40 @@ static int wgm_upload_hubs(wgm_app *a, const wgm_graph_desc *g) {
   return WGM_OK;
 }
 
+/* Colour releases in-neighbours, so it needs the in-edge CSR.  Built by a
+ * counting sort over sources in increasing order; for a symmetric graph
+ * whose rows are sorted this is the graph itself, and the device arrays are
+ * shared instead of copied. */
+static int wgm_upload_transpose(wgm_app *a, const wgm_graph_desc *g) {
+  const int V = g->num_nodes;
+  const int64_t E = g->row_ptr[V];
+  std::vector<int> trow(V + 1, 0), tcol(std::max<int64_t>(E, 1));
+  for (int64_t e = 0; e < E; e++) trow[g->col[e] + 1]++;
+  for (int v = 0; v < V; v++) trow[v + 1] += trow[v];
+  {
+    std::vector<int> fill(trow.begin(), trow.end() - 1);
+    for (int v = 0; v < V; v++)
+      for (int64_t e = g->row_ptr[v]; e < g->row_ptr[v + 1]; e++) tcol[fill[g->col[e]]++] = v;
+  }
+  bool same = std::equal(trow.begin(), trow.end(), g->row_ptr) &&
+              std::equal(tcol.begin(), tcol.begin() + E, g->col);
+  if (a->d_trow) cudaFree(a->d_trow);
+  if (a->d_tcol) cudaFree(a->d_tcol);
+  a->d_trow = a->d_tcol = nullptr;
+  if (same) return WGM_OK;
+  cudaError_t e = wgm_dmalloc(&a->d_trow, (size_t)V + 1);
+  if (e == cudaSuccess) e = wgm_dmalloc(&a->d_tcol, (size_t)std::max<int64_t>(E, 1));
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(a->d_trow, trow.data(), (size_t)(V + 1) * 4, cudaMemcpyHostToDevice,
+                        a->rt->stream);
+  if (e == cudaSuccess && E)
+    e = cudaMemcpyAsync(a->d_tcol, tcol.data(), (size_t)E * 4, cudaMemcpyHostToDevice,
+                        a->rt->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(a->rt->stream);
+  if (e != cudaSuccess) return wgm_cuda_fail(a->rt, e);
+  return WGM_OK;
+}
+
 extern "C" int wgm_app_upload(wgm_app *a, const wgm_graph_desc *g) {
   if (!a) return WGM_ERR_INVALID;
   int s = wgm_validate_graph(a->kind, g);
@@ -194,6 +228,10 @@ extern "C" int wgm_app_upload(wgm_app *a, const wgm_graph_desc *g) {
   if (e != cudaSuccess) return wgm_cuda_fail(a->rt, e);
   if (wgm_uses_static_hubs(a->kind)) {
     s = wgm_upload_hubs(a, g);
+    if (s) return s;
+  }
+  if (a->kind == WGM_APP_PANNOTIA_COLOR) {
+    s = wgm_upload_transpose(a, g);
     if (s) return s;
   }
   if (a->kind == WGM_APP_PAGERANK) {
@@ -249,6 +287,18 @@ extern "C" int wgm_app_create(wgm_runtime *rt, int kind, const wgm_graph_desc *g
       if (e == cudaSuccess) e = cudaMalloc(&a->d_out, a->out_bytes);
       if (e == cudaSuccess) e = wgm_dmalloc(&a->d_node_value, V);
       if (e == cudaSuccess) e = wgm_dmalloc(&a->d_stop, 3 * WGM_LINE);
+      if (e == cudaSuccess && kind == WGM_APP_PANNOTIA_COLOR) {
+        /* frontier pieces of in-edges; every vertex is coloured once, so a
+         * round never holds more than V + E/piece pieces */
+        int64_t avg = (int64_t)((E + V - 1) / std::max<size_t>(V, 1));
+        a->piece = (int)std::max<int64_t>(32, avg);
+        a->wl_cap = (int)(V + (E + a->piece - 1) / a->piece + 64);
+        e = wgm_dmalloc(&a->d_wl_start, 2 * (size_t)a->wl_cap);
+        if (e == cudaSuccess) e = wgm_dmalloc(&a->d_wl_cnt, 2 * (size_t)a->wl_cap);
+        if (e == cudaSuccess) e = wgm_dmalloc(&a->d_wl_u, 2 * (size_t)a->wl_cap);
+        if (e == cudaSuccess) e = wgm_dmalloc(&a->d_stamp, V); /* pending */
+        if (e == cudaSuccess) e = wgm_dmalloc(&a->d_cnt, 3 * WGM_LINE);
+      }
       if (e == cudaSuccess && kind == WGM_APP_PANNOTIA_MIS) e = wgm_dmalloc(&a->d_status, V);
       break;
     case WGM_APP_PANNOTIA_SSSP:
@@ -367,6 +417,15 @@ int wgm_app_fill_mega(wgm_app *a, wgm_mega_args *A) {
       x.hubs = wgm_hubs_view(a);
       x.hub_threshold = a->hub_threshold;
       x.rounds_out = a->d_rounds;
+      x.trow = a->d_trow ? a->d_trow : a->d_row;
+      x.tcol = a->d_tcol ? a->d_tcol : a->d_col;
+      x.pending = a->d_stamp;
+      x.wl_start = a->d_wl_start;
+      x.wl_cnt = a->d_wl_cnt;
+      x.wl_u = a->d_wl_u;
+      x.cap = a->wl_cap;
+      x.piece = a->piece;
+      x.cnt = a->d_cnt;
       return WGM_OK;
     }
     case WGM_APP_PANNOTIA_MIS: {

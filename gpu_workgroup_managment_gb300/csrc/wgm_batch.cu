@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <map>
 #include <cstring>
 #include <new>
 #include <numeric>
@@ -166,7 +167,13 @@ extern "C" int wgm_batch_create(wgm_runtime *rt, int num_graphs, const wgm_graph
     return b->gV[job_graph[x]] > b->gV[job_graph[y]];
   });
   b->queue_of.assign(num_jobs, 0);
+  /* distances in the caller's job order, so one copy returns them all */
+  std::vector<long long> dist_at(num_jobs);
   long long dist_off = 0, stamp_off = 0;
+  for (int k = 0; k < num_jobs; k++) {
+    dist_at[k] = dist_off;
+    dist_off += b->gV[job_graph[k]];
+  }
   for (int q = 0; q < num_jobs; q++) {
     int k = order[q], g = job_graph[k];
     wgm_batch_job j;
@@ -178,8 +185,8 @@ extern "C" int wgm_batch_create(wgm_runtime *rt, int num_graphs, const wgm_graph
     j.col_off = b->g_col_off[g];
     j.graph = g;
     j.team = 1;
-    j.dist_off = dist_off;
-    dist_off += j.V;
+    j.boost = 1;
+    j.dist_off = dist_at[k];
     if (j.algo == 1) {
       j.stamp_off = stamp_off;
       stamp_off += j.V;
@@ -246,6 +253,34 @@ extern "C" int wgm_batch_upload(wgm_batch *b, const wgm_graph_desc *graphs) {
   return WGM_OK;
 }
 
+/* All graphs at once from host arrays laid out like the device arena (rows of
+ * graph g at row_offset(g), cols and weights at col_offset(g)): three copies
+ * instead of three per graph. */
+extern "C" int wgm_batch_upload_packed(wgm_batch *b, const int32_t *rows, const int32_t *cols,
+                                       const uint32_t *weights) {
+  if (!b || !rows || (b->cols_total && !cols)) return WGM_ERR_INVALID;
+  cudaSetDevice(b->rt->device);
+  cudaStream_t s = b->rt->stream;
+  cudaError_t e = cudaMemcpyAsync(b->d_rows, rows, (size_t)b->rows_total * 4,
+                                  cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess && b->cols_total)
+    e = cudaMemcpyAsync(b->d_cols, cols, (size_t)b->cols_total * 4, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess && b->cols_total && weights && b->has_weights)
+    e = cudaMemcpyAsync(b->d_wts, weights, (size_t)b->cols_total * 4, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return wgm_cuda_fail(b->rt, e);
+  return WGM_OK;
+}
+
+/* Where graph g sits in the packed layout. */
+extern "C" int wgm_batch_graph_offsets(wgm_batch *b, int64_t *row_off, int64_t *col_off) {
+  if (!b) return WGM_ERR_INVALID;
+  for (int g = 0; g < b->ngraphs; g++) {
+    if (row_off) row_off[g] = b->g_row_off[g];
+    if (col_off) col_off[g] = b->g_col_off[g];
+  }
+  return WGM_OK;
+}
+
 static wgm_batch_args wgm_batch_kargs(wgm_batch *b) {
   wgm_batch_args B;
   B.jobs = b->d_jobs;
@@ -288,7 +323,7 @@ static int wgm_batch_teams(wgm_batch *b, int grid) {
   std::vector<int2> slots;
   for (int q = 0; q < b->njobs; q++) {
     wgm_batch_job &j = b->jobs[q];
-    long long g = (b->gE[j.graph] + te - 1) / te;
+    long long g = (b->gE[j.graph] + te - 1) / te * std::max(j.boost, 1);
     j.team = (int)std::max(1LL, std::min<long long>(g, mt));
     for (int r = 0; r < j.team; r++) slots.push_back(make_int2(q, r));
   }
@@ -485,15 +520,10 @@ extern "C" int wgm_batch_read_all(wgm_batch *b, uint32_t *out, int64_t n) {
   if (!b || !out || n < b->dist_total) return WGM_ERR_INVALID;
   cudaSetDevice(b->rt->device);
   cudaStream_t s = b->rt->stream;
-  int64_t pos = 0;
-  for (int k = 0; k < b->njobs; k++) {
-    const wgm_batch_job &j = b->jobs[b->queue_of[k]];
-    cudaError_t e = cudaMemcpyAsync(out + pos, b->d_dist + j.dist_off, (size_t)j.V * 4,
-                                    cudaMemcpyDeviceToHost, s);
-    if (e != cudaSuccess) return wgm_cuda_fail(b->rt, e);
-    pos += j.V;
-  }
-  cudaError_t e = cudaStreamSynchronize(s);
+  /* the distance arena is laid out in the caller's job order: one copy */
+  cudaError_t e = cudaMemcpyAsync(out, b->d_dist, (size_t)b->dist_total * 4,
+                                  cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return wgm_cuda_fail(b->rt, e);
   return wgm_batch_check(b);
 }
@@ -535,10 +565,42 @@ extern "C" int wgm_batch_autotune(wgm_batch *b, int reps, int *best_threads,
   if (!b || reps < 1) return WGM_ERR_INVALID;
   const int threads_set[3] = {128, 256, 512};
   const int piece_set[3] = {16, 32, 64};
-  const long long saved_te = b->team_edges;
+  const double factors[6] = {1.0 / 32, 1.0 / 16, 0.125, 0.25, 0.5, 1.0};
   const int saved_mt = b->max_team;
+  long long etot = 0;
+  for (auto &j : b->jobs) etot += b->gE[j.graph];
+  /* one point: configure, run once, queue ordered from that run, time */
+  auto point = [&](int t, int c, int p, long long te, double *ms) {
+    int s = wgm_batch_configure(b, t, c, p);
+    if (!s) s = wgm_batch_configure_teams(b, te, saved_mt);
+    double x = 0;
+    if (!s) s = wgm_batch_run(b, 1, &x);
+    if (!s) s = wgm_batch_reorder_by_last_run(b);
+    if (!s) s = wgm_batch_time(b, reps, ms);
+    return s;
+  };
+  auto grid_of = [&](int t, int c) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wgm_k_batch, t, 0);
+    if (c > 0) per_sm = std::min(per_sm, c);
+    return std::max(1, per_sm * b->rt->prop.multiProcessorCount);
+  };
   double best = 1e300;
-  int bt = b->threads, bc = b->ctas_per_sm, bp = b->piece;
+  int bt = 256, bc = 0, bp = 0;
+  long long bte = 0;
+  /* 1. team size at the default shape */
+  for (double f : factors) {
+    long long te = std::max(1LL << 12, (long long)(etot / grid_of(bt, bc) * f));
+    double ms = 0;
+    int s = point(bt, bc, bp, te, &ms);
+    if (s) return s;
+    if (ms < best) {
+      best = ms;
+      bte = te;
+    }
+  }
+  /* 2. shape at that team size (team_edges scaled with the grid) */
+  const double per_cta = (double)bte * grid_of(256, 0);
   for (int t : threads_set) {
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wgm_k_batch, t, 0) !=
@@ -550,47 +612,75 @@ extern "C" int wgm_batch_autotune(wgm_batch *b, int reps, int *best_threads,
     ctas.push_back(per_sm);
     for (int c : ctas) {
       for (int p : piece_set) {
-        int s = wgm_batch_configure(b, t, c, p);
-        double mn = 0;
-        if (!s) s = wgm_batch_time(b, reps, &mn);
+        long long te = std::max(1LL << 12, (long long)(per_cta / grid_of(t, c)));
+        double ms = 0;
+        int s = point(t, c, p, te, &ms);
         if (s) return s;
-        if (mn < best) {
-          best = mn;
+        if (ms < best) {
+          best = ms;
           bt = t;
           bc = c;
           bp = p;
+          bte = te;
         }
       }
     }
   }
-  int s = wgm_batch_configure(b, bt, bc, bp);
-  if (s) return s;
-  /* team sizes at the winning shape */
-  int grid = 0;
-  s = wgm_batch_grid(b, &grid);
-  if (s) return s;
-  long long etot = 0;
-  for (auto &j : b->jobs) etot += b->gE[j.graph];
-  const long long base = std::max(1LL, etot / std::max(grid, 1));
-  long long bte = saved_te;
-  const double factors[6] = {1.0 / 32, 1.0 / 16, 0.125, 0.25, 0.5, 1.0};
-  for (double f : factors) {
+  /* 3. team size again at the winning shape */
+  const long long base = bte;
+  for (double f : {0.5, 0.75, 1.5, 2.0}) {
     long long te = std::max(1LL << 12, (long long)(base * f));
-    s = wgm_batch_configure_teams(b, te, saved_mt);
-    double mn = 0, ms = 0;
-    /* one run at these team sizes, then the queue ordered by its job times */
-    if (!s) s = wgm_batch_run(b, 1, &ms);
-    if (!s) s = wgm_batch_reorder_by_last_run(b);
-    if (!s) s = wgm_batch_time(b, reps, &mn);
+    double ms = 0;
+    int s = point(bt, bc, bp, te, &ms);
     if (s) return s;
-    if (mn < best) {
-      best = mn;
+    if (ms < best) {
+      best = ms;
       bte = te;
     }
   }
-  s = wgm_batch_configure_teams(b, bte, saved_mt);
+  /* 4. critical path: the jobs that run longest double their team, while
+   * that shortens the launch */
+  int s = point(bt, bc, bp, bte, &best);
+  if (s) return s;
+  for (int it = 0; it < 6; it++) {
+    std::vector<unsigned long long> t(2 * (size_t)b->njobs);
+    if (cudaMemcpy(t.data(), b->d_times, t.size() * 8, cudaMemcpyDeviceToHost) != cudaSuccess)
+      break;
+    unsigned long long t0 = ~0ull, t1 = 0;
+    for (int q = 0; q < b->njobs; q++) {
+      t0 = std::min(t0, t[2 * q]);
+      t1 = std::max(t1, t[2 * q + 1]);
+    }
+    const double span = (double)(t1 - t0);
+    std::map<long long, int> saved; /* job (by its distance offset) -> boost */
+    int boosted = 0;
+    for (int q = 0; q < b->njobs; q++) {
+      saved[b->jobs[q].dist_off] = b->jobs[q].boost;
+      if ((double)(t[2 * q + 1] - t[2 * q]) > 0.6 * span && b->jobs[q].team < grid_of(bt, bc) / 4) {
+        b->jobs[q].boost *= 2;
+        boosted++;
+      }
+    }
+    if (!boosted) break;
+    b->teams_grid = 0;
+    wgm_batch_free_graph(b);
+    double x = 0, ms = 0;
+    s = wgm_batch_run(b, 1, &x);
+    if (!s) s = wgm_batch_reorder_by_last_run(b);
+    if (!s) s = wgm_batch_time(b, reps, &ms);
+    if (s) return s;
+    if (ms < best) {
+      best = ms;
+      continue;
+    }
+    /* no gain: undo (the queue was re-ordered, so match jobs by offset) */
+    for (int q = 0; q < b->njobs; q++) b->jobs[q].boost = saved[b->jobs[q].dist_off];
+    b->teams_grid = 0;
+    wgm_batch_free_graph(b);
+    break;
+  }
   double ms = 0;
-  if (!s) s = wgm_batch_run(b, 1, &ms);
+  s = wgm_batch_run(b, 1, &ms);
   if (!s) s = wgm_batch_reorder_by_last_run(b);
   if (best_threads) *best_threads = bt;
   if (best_ctas_per_sm) *best_ctas_per_sm = bc;

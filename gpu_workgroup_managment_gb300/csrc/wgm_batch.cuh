@@ -41,7 +41,7 @@ struct wgm_batch_job {
   int cap;
   int graph; /* graph index (host bookkeeping) */
   int team;  /* CTAs working on the job */
-  int pad;
+  int boost; /* host: team multiplier from the critical-path pass */
 };
 
 /* Control block, cleared before every launch: line 0 = queue head, then per
@@ -134,10 +134,13 @@ __device__ void wgm_cta_lonestar(const wgm_batch_args &B, const wgm_batch_job &j
     o.o_cnt = wl_cnt + oo;
     o.o_u = wl_u ? wl_u + oo : nullptr;
     o.cap = cap;
-    for (int b = warp * 32; b < n; b += nw * 32) {
+    /* pieces per warp: 32, or fewer when the list is short, so a small
+     * frontier spreads over every warp instead of queueing on a few */
+    const int per = max(1, min(32, (n + nw - 1) / nw));
+    for (int b = warp * per; b < n; b += nw * per) {
       int i = b + lane, deg = 0, start = 0;
       unsigned dv = 0;
-      if (i < n) {
+      if (lane < per && i < n) {
         start = wl_start[io + i];
         deg = wl_cnt[io + i];
         if (SSSP) dv = __ldcg(&dist[wl_u[io + i]]);
@@ -232,10 +235,13 @@ __device__ int wgm_team_ls_run(const wgm_ls_job &J, wgm_warp_smem *sm, int *err,
     o.o_cnt = J.wl_cnt + oo;
     o.o_u = J.wl_u ? J.wl_u + oo : nullptr;
     o.cap = cap;
-    for (int b = gw * 32; b < n; b += NW * 32) {
+    /* pieces per warp: 32, or fewer when the list is short, so a small
+     * frontier spreads over every warp instead of queueing on a few */
+    const int per = max(1, min(32, (n + NW - 1) / NW));
+    for (int b = gw * per; b < n; b += NW * per) {
       int i = b + lane, deg = 0, start = 0;
       unsigned dv = 0;
-      if (i < n) {
+      if (lane < per && i < n) {
         start = __ldcg(&J.wl_start[io + i]);
         deg = __ldcg(&J.wl_cnt[io + i]);
         if (SSSP) dv = __ldcg(&J.dist[__ldcg(&J.wl_u[io + i])]);

@@ -69,6 +69,7 @@
 #define WGM_BARRIER_XF 1    /* master/slave flags (iw_barrier.cl:63-109) */
 #define WGM_BARRIER_TREE 2  /* two-level counter tree, then generation word */
 #define WGM_BARRIER_COUNT 3 /* monotonic arrival counter, waiters poll it */
+#define WGM_BARRIER_SPREAD 4 /* counter + generation copied on 16 lines */
 
 #define WGM_POLL_CLOSED 0x40000000
 
@@ -130,6 +131,9 @@ typedef struct wgm_dev_state {
   /* Counting barrier: arrivals of launch generation g on line g&1; the
    * discovery closer of launch g zeroes line (g+1)&1 for the next launch. */
   int32_t bar_arrivals[2 * WGM_LINE];
+  /* Spread barrier: the generation word copied on 16 lines, CTA i polls
+   * line i % 16. */
+  int32_t bar_gen_spread[16 * WGM_LINE];
 
   /* Kernel contexts (kernel_ctx.h:6-11): [0] non-persistent, [1] persistent. */
   int32_t k_num_groups[2][WGM_LINE];

@@ -363,6 +363,51 @@ __device__ __forceinline__ bool wgm_barrier_count(const wgm_launch &L, wgm_cta *
   return c->ok;
 }
 
+/* Spread barrier: the sense barrier's counter, but the last arriver releases
+ * the new generation on 16 lines and CTA i polls line i % 16, so no line has
+ * more than ngroups/16 pollers queued on it.  Arrival is a release-only
+ * fetch-add; only the last arriver, which must see every other CTA's writes
+ * before it releases them, pays for an acquire fence.  Waiters poll with
+ * relaxed loads and fence once. */
+__device__ __forceinline__ bool wgm_barrier_spread(const wgm_launch &L, wgm_cta *c,
+                                                   int ngroups) {
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    const int g = c->gen;
+    int last = 0;
+    if (lane == 0) {
+      int old;
+      asm volatile("atom.release.gpu.global.add.s32 %0, [%1], 1;"
+                   : "=r"(old) : "l"(&L.st->bar_count) : "memory");
+      last = old + 1 == ngroups;
+    }
+    last = __shfl_sync(0xffffffffu, last, 0);
+    if (last) {
+      if (lane == 0) {
+        wgm_fence_acqrel_gpu();
+        wgm_st_relaxed_gpu(&L.st->bar_count, 0);
+        wgm_st_release_gpu(&L.st->bar_gen, g + 1);
+      }
+      __syncwarp();
+      if (lane < 16) wgm_st_release_gpu(&L.st->bar_gen_spread[lane * WGM_LINE], g + 1);
+    } else if (lane == 0) {
+      const int *line = &L.st->bar_gen_spread[(c->id & 15) * WGM_LINE];
+      wgm_spin s = wgm_spin_start(L);
+      while ((int)((unsigned)wgm_ld_relaxed_gpu(line) - (unsigned)(g + 1)) < 0) {
+        if (wgm_spin_giveup(L, s, WGM_SITE_BARRIER)) {
+          c->ok = 0;
+          break;
+        }
+      }
+      wgm_fence_acqrel_gpu();
+    }
+    if (lane == 0) c->gen = g + 1;
+  }
+  __syncthreads();
+  return c->ok;
+}
+
 /* Two-level barrier: groups arrive on a per-leaf counter (tree_fanin groups
  * per leaf, each leaf on its own line); the last of a leaf arrives at the
  * root; the last at the root releases the generation every CTA polls. */
@@ -451,6 +496,8 @@ __device__ __forceinline__ bool wgm_barrier(const wgm_launch &L, wgm_cta *c) {
       return wgm_barrier_tree(L, c, c->ngroups);
     case WGM_BARRIER_COUNT:
       return wgm_barrier_count(L, c, c->ngroups);
+    case WGM_BARRIER_SPREAD:
+      return wgm_barrier_spread(L, c, c->ngroups);
     default:
       return wgm_barrier_sense(L, c, c->ngroups);
   }

@@ -359,10 +359,13 @@ __device__ __forceinline__ bool wgm_ls_level(const wgm_launch &Lc, wgm_cta *c,
   o.o_u = a.wl_u ? a.wl_u + out_off : nullptr;
   o.cap = a.cap;
   bool ok = true;
-  for (int b = gw * 32; b < n; b += NW * 32) {
+  /* pieces per warp: 32, or fewer when the list is short, so a small
+   * frontier spreads over every warp instead of queueing on a few */
+  const int per = max(1, min(32, (n + NW - 1) / NW));
+  for (int b = gw * per; b < n; b += NW * per) {
     int i = b + lane, deg = 0, start = 0;
     unsigned dv = 0;
-    if (i < n) {
+    if (lane < per && i < n) {
       start = __ldcg(&i_start[i]);
       deg = __ldcg(&i_cnt[i]);
       if (SSSP) dv = __ldcg(&a.dist[__ldcg(&i_u[i])]);
@@ -485,121 +488,278 @@ struct wgm_color_args {
   int V;
   const int *row; /* [V+1] */
   const int *col;
+  const int *trow; /* in-edges (the transpose; the graph itself when symmetric) */
+  const int *tcol;
   const float *node_value;
   int *color;    /* [V] output: 1-based colours */
-  int *stop;     /* [3 lines] */
-  int *hub_acc;  /* [H] running max (float bits) */
-  wgm_hubs hubs;
+  int *stop;     /* unused (kept for the argument layout of older callers) */
+  int *hub_acc;  /* unused */
+  wgm_hubs hubs; /* static layout of out-degree > hub_threshold vertices */
   int hub_threshold;
   int *rounds_out;
+  int *pending;  /* [V] larger out-neighbours not yet coloured */
+  int *wl_start, *wl_cnt, *wl_u; /* [2][cap] frontier pieces of in-edges */
+  int cap, piece;
+  int *cnt;      /* [3 lines] frontier sizes by round mod 3 */
 };
 
-/* "Uncoloured at the start of round r": colours are written as the round
- * number, so a vertex coloured earlier in the same round still counts as
- * uncoloured for its neighbours - exactly the reference's view, where colours
- * only change in the color2 phase after the barrier (color.cl:66-83). */
-__device__ __forceinline__ bool wgm_uncoloured_at(int cval, int r) {
-  return cval == -1 || cval == r;
+/* Pannotia colour (color.cl:3-97) computed as the frontier recurrence it
+ * implies.  In the reference a vertex v takes colour r in the first round r
+ * in which no out-neighbour with a larger value is uncoloured at the start
+ * of r (color.cl:66-83; a vertex coloured in round r still counts as
+ * uncoloured during r).  Hence colour(v) = 1 + max colour of its larger
+ * out-neighbours (1 if none), degree-1 vertices take colour 1 because they
+ * skip their neighbours (color.cl:46), and the reference's round count is
+ * the largest colour (its exit test, color.cl:85-87, first fails in the
+ * round after the last vertex is coloured).  So: count each vertex's larger
+ * out-neighbours once (`pending`), colour the vertices with none in round 1,
+ * and in round r let every vertex coloured r decrement its smaller
+ * in-neighbours; one that reaches zero takes colour r+1.  Same colours and
+ * round count as the reference, each edge looked at twice in all instead of
+ * once per round.
+ * Phases: (0) init; (3,0) count larger out-neighbours; (4,0) round-1
+ * frontier; (1,r) the vertices coloured r release their in-neighbours. */
+template <class Rel>
+__device__ __forceinline__ bool wgm_frontier_chunk(const int *trow, const int *tcol, int P,
+                                                   int start, int deg, unsigned sv,
+                                                   const wgm_ls_out &o, Rel &&rel) {
+  constexpr int K = WGM_LS_K;
+  const int lane = wgm_lane();
+  const int incl = wgm_warp_incl_scan(deg);
+  const int total = __shfl_sync(WGM_FULL, incl, 31);
+  const int off = incl - deg;
+  const int base = start - off;
+  bool ok = true;
+  for (int w = 0; w < total; w += 32 * K) {
+    int u[K], rs[K], d[K], np[K];
+    unsigned src[K];
+    bool f[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      const int s = w + 32 * k + lane;
+      f[k] = s < total;
+      const int own = wgm_owner_of(off, min(s, total - 1));
+      const int e = __shfl_sync(WGM_FULL, base, own) + s;
+      src[k] = __shfl_sync(WGM_FULL, sv, own);
+      u[k] = f[k] ? __ldg(&tcol[e]) : -1;
+    }
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      rs[k] = 0;
+      d[k] = 0;
+      if (f[k]) {
+        f[k] = rel(u[k], src[k]);
+        if (f[k]) {
+          rs[k] = __ldg(&trow[u[k]]);
+          d[k] = __ldg(&trow[u[k] + 1]);
+        }
+      }
+    }
+    int mine = 0;
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      d[k] = f[k] ? max(d[k] - rs[k], 0) : 0;
+      np[k] = (d[k] + P - 1) / P;
+      mine += np[k];
+    }
+    const int pincl = wgm_warp_incl_scan(mine);
+    const int ptotal = __shfl_sync(WGM_FULL, pincl, 31);
+    if (ptotal == 0) continue;
+    int pbase = 0;
+    if (lane == 31) pbase = atomicAdd(o.counter, ptotal);
+    pbase = __shfl_sync(WGM_FULL, pbase, 31);
+    if (pbase + ptotal > o.cap) {
+      ok = false;
+      continue;
+    }
+    int slot = pbase + pincl - mine;
+    int sl[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      sl[k] = slot;
+      if (np[k] <= WGM_LS_LANE_PIECES) {
+        for (int q = 0; q < np[k]; q++) {
+          o.o_start[slot + q] = rs[k] + q * P;
+          o.o_cnt[slot + q] = min(P, d[k] - q * P);
+          o.o_u[slot + q] = u[k];
+        }
+      }
+      slot += np[k];
+    }
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      unsigned big = __ballot_sync(WGM_FULL, np[k] > WGM_LS_LANE_PIECES);
+      while (big) {
+        const int j = __ffs(big) - 1;
+        big &= big - 1;
+        const int bs = __shfl_sync(WGM_FULL, rs[k], j), bd = __shfl_sync(WGM_FULL, d[k], j);
+        const int bu = __shfl_sync(WGM_FULL, u[k], j), bsl = __shfl_sync(WGM_FULL, sl[k], j);
+        const int bn = (bd + P - 1) / P;
+        for (int q = lane; q < bn; q += 32) {
+          o.o_start[bsl + q] = bs + q * P;
+          o.o_cnt[bsl + q] = min(P, bd - q * P);
+          o.o_u[bsl + q] = bu;
+        }
+      }
+    }
+  }
+  return ok;
 }
 
-/* Phases: (0) init; (1,r) round r for every non-hub vertex - colour1 and
- * colour2 fused: max over the neighbours uncoloured at round start (skipping
- * all neighbours of degree-1 vertices, color.cl:46), colour r if the vertex's
- * value is larger (color.cl:78-81) - while hub maxima accumulate over the
- * grid; (2,r) hub decisions.  One barrier per round when there are no hubs,
- * two otherwise (the reference uses two every round).  Phase (1,r) first
- * applies the reference's exit test to round r-1 (color.cl:85-87). */
+/* Queue the in-edge pieces of the lanes' flagged vertices (one vertex per
+ * lane, the whole warp writes). */
+__device__ __forceinline__ bool wgm_frontier_push(const int *trow, int P, bool flag, int v,
+                                                  const wgm_ls_out &o, int *tab) {
+  int start = 0, deg = 0, np = 0;
+  if (flag) {
+    start = __ldg(&trow[v]);
+    deg = max(__ldg(&trow[v + 1]) - start, 0);
+    np = (deg + P - 1) / P;
+  }
+  int incl = wgm_warp_incl_scan(np);
+  int total = __shfl_sync(WGM_FULL, incl, 31);
+  if (total == 0) return true;
+  int base = 0;
+  if (wgm_lane() == 0) base = atomicAdd(o.counter, total);
+  base = __shfl_sync(WGM_FULL, base, 0);
+  if (base + total > o.cap) return false;
+  int off = incl - np;
+  wgm_for_each_edge(off, np, -off, total, 0, 32, tab, [&](bool valid, int k, int owner) {
+    int s = __shfl_sync(WGM_FULL, start, owner);
+    int d = __shfl_sync(WGM_FULL, deg, owner);
+    int x = __shfl_sync(WGM_FULL, v, owner);
+    int oo = __shfl_sync(WGM_FULL, off, owner);
+    if (valid) {
+      int slot = base + oo + k;
+      o.o_start[slot] = s + k * P;
+      o.o_cnt[slot] = min(P, d - k * P);
+      o.o_u[slot] = x;
+    }
+  });
+  return true;
+}
+
 static __device__ int wgm_phase_color(const wgm_launch &Lc, wgm_cta *c, const wgm_color_args &a,
                                       wgm_warp_smem *sm, wgm_step cur, wgm_step *nxt) {
   const wgm_split s(c);
   const int V = a.V;
-  const int NEG1 = __float_as_int(-1.0f);
+  const int lane = s.lane, warp = s.warp;
   if (cur.target == 0) {
-    for (int i = s.tid; i < V; i += s.nth) a.color[i] = -1; /* color.h:50 */
-    for (int h = s.tid; h < a.hubs.H; h += s.nth) a.hub_acc[h] = NEG1;
-    if (c->id == 0 && threadIdx.x == 0)
-      for (int k = 0; k < 3; k++) a.stop[k * WGM_LINE] = 0;
+    for (int i = s.tid; i < V; i += s.nth) {
+      a.color[i] = -1; /* color.h:50 */
+      a.pending[i] = 0;
+    }
+    if (c->id == 0 && threadIdx.x < 3) a.cnt[threadIdx.x * WGM_LINE] = 0;
+    *nxt = {3, 0};
+    return WGM_PHASE_NEXT;
+  }
+  if (cur.target == 3) {
+    /* larger out-neighbours of every vertex; a degree-1 vertex has none
+     * (color.cl:46) */
+    for (int b = s.gw * 32; b < V; b += s.NW * 32) {
+      const int i = b + lane;
+      int deg = 0, start = 0;
+      float vi = 0.f;
+      if (i < V) {
+        start = __ldg(&a.row[i]);
+        const int d = __ldg(&a.row[i + 1]) - start;
+        deg = (d == 1 || d > a.hub_threshold) ? 0 : d;
+        vi = __ldg(&a.node_value[i]);
+      }
+      sm->acc[warp][lane] = 0;
+      int incl = wgm_warp_incl_scan(deg);
+      int total = __shfl_sync(WGM_FULL, incl, 31);
+      int off = incl - deg;
+      __syncwarp();
+      wgm_for_each_edge(off, deg, start - off, total, 0, 32, sm->tab[warp],
+                        [&](bool valid, int e, int owner) {
+                          const float vo = __shfl_sync(WGM_FULL, vi, owner);
+                          if (valid && __ldg(&a.node_value[__ldg(&a.col[e])]) > vo)
+                            atomicAdd(&sm->acc[warp][owner], 1);
+                        });
+      __syncwarp();
+      if (i < V && deg > 0) a.pending[i] = sm->acc[warp][lane];
+    }
+    const int nwin = (a.hubs.total + 31) >> 5;
+    for (int k = s.gw; k < nwin; k += s.NW) {
+      wgm_hub_window(a.hubs, a.row, k, [&](bool valid, int h, int e) {
+        int h0 = __shfl_sync(WGM_FULL, h, 0);
+        int cntv = 0;
+        if (valid) {
+          const int v = __ldg(&a.hubs.ids[h]);
+          cntv = __ldg(&a.node_value[__ldg(&a.col[e])]) > __ldg(&a.node_value[v]) ? 1 : 0;
+        }
+        int m0, m1;
+        float f0, f1;
+        wgm_two_seg_reduce(h == h0, 0, (float)cntv, 2, &m0, &m1, &f0, &f1);
+        if (lane == 0) {
+          if (f0 > 0.f) atomicAdd(&a.pending[__ldg(&a.hubs.ids[h0])], (int)f0);
+          if (f1 > 0.f && h0 + 1 < a.hubs.H)
+            atomicAdd(&a.pending[__ldg(&a.hubs.ids[h0 + 1])], (int)f1);
+        }
+      });
+    }
+    *nxt = {4, 0};
+    return WGM_PHASE_NEXT;
+  }
+  wgm_ls_out o;
+  o.cap = a.cap;
+  if (cur.target == 4) {
+    /* round 1: every vertex without a larger out-neighbour */
+    o.counter = &a.cnt[1 * WGM_LINE];
+    o.o_start = a.wl_start + a.cap;
+    o.o_cnt = a.wl_cnt + a.cap;
+    o.o_u = a.wl_u + a.cap;
+    bool ok = true;
+    for (int b = s.gw * 32; b < V; b += s.NW * 32) {
+      const int i = b + lane;
+      const bool f = i < V && __ldcg(&a.pending[i]) == 0;
+      if (f) a.color[i] = 1;
+      ok &= wgm_frontier_push(a.trow, a.piece, f, i, o, sm->tab[warp]);
+    }
+    if (!ok) wgm_fail(Lc, WGM_DEV_OVERFLOW, WGM_SITE_QUEUE, 1);
     *nxt = {1, 1};
     return WGM_PHASE_NEXT;
   }
   const int r = cur.round;
-  if (cur.target == 2) {
-    /* Hub decisions (color.cl:77-81 for hubs), then reset the maxima. */
-    for (int h = s.tid; h < a.hubs.H; h += s.nth) {
-      int v = __ldg(&a.hubs.ids[h]);
-      if (__ldcg(&a.color[v]) == -1 &&
-          __ldg(&a.node_value[v]) > __int_as_float(__ldcg(&a.hub_acc[h])))
-        a.color[v] = r;
-      a.hub_acc[h] = NEG1;
-    }
-    *nxt = {1, r + 1};
-    return WGM_PHASE_NEXT;
-  }
-  if (r > 1 && __ldcg(&a.stop[((r - 1) % 3) * WGM_LINE]) == 0) {
+  const int n = __ldcg(&a.cnt[(r % 3) * WGM_LINE]);
+  if (n == 0) {
     if (c->id == 0 && threadIdx.x == 0 && a.rounds_out) *a.rounds_out = r - 1;
     return WGM_PHASE_DONE;
   }
-  if (r > V + 2) { /* every round colours at least one vertex of a valid input */
+  if (n > a.cap || r > V + 2) {
     wgm_fail(Lc, WGM_DEV_BAD_INPUT, WGM_SITE_QUEUE, r);
     return WGM_PHASE_DONE;
   }
-  if (c->id == 0 && threadIdx.x == 0) a.stop[((r + 1) % 3) * WGM_LINE] = 0;
-  bool any = false;
-  const int lane = s.lane, warp = s.warp;
-  for (int b = s.gw * 32; b < V; b += s.NW * 32) {
-    int i = b + lane;
-    int deg = 0, start = 0;
-    bool unc = false;
-    if (i < V) {
-      unc = __ldcg(&a.color[i]) == -1;
-      start = __ldg(&a.row[i]);
-      int d = __ldg(&a.row[i + 1]) - start;
-      if (unc && d <= a.hub_threshold) deg = (d == 1) ? 0 : d;
-      if (d > a.hub_threshold) unc = false;
+  if (c->id == 0 && threadIdx.x == 0) a.cnt[((r + 2) % 3) * WGM_LINE] = 0;
+  const size_t io = (size_t)(r & 1) * a.cap, oo = (size_t)((r + 1) & 1) * a.cap;
+  o.counter = &a.cnt[((r + 1) % 3) * WGM_LINE];
+  o.o_start = a.wl_start + oo;
+  o.o_cnt = a.wl_cnt + oo;
+  o.o_u = a.wl_u + oo;
+  const int next_colour = r + 1;
+  bool ok = true;
+  /* pieces per warp: 32, or fewer when the frontier is short */
+  const int per = max(1, min(32, (n + s.NW - 1) / s.NW));
+  for (int b = s.gw * per; b < n; b += s.NW * per) {
+    int i = b + lane, deg = 0, start = 0;
+    unsigned sv = 0;
+    if (lane < per && i < n) {
+      start = __ldcg(&a.wl_start[io + i]);
+      deg = __ldcg(&a.wl_cnt[io + i]);
+      sv = __float_as_uint(__ldg(&a.node_value[__ldcg(&a.wl_u[io + i])]));
     }
-    sm->acc[warp][lane] = NEG1;
-    int incl = wgm_warp_incl_scan(deg);
-    int total = __shfl_sync(WGM_FULL, incl, 31);
-    int off = incl - deg;
-    __syncwarp();
-    wgm_for_each_edge(off, deg, start - off, total, 0, 32, sm->tab[warp],
-                      [&](bool valid, int e, int owner) {
-                        if (valid) {
-                          int j = __ldg(&a.col[e]);
-                          if (wgm_uncoloured_at(__ldcg(&a.color[j]), r)) {
-                            any = true;
-                            atomicMax(&sm->acc[warp][owner],
-                                      __float_as_int(__ldg(&a.node_value[j])));
-                          }
-                        }
-                      });
-    __syncwarp();
-    if (unc && __ldg(&a.node_value[i]) > __int_as_float(sm->acc[warp][lane])) a.color[i] = r;
+    ok &= wgm_frontier_chunk(a.trow, a.tcol, a.piece, start, deg, sv, o,
+                             [&](int w, unsigned src) {
+                               /* w has the coloured vertex as a larger out-neighbour */
+                               if (!(__ldg(&a.node_value[w]) < __uint_as_float(src))) return false;
+                               if (atomicSub(&a.pending[w], 1) != 1) return false;
+                               a.color[w] = next_colour;
+                               return true;
+                             });
   }
-  /* Hubs still uncoloured: spread their edges over every warp. */
-  int nwin = (a.hubs.total + 31) >> 5;
-  for (int k = s.gw; k < nwin; k += s.NW) {
-    wgm_hub_window(a.hubs, a.row, k, [&](bool valid, int h, int e) {
-      int h0 = __shfl_sync(WGM_FULL, h, 0);
-      int val = INT_MIN;
-      if (valid && __ldcg(&a.color[__ldg(&a.hubs.ids[h])]) == -1) {
-        int j = __ldg(&a.col[e]);
-        if (wgm_uncoloured_at(__ldcg(&a.color[j]), r)) {
-          any = true;
-          val = __float_as_int(__ldg(&a.node_value[j]));
-        }
-      }
-      int m0, m1;
-      float f0, f1;
-      wgm_two_seg_reduce(h == h0, val, 0.f, 0, &m0, &m1, &f0, &f1);
-      if (lane == 0) {
-        if (m0 != INT_MIN) atomicMax(&a.hub_acc[h0], m0);
-        if (m1 != INT_MIN && h0 + 1 < a.hubs.H) atomicMax(&a.hub_acc[h0 + 1], m1);
-      }
-    });
-  }
-  if (__any_sync(WGM_FULL, any) && lane == 0) a.stop[(r % 3) * WGM_LINE] = 1;
-  *nxt = (a.hubs.H > 0) ? wgm_step{2, r} : wgm_step{1, r + 1};
+  if (!ok) wgm_fail(Lc, WGM_DEV_OVERFLOW, WGM_SITE_QUEUE, r);
+  *nxt = {1, r + 1};
   return WGM_PHASE_NEXT;
 }
 

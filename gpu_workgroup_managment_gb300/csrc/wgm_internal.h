@@ -55,6 +55,8 @@ struct wgm_app {
   int *d_hub_acc = nullptr, *d_status = nullptr;
   float *d_contrib = nullptr, *d_dang = nullptr, *d_hub_sum = nullptr;
   int *d_rounds = nullptr;
+  /* colour: in-edge CSR when the graph is not symmetric (else the graph) */
+  int *d_trow = nullptr, *d_tcol = nullptr;
   int source = 0;
   float damping = 0.85f;
   float dang0 = 0.f;

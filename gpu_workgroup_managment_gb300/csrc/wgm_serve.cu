@@ -176,6 +176,7 @@ struct wgm_serve {
   wgm_app *color = nullptr, *bfs = nullptr;
   /* resident datasets */
   std::vector<wgm_serve_graph> graphs;
+  std::vector<long long> gE;
   int *d_rows = nullptr, *d_cols = nullptr;
   wgm_serve_graph *d_graphs = nullptr;
   float *d_vecs = nullptr, *d_mats = nullptr;
@@ -283,6 +284,7 @@ extern "C" int wgm_serve_create(wgm_runtime *rt, wgm_app *color, wgm_app *bfs, i
     rows += d.num_nodes + 1;
     cols += d.num_edges;
     s->graphs.push_back(sg);
+    s->gE.push_back(d.num_edges);
   }
   cudaSetDevice(rt->device);
   cudaError_t e = cudaSuccess;
@@ -472,7 +474,12 @@ extern "C" int wgm_serve_run(wgm_serve *s, const wgm_serve_config *cfg, wgm_serv
     A.ls = M.ls;
   }
   A.reps = s->color ? cfg->reps : 0;
-  A.persist_groups = A.reps > 0 ? (cfg->persist_groups > 0 ? cfg->persist_groups : lpg_max) : 0;
+  /* by default the resident job starts on every group but the reserve, so
+   * the first requests need not wait for a kill */
+  A.persist_groups =
+      A.reps > 0 ? (cfg->persist_groups > 0 ? cfg->persist_groups
+                                            : std::max(1, lpg_max - std::max(0, cfg->reserve)))
+                 : 0;
   A.ring = s->ring_d;
   A.ring_size = s->ring;
   A.completions = s->comp_d;
@@ -541,6 +548,9 @@ extern "C" int wgm_serve_run(wgm_serve *s, const wgm_serve_config *cfg, wgm_serv
       lg.arg0 = a.arg0;
       lg.arg1 = a.arg1;
       lg.groups = a.kind == WGM_REQ_BFS ? tb : (a.kind == WGM_REQ_REDUCE ? tr : tm);
+      if (a.kind == WGM_REQ_BFS && cfg->bfs_edges_per_group > 0)
+        lg.groups = team((int)std::min<long long>(
+            tb, (s->gE[a.arg0] + cfg->bfs_edges_per_group - 1) / cfg->bfs_edges_per_group));
       lg.arrive_ns = a.t;
       lg.submit_ns = now;
       lg.done_ns = 0;
@@ -587,7 +597,9 @@ extern "C" int wgm_serve_run(wgm_serve *s, const wgm_serve_config *cfg, wgm_serv
         k++;
       }
     }
-    if (!stream_open && wait_head == waiting.size() && inflight.empty()) break;
+    if (!stream_open && wait_head == waiting.size() && inflight.empty() &&
+        (reps == 0 || persist_done_at))
+      break;
   }
   __atomic_store_n(&s->hs_h->quit, 1, __ATOMIC_RELEASE);
   int status = wgm_synchronize(rt);

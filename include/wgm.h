@@ -47,6 +47,7 @@ extern "C" {
 #define WGM_BARRIER_XF 1
 #define WGM_BARRIER_TREE 2
 #define WGM_BARRIER_COUNT 3 /* monotonic arrival counter, waiters poll it */
+#define WGM_BARRIER_SPREAD 4 /* counter, generation released on 16 lines */
 
 /* ---- persistent apps (the reference selects them by macro, skel.cpp:50-77) */
 #define WGM_APP_LONESTAR_BFS 1
@@ -233,6 +234,12 @@ int wgm_batch_create(wgm_runtime *rt, int num_graphs, const wgm_graph_desc *grap
                      const int32_t *job_source, wgm_batch **out);
 /* Re-upload graphs of the same shapes. */
 int wgm_batch_upload(wgm_batch *b, const wgm_graph_desc *graphs);
+/* Re-upload every graph from host arrays packed like the device arena (graph
+ * g's rows at row_off[g], its cols and weights at col_off[g], as returned by
+ * wgm_batch_graph_offsets): three copies in all. */
+int wgm_batch_upload_packed(wgm_batch *b, const int32_t *rows, const int32_t *cols,
+                            const uint32_t *weights);
+int wgm_batch_graph_offsets(wgm_batch *b, int64_t *row_off, int64_t *col_off);
 /* threads per CTA, CTAs per SM (0: occupancy maximum), piece (0: per graph). */
 int wgm_batch_configure(wgm_batch *b, int threads_per_cta, int ctas_per_sm, int piece);
 /* Team sizing: a job of E edges runs on ceil(E / team_edges) CTAs, at most
@@ -286,12 +293,15 @@ typedef struct wgm_serve_config {
   double frac_bfs;     /* request mix; the rest after frac_reduce are matmuls */
   double frac_reduce;
   int reps;            /* persistent job repetitions (0: no persistent job) */
-  int persist_groups;  /* groups the persistent job starts with (0: all) */
+  int persist_groups;  /* groups the persistent job starts with (0: all but the
+                          reserve) */
   int reserve;         /* free groups the persistent job leaves to requests */
   int bfs_groups, reduce_groups, matmul_groups; /* team sizes */
   int max_in_flight;   /* admitted and unfinished requests (<= 4000) */
   int keep_results;    /* copy every request's output to the host (tests) */
   int threads_per_wg;  /* 0: the runtime's */
+  int64_t bfs_edges_per_group; /* > 0: a BFS query gets ceil(E / this) groups, at
+                                  most bfs_groups */
 } wgm_serve_config;
 typedef struct wgm_serve_stats {
   int64_t arrived, completed, waited_for_memory;

@@ -87,6 +87,7 @@ def test_few_groups(rt, num_wgs):
 @pytest.mark.parametrize("cfg", [
     dict(barrier_kind=1), dict(barrier_kind=2), dict(barrier_kind=2, tree_fanin=3),
     dict(barrier_kind=3), dict(barrier_kind=3, threads_per_wg=128),
+    dict(barrier_kind=4), dict(barrier_kind=4, threads_per_wg=1024),
     dict(discovery_mode=1, discovery_extra_rounds=2), dict(threads_per_wg=128),
     dict(threads_per_wg=512), dict(threads_per_wg=1024), dict(hub_threshold=32),
     dict(hub_threshold=100000), dict(host_handshake=1),
@@ -217,6 +218,24 @@ def test_c2_rmat20_bfs_full_size(rt, rmat20):
         a.run()
         d = a.result()
     assert np.array_equal(d, oracle.lonestar_bfs(g, src, omp=True))
+
+
+def test_c3_rmat22_pagerank_full_size(rt):
+    """Configuration 3: FP32 pull PageRank on RMAT-22, damping 0.85, 20
+    iterations, within 1e-5 relative L-inf of the FP64 oracle; and the colour
+    of the same graph (the served form's resident job) against the oracle."""
+    g = graphs.rmat(22, 16, seed=1)
+    with PersistentApp(rt, "pagerank", g) as a:
+        a.run()
+        p = a.result()
+    p64 = oracle.pagerank_f64(g)
+    err = np.max(np.abs(p.astype(np.float64) - p64)) / np.max(np.abs(p64))
+    assert err <= PR_TOL, f"pagerank rel Linf {err}"
+    nv = graphs.seeded_node_values(g.num_nodes, 1)
+    with PersistentApp(rt, "color", g, node_values=nv) as a:
+        a.run()
+        c = a.result()
+    assert np.array_equal(c, oracle.color(g, nv, omp=True))
 
 
 def test_invalid_inputs_rejected(rt):
