@@ -28,6 +28,13 @@
 
 #include "wgm_graph.cuh"
 
+/* Whether batch jobs read dist[dst] before the atomic (one more dependent
+ * load, fewer atomics).  The batch's graphs are small and its critical path
+ * is latency: go straight to the atomic. */
+#ifndef WGM_BATCH_PRECHECK
+#define WGM_BATCH_PRECHECK false
+#endif
+
 struct wgm_batch_job {
   int V;
   int algo;   /* 0 = BFS, 1 = SSSP */
@@ -138,14 +145,14 @@ __device__ void wgm_cta_lonestar(const wgm_batch_args &B, const wgm_batch_job &j
      * frontier spreads over every warp instead of queueing on a few */
     const int per = max(1, min(32, (n + nw - 1) / nw));
     for (int b = warp * per; b < n; b += nw * per) {
-      int i = b + lane, deg = 0, start = 0;
-      unsigned dv = 0;
+      int i = b + lane, deg = 0, start = 0, src = 0;
       if (lane < per && i < n) {
         start = wl_start[io + i];
         deg = wl_cnt[io + i];
-        if (SSSP) dv = __ldcg(&dist[wl_u[io + i]]);
+        if (SSSP) src = wl_u[io + i];
       }
-      wgm_ls_chunk<SSSP>(row, col, wt, dist, stamp, V, j.piece, L, start, deg, dv, o);
+      wgm_ls_chunk<SSSP, WGM_BATCH_PRECHECK>(row, col, wt, dist, stamp, V, j.piece, L, start,
+                                             deg, src, o);
     }
     __syncthreads();
     L++;
@@ -239,14 +246,14 @@ __device__ int wgm_team_ls_run(const wgm_ls_job &J, wgm_warp_smem *sm, int *err,
      * frontier spreads over every warp instead of queueing on a few */
     const int per = max(1, min(32, (n + NW - 1) / NW));
     for (int b = gw * per; b < n; b += NW * per) {
-      int i = b + lane, deg = 0, start = 0;
-      unsigned dv = 0;
+      int i = b + lane, deg = 0, start = 0, src = 0;
       if (lane < per && i < n) {
         start = __ldcg(&J.wl_start[io + i]);
         deg = __ldcg(&J.wl_cnt[io + i]);
-        if (SSSP) dv = __ldcg(&J.dist[__ldcg(&J.wl_u[io + i])]);
+        if (SSSP) src = __ldcg(&J.wl_u[io + i]);
       }
-      wgm_ls_chunk<SSSP>(J.row, J.col, J.wt, J.dist, J.stamp, V, J.piece, L, start, deg, dv, o);
+      wgm_ls_chunk<SSSP, WGM_BATCH_PRECHECK>(J.row, J.col, J.wt, J.dist, J.stamp, V, J.piece, L,
+                                             start, deg, src, o);
     }
     if (!wgm_team_barrier(err, spin_ns, J.arr, G, &nb)) return -1;
     L++;

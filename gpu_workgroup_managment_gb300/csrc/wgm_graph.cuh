@@ -231,10 +231,10 @@ struct wgm_ls_out {
  *   one warp scan and one counter atomic for every piece of the batch.
  * The relaxation rules are stated above wgm_ls_push; the order of
  * relaxations inside a level does not change the fixpoint. */
-template <bool SSSP>
+template <bool SSSP, bool PRE = true>
 __device__ __forceinline__ bool wgm_ls_chunk(const int *row, const int *col, const unsigned *wt,
                                              unsigned *dist, int *stamp, int V, int P, int L,
-                                             int start, int deg, unsigned dv,
+                                             int start, int deg, int src,
                                              const wgm_ls_out &o) {
   constexpr int K = WGM_LS_K;
   const int lane = wgm_lane();
@@ -244,7 +244,7 @@ __device__ __forceinline__ bool wgm_ls_chunk(const int *row, const int *col, con
   const int base = start - off;
   bool ok = true;
   for (int w = 0; w < total; w += 32 * K) {
-    int e[K], u[K], rs[K], d[K], np[K];
+    int e[K], u[K], rs[K], d[K], np[K], sv[K];
     unsigned alt[K];
     bool f[K];
 #pragma unroll
@@ -253,21 +253,24 @@ __device__ __forceinline__ bool wgm_ls_chunk(const int *row, const int *col, con
       f[k] = s < total;
       const int own = wgm_owner_of(off, min(s, total - 1));
       e[k] = __shfl_sync(WGM_FULL, base, own) + s;
-      alt[k] = SSSP ? __shfl_sync(WGM_FULL, dv, own) : 0u;
+      sv[k] = SSSP ? __shfl_sync(WGM_FULL, src, own) : 0;
     }
+    /* the piece vertex's distance is read beside the edge's col and weight
+     * (the lanes of one piece read the same word), not before them */
 #pragma unroll
     for (int k = 0; k < K; k++) {
       u[k] = f[k] ? __ldg(&col[e[k]]) : -1;
       if (SSSP) {
         unsigned wk = f[k] ? __ldg(&wt[e[k]]) : WGM_LONESTAR_INF;
+        unsigned dvk = f[k] ? __ldcg(&dist[sv[k]]) : 0u;
         f[k] = f[k] && wk < WGM_LONESTAR_INF; /* sssp.cl:120 */
-        alt[k] += wk;
+        alt[k] = dvk + wk;
       }
     }
 #pragma unroll
     for (int k = 0; k < K; k++) {
       f[k] = f[k] && (unsigned)u[k] < (unsigned)V; /* bfs.cl:116 */
-      if (f[k]) {
+      if (PRE && f[k]) {
         unsigned cur = __ldcg(&dist[u[k]]);
         f[k] = SSSP ? (alt[k] < cur) : (cur == WGM_LONESTAR_INF);
       }
@@ -363,15 +366,14 @@ __device__ __forceinline__ bool wgm_ls_level(const wgm_launch &Lc, wgm_cta *c,
    * frontier spreads over every warp instead of queueing on a few */
   const int per = max(1, min(32, (n + NW - 1) / NW));
   for (int b = gw * per; b < n; b += NW * per) {
-    int i = b + lane, deg = 0, start = 0;
-    unsigned dv = 0;
+    int i = b + lane, deg = 0, start = 0, src = 0;
     if (lane < per && i < n) {
       start = __ldcg(&i_start[i]);
       deg = __ldcg(&i_cnt[i]);
-      if (SSSP) dv = __ldcg(&a.dist[__ldcg(&i_u[i])]);
+      if (SSSP) src = __ldcg(&i_u[i]);
     }
     ok &= wgm_ls_chunk<SSSP>(a.row, a.col, a.wt, a.dist, a.stamp, a.V, a.piece, L, start, deg,
-                             dv, o);
+                             src, o);
   }
   (void)sm;
   return ok;
@@ -1102,25 +1104,43 @@ static __device__ int wgm_phase_pagerank(const wgm_launch &Lc, wgm_cta *c, const
       deg = dfull > a.hub_threshold ? 0 : dfull;
     }
     acc[lane] = 0.f;
-    int incl = wgm_warp_incl_scan(deg);
-    int total = __shfl_sync(WGM_FULL, incl, 31);
-    int off = incl - deg;
+    const int incl = wgm_warp_incl_scan(deg);
+    const int total = __shfl_sync(WGM_FULL, incl, 31);
+    const int off = incl - deg;
+    const int ebase = start - off;
     __syncwarp();
-    wgm_for_each_edge(off, deg, start - off, total, 0, 32, sm->tab[warp],
-                      [&](bool valid, int e, int owner) {
-                        float v = valid ? __ldcg(&cin[__ldg(&a.col[e])]) : 0.f;
-                        /* segmented inclusive scan over lanes with equal owner */
-                        int own = valid ? owner : -1;
+    /* windows of 32 edge slots, four at a time: the col loads of the four
+     * windows, then their gathers, are in flight together; each window's
+     * contributions are then summed per owner by a segmented scan, windows
+     * in order, so a vertex's sum has a fixed order */
+    for (int w = 0; w < total; w += 128) {
+      int own[4], u[4];
+      float v[4];
 #pragma unroll
-                        for (int o = 1; o < 32; o <<= 1) {
-                          float y = __shfl_up_sync(WGM_FULL, v, o);
-                          int oy = __shfl_up_sync(WGM_FULL, own, o);
-                          if (lane >= o && oy == own) v += y;
-                        }
-                        int nx = __shfl_down_sync(WGM_FULL, own, 1);
-                        if (own >= 0 && (lane == 31 || nx != own)) acc[own] += v;
-                        __syncwarp();
-                      });
+      for (int q = 0; q < 4; q++) {
+        const int sl = w + 32 * q + lane;
+        const int o = wgm_owner_of(off, min(sl, total - 1));
+        own[q] = sl < total ? o : -1;
+        const int e = __shfl_sync(WGM_FULL, ebase, o) + sl;
+        u[q] = own[q] >= 0 ? __ldg(&a.col[e]) : 0;
+      }
+#pragma unroll
+      for (int q = 0; q < 4; q++) v[q] = own[q] >= 0 ? __ldcg(&cin[u[q]]) : 0.f;
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        float x = v[q];
+        const int ow = own[q];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          float y = __shfl_up_sync(WGM_FULL, x, o);
+          int oy = __shfl_up_sync(WGM_FULL, ow, o);
+          if (lane >= o && oy == ow) x += y;
+        }
+        int nx = __shfl_down_sync(WGM_FULL, ow, 1);
+        if (ow >= 0 && (lane == 31 || nx != ow)) acc[ow] += x;
+        __syncwarp();
+      }
+    }
     __syncwarp();
     if (i < V && dfull <= a.hub_threshold) {
       float p = base + d * acc[lane];
