@@ -320,11 +320,18 @@ __device__ __forceinline__ bool wgm_barrier_sense(const wgm_launch &L, wgm_cta *
       wgm_st_relaxed_gpu(&L.st->bar_count, 0);
       wgm_st_release_gpu(&L.st->bar_gen, g + 1);
     } else {
-      wgm_spin s = wgm_spin_start(L);
-      while (wgm_ld_acquire_gpu(&L.st->bar_gen) == g) {
-        if (wgm_spin_giveup(L, s, WGM_SITE_BARRIER)) {
-          c->ok = 0;
-          break;
+      /* the deadline clock starts only once the wait has polled a while:
+       * most barriers complete within a few polls */
+      unsigned quick = 0;
+      while (wgm_ld_acquire_gpu(&L.st->bar_gen) == g && ++quick < 64) {
+      }
+      if (quick >= 64) {
+        wgm_spin s = wgm_spin_start(L);
+        while (wgm_ld_acquire_gpu(&L.st->bar_gen) == g) {
+          if (wgm_spin_giveup(L, s, WGM_SITE_BARRIER)) {
+            c->ok = 0;
+            break;
+          }
         }
       }
     }
@@ -481,10 +488,10 @@ __device__ __forceinline__ bool wgm_barrier_xf(const wgm_launch &L, wgm_cta *c,
 }
 
 __device__ __forceinline__ bool wgm_barrier(const wgm_launch &L, wgm_cta *c) {
-  /* Every 64 barriers each CTA looks at the host abort word once, so a run
-   * the host gives up on ends within a few rounds even when no wait spins
-   * long (the other CTAs then see dev_error in their next wait). */
-  if (threadIdx.x == 0 && ((++c->tmp[0]) & 63) == 0 &&
+  /* Every 1024 barriers each CTA looks at the host abort word once (a few
+   * ms of barriers), so a run the host gives up on ends soon even when no
+   * wait spins long (the other CTAs then see dev_error in their next wait). */
+  if (threadIdx.x == 0 && ((++c->tmp[0]) & 1023) == 0 &&
       wgm_ld_relaxed_sys(&L.hf->abort_flag) != 0) {
     wgm_fail(L, WGM_DEV_ABORTED, WGM_SITE_BARRIER, c->id);
     c->ok = 0;
