@@ -52,7 +52,8 @@ class WgmServeConfig(C.Structure):
                 ("persist_groups", C.c_int), ("reserve", C.c_int), ("bfs_groups", C.c_int),
                 ("reduce_groups", C.c_int), ("matmul_groups", C.c_int),
                 ("max_in_flight", C.c_int), ("keep_results", C.c_int),
-                ("threads_per_wg", C.c_int), ("bfs_edges_per_group", C.c_int64)]
+                ("threads_per_wg", C.c_int), ("bfs_edges_per_group", C.c_int64),
+                ("frac_int", C.c_double)]
 
 
 class WgmServeStats(C.Structure):
@@ -125,6 +126,7 @@ _PROTOS = {
     "wgm_batch_configure": (_I, [_P, _I, _I, _I]),
     "wgm_batch_configure_teams": (_I, [_P, C.c_int64, _I]),
     "wgm_batch_team_info": (_I, [_P, _P, _P]),
+    "wgm_batch_configure_local": (_I, [_P, _I]),
     "wgm_batch_upload_packed": (_I, [_P, _P, _P, _P]),
     "wgm_batch_graph_offsets": (_I, [_P, _P, _P]),
     "wgm_batch_job_stats": (_I, [_P, _P, _P, _P, _P]),
@@ -134,6 +136,7 @@ _PROTOS = {
     "wgm_serve_requests": (_I, [_P, _P, _P, _P, _P, _P, _P]),
     "wgm_serve_result": (_I, [_P, C.c_int64, _P, C.c_int64]),
     "wgm_serve_destroy": (_I, [_P]),
+    "wgm_serve_set_int_data": (_I, [_P, _I, _I, _P, _I, _I, _P]),
     "wgm_serve_diag": (_I, [_P, C.c_char_p, C.c_size_t]),
     "wgm_batch_launch": (_I, [_P, _I]),
     "wgm_batch_run": (_I, [_P, _I, C.POINTER(C.c_double)]),

@@ -81,6 +81,10 @@ class Batch:
         (0 = defaults: total edges / grid, a quarter of the grid)."""
         check(lib.wgm_batch_configure_teams(self._h, team_edges, max_team), "configure_teams")
 
+    def configure_local(self, rounds: int) -> None:
+        """Warp-local continuation rounds per level (0 = plain levels)."""
+        check(lib.wgm_batch_configure_local(self._h, rounds), "configure_local")
+
     def launch(self, use_cuda_graph: bool = True) -> None:
         check(lib.wgm_batch_launch(self._h, int(use_cuda_graph)), "wgm_batch_launch")
 

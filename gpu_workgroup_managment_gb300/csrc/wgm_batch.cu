@@ -20,6 +20,8 @@
 
 __global__ void __launch_bounds__(1024) wgm_k_batch(wgm_batch_args B) {
   __shared__ wgm_warp_smem sm;
+  extern __shared__ wgm_lq wgm_lqs[]; /* one local queue per warp */
+  wgm_lq *q = &wgm_lqs[threadIdx.x >> 5];
   __shared__ int s_cnt[4];
   __shared__ int s_slot;
   for (;;) {
@@ -30,21 +32,31 @@ __global__ void __launch_bounds__(1024) wgm_k_batch(wgm_batch_args B) {
     const int2 sr = B.slots[slot];
     const wgm_batch_job j = B.jobs[sr.x];
     if (sr.y == 0 && threadIdx.x == 0) B.times[2 * sr.x] = wgm_globaltimer();
+    const bool async = B.lq_rounds > 0;
     if (j.team <= 1) {
-      if (j.algo == 0)
-        wgm_cta_lonestar<false>(B, j, sr.x, s_cnt, &sm);
-      else
-        wgm_cta_lonestar<true>(B, j, sr.x, s_cnt, &sm);
+      if (j.algo == 0) {
+        if (async) wgm_cta_lonestar<false, true>(B, j, sr.x, s_cnt, &sm, q);
+        else wgm_cta_lonestar<false, false>(B, j, sr.x, s_cnt, &sm, q);
+      } else {
+        if (async) wgm_cta_lonestar<true, true>(B, j, sr.x, s_cnt, &sm, q);
+        else wgm_cta_lonestar<true, false>(B, j, sr.x, s_cnt, &sm, q);
+      }
     } else {
-      if (j.algo == 0)
-        wgm_team_lonestar<false>(B, j, sr.x, sr.y, &sm);
-      else
-        wgm_team_lonestar<true>(B, j, sr.x, sr.y, &sm);
+      if (j.algo == 0) {
+        if (async) wgm_team_lonestar<false, true>(B, j, sr.x, sr.y, &sm, q);
+        else wgm_team_lonestar<false, false>(B, j, sr.x, sr.y, &sm, q);
+      } else {
+        if (async) wgm_team_lonestar<true, true>(B, j, sr.x, sr.y, &sm, q);
+        else wgm_team_lonestar<true, false>(B, j, sr.x, sr.y, &sm, q);
+      }
     }
     if (sr.y == 0 && threadIdx.x == 0) B.times[2 * sr.x + 1] = wgm_globaltimer();
     __syncthreads();
   }
 }
+
+/* Dynamic shared memory of a launch: one local queue per warp. */
+static size_t wgm_batch_dyn_smem(int threads) { return (size_t)(threads / 32) * sizeof(wgm_lq); }
 
 struct wgm_batch {
   wgm_runtime *rt = nullptr;
@@ -69,6 +81,7 @@ struct wgm_batch {
             stamp_total = 0;
   bool has_weights = false;
   int threads = 256, ctas_per_sm = 0, piece = 0;
+  int lq_rounds = 0; /* warp-local continuation rounds per level (0: off) */
   int teams_grid = 0; /* grid the team sizes were computed for (0 = stale) */
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -187,10 +200,8 @@ extern "C" int wgm_batch_create(wgm_runtime *rt, int num_graphs, const wgm_graph
     j.team = 1;
     j.boost = 1;
     j.dist_off = dist_at[k];
-    if (j.algo == 1) {
-      j.stamp_off = stamp_off;
-      stamp_off += j.V;
-    }
+    j.stamp_off = stamp_off; /* every job: claims of the warp-local queues */
+    stamp_off += j.V;
     b->jobs.push_back(j);
     b->queue_of[k] = q;
   }
@@ -289,6 +300,7 @@ static wgm_batch_args wgm_batch_kargs(wgm_batch *b) {
   B.ctl = b->d_ctl;
   B.err = b->d_err;
   B.times = b->d_times;
+  B.lq_rounds = b->lq_rounds;
   B.spin_ns = b->rt->cfg.spin_timeout_ns ? b->rt->cfg.spin_timeout_ns : 2000000000ull;
   B.rows = b->d_rows;
   B.cols = b->d_cols;
@@ -303,7 +315,8 @@ static wgm_batch_args wgm_batch_kargs(wgm_batch *b) {
 static int wgm_batch_grid(wgm_batch *b, int *grid) {
   int per_sm = 0;
   cudaError_t e =
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wgm_k_batch, b->threads, 0);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wgm_k_batch, b->threads,
+                                                    wgm_batch_dyn_smem(b->threads));
   if (e != cudaSuccess) return wgm_cuda_fail(b->rt, e);
   if (per_sm < 1) return WGM_ERR_INVALID;
   int k = b->ctas_per_sm > 0 ? std::min(b->ctas_per_sm, per_sm) : per_sm;
@@ -364,7 +377,7 @@ static cudaError_t wgm_batch_enqueue(wgm_batch *b, int grid, cudaStream_t s) {
   cudaError_t e = cudaMemsetAsync(
       b->d_ctl, 0, (size_t)(1 + WGM_BATCH_CTL_LINES_PER_JOB * b->njobs) * WGM_LINE * 4, s);
   if (e != cudaSuccess) return e;
-  wgm_k_batch<<<grid, b->threads, 0, s>>>(wgm_batch_kargs(b));
+  wgm_k_batch<<<grid, b->threads, wgm_batch_dyn_smem(b->threads), s>>>(wgm_batch_kargs(b));
   return cudaGetLastError();
 }
 
@@ -581,7 +594,7 @@ extern "C" int wgm_batch_autotune(wgm_batch *b, int reps, int *best_threads,
   };
   auto grid_of = [&](int t, int c) {
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wgm_k_batch, t, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wgm_k_batch, t, wgm_batch_dyn_smem(t));
     if (c > 0) per_sm = std::min(per_sm, c);
     return std::max(1, per_sm * b->rt->prop.multiProcessorCount);
   };
@@ -603,7 +616,8 @@ extern "C" int wgm_batch_autotune(wgm_batch *b, int reps, int *best_threads,
   const double per_cta = (double)bte * grid_of(256, 0);
   for (int t : threads_set) {
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wgm_k_batch, t, 0) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wgm_k_batch, t,
+                                                      wgm_batch_dyn_smem(t)) !=
             cudaSuccess ||
         per_sm < 1)
       continue;
@@ -638,9 +652,23 @@ extern "C" int wgm_batch_autotune(wgm_batch *b, int reps, int *best_threads,
       bte = te;
     }
   }
-  /* 4. critical path: the jobs that run longest double their team, while
+  /* 4. warp-local continuation rounds at the winning point */
+  int blq = 0;
+  for (int lq : {4, 12}) {
+    int s = wgm_batch_configure_local(b, lq);
+    double ms = 0;
+    if (!s) s = point(bt, bc, bp, bte, &ms);
+    if (s) return s;
+    if (ms < best) {
+      best = ms;
+      blq = lq;
+    }
+  }
+  int s = wgm_batch_configure_local(b, blq);
+  if (s) return s;
+  /* 5. critical path: the jobs that run longest double their team, while
    * that shortens the launch */
-  int s = point(bt, bc, bp, bte, &best);
+  s = point(bt, bc, bp, bte, &best);
   if (s) return s;
   for (int it = 0; it < 6; it++) {
     std::vector<unsigned long long> t(2 * (size_t)b->njobs);
@@ -744,6 +772,15 @@ extern "C" int wgm_batch_reorder_by_last_run(wgm_batch *b) {
   for (int k = 0; k < b->njobs; k++) b->queue_of[k] = new_pos[b->queue_of[k]];
   b->jobs.swap(jobs);
   b->teams_grid = 0;
+  wgm_batch_free_graph(b);
+  return WGM_OK;
+}
+
+extern "C" int wgm_batch_configure_local(wgm_batch *b, int rounds) {
+  if (!b || rounds < 0 || rounds > WGM_LQ_ROUNDS_MAX) return WGM_ERR_INVALID;
+  cudaSetDevice(b->rt->device);
+  cudaStreamSynchronize(b->rt->stream);
+  b->lq_rounds = rounds;
   wgm_batch_free_graph(b);
   return WGM_OK;
 }

@@ -69,8 +69,209 @@ struct wgm_batch_args {
   int *levels; /* per job */
   int *err;    /* first error (WGM_DEV_*), site in err[1] */
   unsigned long long *times; /* per job: start, end (%globaltimer ns) */
+  int lq_rounds;             /* 0: plain levels; > 0: warp-local continuation */
   unsigned long long spin_ns;
 };
+
+/* ---- warp-local continuation (batch jobs) --------------------------------
+ *
+ * A batch job relaxes by atomic_min for BFS too (unit weights: the fixpoint
+ * is the hop distance, which is the Lonestar BFS level), so the order of
+ * relaxations does not matter and a warp may relax a vertex it has just
+ * improved again within the same level instead of queueing it for the next
+ * one.  High-diameter graphs (the 512x512 grids of the batch run ~1000
+ * levels) then advance several hops per level.
+ *
+ * Stamps: stamp[v] == L means "v is queued (globally for level L+1, or in
+ * some warp's local queue) and nobody has started to relax it".  The claim
+ * after an improvement is an acq_rel exchange to L; a warp about to relax a
+ * locally queued vertex first exchanges the stamp away (acq_rel) and only
+ * then reads dist[v].  An improvement that lands after that exchange sees a
+ * stamp != L and queues v again; one that landed before it is ordered
+ * before the exchange (its claim exchange was read by ours), so our read of
+ * dist[v] sees it.  Every improvement is therefore followed by a relaxation
+ * that reads it, which is all the fixpoint needs. */
+#define WGM_LQ 32   /* local queue entries per warp and buffer */
+#define WGM_LQ_ROUNDS_MAX 12
+
+struct wgm_lq {     /* per warp, dynamic shared memory */
+  int v[2][WGM_LQ];
+  int rs[2][WGM_LQ];
+  int d[2][WGM_LQ];
+  int n[2];
+};
+
+__device__ __forceinline__ int wgm_atom_exch_acqrel_gpu(int *p, int v) {
+  int old;
+  asm volatile("atom.acq_rel.gpu.global.exch.b32 %0, [%1], %2;"
+               : "=r"(old) : "l"(p), "r"(v) : "memory");
+  return old;
+}
+
+/* wgm_ls_chunk with atomic_min relaxation for both algorithms and a local
+ * sink: a claimed vertex of at most one piece goes to the warp's next local
+ * buffer while it has room, everything else to the global list. */
+template <bool SSSP>
+__device__ __forceinline__ bool wgm_ls_chunk_async(const int *row, const int *col,
+                                                   const unsigned *wt, unsigned *dist,
+                                                   int *stamp, int V, int P, int L, int start,
+                                                   int deg, int src, const wgm_ls_out &o,
+                                                   wgm_lq *q, int nb) {
+  constexpr int K = WGM_LS_K;
+  const int lane = wgm_lane();
+  const int incl = wgm_warp_incl_scan(deg);
+  const int total = __shfl_sync(WGM_FULL, incl, 31);
+  const int off = incl - deg;
+  const int base = start - off;
+  bool ok = true;
+  for (int w = 0; w < total; w += 32 * K) {
+    int e[K], u[K], rs[K], d[K], np[K], sv[K];
+    unsigned alt[K];
+    bool f[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      const int s = w + 32 * k + lane;
+      f[k] = s < total;
+      const int own = wgm_owner_of(off, min(s, total - 1));
+      e[k] = __shfl_sync(WGM_FULL, base, own) + s;
+      sv[k] = __shfl_sync(WGM_FULL, src, own);
+    }
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      u[k] = f[k] ? __ldg(&col[e[k]]) : -1;
+      unsigned wk = 1u;
+      if (SSSP) wk = f[k] ? __ldg(&wt[e[k]]) : WGM_LONESTAR_INF;
+      const unsigned dvk = f[k] ? __ldcg(&dist[sv[k]]) : 0u;
+      f[k] = f[k] && wk < WGM_LONESTAR_INF && dvk < WGM_LONESTAR_INF; /* sssp.cl:120 */
+      alt[k] = dvk + wk;
+    }
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      f[k] = f[k] && (unsigned)u[k] < (unsigned)V; /* bfs.cl:116 */
+      rs[k] = 0;
+      d[k] = 0;
+      if (f[k]) {
+        f[k] = alt[k] < atomicMin(&dist[u[k]], alt[k]);
+        rs[k] = __ldg(&row[u[k]]);
+        d[k] = __ldg(&row[u[k] + 1]);
+      }
+    }
+    int mine = 0;
+    bool loc[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      if (f[k]) f[k] = wgm_atom_exch_acqrel_gpu(&stamp[u[k]], L) != L;
+      d[k] = f[k] ? max(d[k] - rs[k], 0) : 0; /* a vertex without edges is not queued */
+      np[k] = (d[k] + P - 1) / P;
+      /* one-piece vertices go to the local queue while it has room */
+      const unsigned want = __ballot_sync(WGM_FULL, np[k] == 1);
+      const int have = q->n[nb];
+      const int pos = have + __popc(want & wgm_lanemask_lt());
+      loc[k] = np[k] == 1 && pos < WGM_LQ;
+      if (loc[k]) {
+        q->v[nb][pos] = u[k];
+        q->rs[nb][pos] = rs[k];
+        q->d[nb][pos] = d[k];
+        np[k] = 0;
+      }
+      __syncwarp();
+      if (lane == 0) q->n[nb] = min(WGM_LQ, have + __popc(want));
+      __syncwarp();
+      mine += np[k];
+    }
+    const int pincl = wgm_warp_incl_scan(mine);
+    const int ptotal = __shfl_sync(WGM_FULL, pincl, 31);
+    if (ptotal == 0) continue;
+    int pbase = 0;
+    if (lane == 31) pbase = atomicAdd(o.counter, ptotal);
+    pbase = __shfl_sync(WGM_FULL, pbase, 31);
+    if (pbase + ptotal > o.cap) {
+      ok = false;
+      continue;
+    }
+    int slot = pbase + pincl - mine;
+    int sl[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      sl[k] = slot;
+      if (np[k] <= WGM_LS_LANE_PIECES) {
+        for (int qq = 0; qq < np[k]; qq++) {
+          o.o_start[slot + qq] = rs[k] + qq * P;
+          o.o_cnt[slot + qq] = min(P, d[k] - qq * P);
+          o.o_u[slot + qq] = u[k];
+        }
+      }
+      slot += np[k];
+    }
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      unsigned big = __ballot_sync(WGM_FULL, np[k] > WGM_LS_LANE_PIECES);
+      while (big) {
+        const int j = __ffs(big) - 1;
+        big &= big - 1;
+        const int bs = __shfl_sync(WGM_FULL, rs[k], j), bd = __shfl_sync(WGM_FULL, d[k], j);
+        const int bu = __shfl_sync(WGM_FULL, u[k], j), bsl = __shfl_sync(WGM_FULL, sl[k], j);
+        const int bn = (bd + P - 1) / P;
+        for (int qq = lane; qq < bn; qq += 32) {
+          o.o_start[bsl + qq] = bs + qq * P;
+          o.o_cnt[bsl + qq] = min(P, bd - qq * P);
+          o.o_u[bsl + qq] = bu;
+        }
+      }
+    }
+  }
+  return ok;
+}
+
+/* After a warp's share of a level: relax the locally queued vertices for up
+ * to WGM_LQ_ROUNDS rounds (each round's improvements feed the next), then
+ * move what is left to the global list for the next level (still claimed). */
+template <bool SSSP>
+__device__ __forceinline__ bool wgm_ls_local_rounds(const int *row, const int *col,
+                                                    const unsigned *wt, unsigned *dist,
+                                                    int *stamp, int V, int P, int L,
+                                                    const wgm_ls_out &o, wgm_lq *q,
+                                                    int rounds) {
+  const int lane = wgm_lane();
+  bool ok = true;
+  int cur = 0;
+  for (int round = 0; round < rounds; round++) {
+    const int n = q->n[cur];
+    if (n == 0) return ok;
+    const int nxt = cur ^ 1;
+    __syncwarp();
+    if (lane == 0) q->n[nxt] = 0;
+    __syncwarp();
+    const bool have = lane < n;
+    const int v = have ? q->v[cur][lane] : 0;
+    const int rs = have ? q->rs[cur][lane] : 0;
+    const int d = have ? q->d[cur][lane] : 0;
+    if (lane == 0) q->n[cur] = 0;
+    __syncwarp();
+    if (have) wgm_atom_exch_acqrel_gpu(&stamp[v], -1); /* unclaim, then read dist[v] */
+    __syncwarp(); /* the lanes that read dist[v] are ordered after the unclaim */
+    ok &= wgm_ls_chunk_async<SSSP>(row, col, wt, dist, stamp, V, P, L, rs, have ? d : 0, v, o,
+                                   q, nxt);
+    cur = nxt;
+  }
+  /* budget spent: the rest goes to the next level as one piece each */
+  const int n = q->n[cur];
+  if (n == 0) return ok;
+  const bool have = lane < n;
+  int base = 0;
+  if (lane == 0) base = atomicAdd(o.counter, n);
+  base = __shfl_sync(WGM_FULL, base, 0);
+  if (base + n > o.cap) return false;
+  if (have) {
+    o.o_start[base + lane] = q->rs[cur][lane];
+    o.o_cnt[base + lane] = q->d[cur][lane];
+    o.o_u[base + lane] = q->v[cur][lane];
+  }
+  __syncwarp();
+  if (lane == 0) q->n[cur] = 0;
+  __syncwarp();
+  return ok;
+}
 
 /* Queue a warp's flagged vertices as pieces, CTA-local counter in smem. */
 __device__ __forceinline__ void wgm_cta_push(const int *row, int piece, bool flag, int u,
@@ -104,25 +305,26 @@ __device__ __forceinline__ void wgm_cta_push(const int *row, int piece, bool fla
 }
 
 /* One job on one CTA.  s_cnt: 3 shared level counters. */
-template <bool SSSP>
+template <bool SSSP, bool ASYNC>
 __device__ void wgm_cta_lonestar(const wgm_batch_args &B, const wgm_batch_job &j, int job,
-                                 int *s_cnt, wgm_warp_smem *sm) {
+                                 int *s_cnt, wgm_warp_smem *sm, wgm_lq *q) {
   const int V = j.V;
   const int *row = B.rows + j.row_off;
   const int *col = B.cols + j.col_off;
   const unsigned *wt = SSSP ? B.wts + j.col_off : nullptr;
   unsigned *dist = B.dist + j.dist_off;
-  int *stamp = SSSP ? B.stamp + j.stamp_off : nullptr;
+  int *stamp = B.stamp + j.stamp_off;
   const int cap = j.cap;
   int *wl_start = B.scratch + j.wl_off;
   int *wl_cnt = wl_start + 2 * (size_t)cap;
-  int *wl_u = SSSP ? wl_cnt + 2 * (size_t)cap : nullptr;
+  int *wl_u = wl_cnt + 2 * (size_t)cap;
   const int lane = wgm_lane(), warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   for (int i = threadIdx.x; i < V; i += blockDim.x) {
     dist[i] = (i == j.source) ? 0u : WGM_LONESTAR_INF;
-    if (SSSP) stamp[i] = 0;
+    stamp[i] = 0;
   }
   if (threadIdx.x < 3) s_cnt[threadIdx.x] = 0;
+  if (lane == 0) q->n[0] = q->n[1] = 0;
   __syncthreads();
   if (threadIdx.x < 32)
     wgm_cta_push(row, j.piece, threadIdx.x == 0, j.source, &s_cnt[1], wl_start + cap,
@@ -149,11 +351,17 @@ __device__ void wgm_cta_lonestar(const wgm_batch_args &B, const wgm_batch_job &j
       if (lane < per && i < n) {
         start = wl_start[io + i];
         deg = wl_cnt[io + i];
-        if (SSSP) src = wl_u[io + i];
+        src = wl_u[io + i];
       }
-      wgm_ls_chunk<SSSP, WGM_BATCH_PRECHECK>(row, col, wt, dist, stamp, V, j.piece, L, start,
-                                             deg, src, o);
+      if (ASYNC)
+        wgm_ls_chunk_async<SSSP>(row, col, wt, dist, stamp, V, j.piece, L, start, deg, src, o,
+                                 q, 0);
+      else
+        wgm_ls_chunk<SSSP, WGM_BATCH_PRECHECK>(row, col, wt, dist, stamp, V, j.piece, L, start,
+                                               deg, src, o);
     }
+    if (ASYNC) wgm_ls_local_rounds<SSSP>(row, col, wt, dist, stamp, V, j.piece, L, o, q,
+                                         B.lq_rounds);
     __syncthreads();
     L++;
   }
@@ -207,6 +415,7 @@ struct wgm_ls_job {
   int *wl_start, *wl_cnt, *wl_u; /* [2][cap] each */
   int *cnt;                      /* 3 level-counter lines, zero at start */
   int *arr;                      /* team barrier arrival line, zero at start */
+  int lq_rounds;                 /* warp-local continuation rounds (async runs) */
 };
 
 /* Run a job on a team of G > 1 CTAs.  The level loop is the persistent
@@ -214,17 +423,18 @@ struct wgm_ls_job {
  * level with the level counters triple-buffered in the job's control lines.
  * Returns the number of levels (the Lonestar iteration count), or -1 when a
  * team wait failed. */
-template <bool SSSP>
+template <bool SSSP, bool ASYNC = false>
 __device__ int wgm_team_ls_run(const wgm_ls_job &J, wgm_warp_smem *sm, int *err,
-                               unsigned long long spin_ns) {
+                               unsigned long long spin_ns, wgm_lq *q = nullptr) {
   const int V = J.V, G = J.G, rank = J.rank, cap = J.cap;
   const int lane = wgm_lane(), warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   unsigned nb = 0;
   const int tid = rank * blockDim.x + threadIdx.x, nth = G * blockDim.x;
   for (int i = tid; i < V; i += nth) {
     J.dist[i] = (i == J.source) ? 0u : WGM_LONESTAR_INF;
-    if (SSSP) J.stamp[i] = 0;
+    if (SSSP || ASYNC) J.stamp[i] = 0;
   }
+  if (ASYNC && lane == 0) q->n[0] = q->n[1] = 0;
   if (rank == 0 && threadIdx.x < 32)
     wgm_cta_push(J.row, J.piece, threadIdx.x == 0, J.source, &J.cnt[1 * WGM_LINE],
                  J.wl_start + cap, J.wl_cnt + cap, J.wl_u ? J.wl_u + cap : nullptr, sm->acc[0]);
@@ -250,11 +460,18 @@ __device__ int wgm_team_ls_run(const wgm_ls_job &J, wgm_warp_smem *sm, int *err,
       if (lane < per && i < n) {
         start = __ldcg(&J.wl_start[io + i]);
         deg = __ldcg(&J.wl_cnt[io + i]);
-        if (SSSP) src = __ldcg(&J.wl_u[io + i]);
+        if (SSSP || ASYNC) src = __ldcg(&J.wl_u[io + i]);
       }
-      wgm_ls_chunk<SSSP, WGM_BATCH_PRECHECK>(J.row, J.col, J.wt, J.dist, J.stamp, V, J.piece, L,
-                                             start, deg, src, o);
+      if (ASYNC)
+        wgm_ls_chunk_async<SSSP>(J.row, J.col, J.wt, J.dist, J.stamp, V, J.piece, L, start, deg,
+                                 src, o, q, 0);
+      else
+        wgm_ls_chunk<SSSP, WGM_BATCH_PRECHECK>(J.row, J.col, J.wt, J.dist, J.stamp, V, J.piece,
+                                               L, start, deg, src, o);
     }
+    if (ASYNC)
+      wgm_ls_local_rounds<SSSP>(J.row, J.col, J.wt, J.dist, J.stamp, V, J.piece, L, o, q,
+                                J.lq_rounds);
     if (!wgm_team_barrier(err, spin_ns, J.arr, G, &nb)) return -1;
     L++;
   }
@@ -262,9 +479,9 @@ __device__ int wgm_team_ls_run(const wgm_ls_job &J, wgm_warp_smem *sm, int *err,
 }
 
 /* One batch job on a team of G > 1 CTAs; this CTA is member `rank`. */
-template <bool SSSP>
+template <bool SSSP, bool ASYNC>
 __device__ void wgm_team_lonestar(const wgm_batch_args &B, const wgm_batch_job &j, int job,
-                                  int rank, wgm_warp_smem *sm) {
+                                  int rank, wgm_warp_smem *sm, wgm_lq *q) {
   wgm_ls_job J;
   J.V = j.V;
   J.source = j.source;
@@ -276,14 +493,15 @@ __device__ void wgm_team_lonestar(const wgm_batch_args &B, const wgm_batch_job &
   J.col = B.cols + j.col_off;
   J.wt = SSSP ? B.wts + j.col_off : nullptr;
   J.dist = B.dist + j.dist_off;
-  J.stamp = SSSP ? B.stamp + j.stamp_off : nullptr;
+  J.stamp = B.stamp + j.stamp_off;
   J.wl_start = B.scratch + j.wl_off;
   J.wl_cnt = J.wl_start + 2 * (size_t)j.cap;
-  J.wl_u = SSSP ? J.wl_cnt + 2 * (size_t)j.cap : nullptr;
+  J.wl_u = J.wl_cnt + 2 * (size_t)j.cap;
   int *ctl = B.ctl + (size_t)(1 + job * WGM_BATCH_CTL_LINES_PER_JOB) * WGM_LINE;
   J.cnt = ctl;
   J.arr = ctl + 3 * WGM_LINE;
-  const int L = wgm_team_ls_run<SSSP>(J, sm, B.err, B.spin_ns);
+  J.lq_rounds = B.lq_rounds;
+  const int L = wgm_team_ls_run<SSSP, ASYNC>(J, sm, B.err, B.spin_ns, q);
   if (L > 0 && rank == 0 && threadIdx.x == 0 && B.levels) B.levels[job] = L;
 }
 

@@ -99,6 +99,10 @@ __global__ void __launch_bounds__(1024) wgm_k_serve(wgm_launch L, wgm_serve_args
         wgm_req_reduce(A, r, rank);
       else if (r.kind == WGM_REQ_MATMUL)
         wgm_req_matmul(A, r, rank);
+      else if (r.kind == WGM_REQ_REDUCE_I32)
+        wgm_req_reduce_i32(A, r, rank);
+      else if (r.kind == WGM_REQ_MATMUL_I32)
+        wgm_req_matmul_i32(A, r, rank);
       __syncthreads();
       if (threadIdx.x == 0) {
         int *ctl = wgm_req_ctl(A, r);
@@ -181,6 +185,8 @@ struct wgm_serve {
   wgm_serve_graph *d_graphs = nullptr;
   float *d_vecs = nullptr, *d_mats = nullptr;
   int nvecs = 0, vec_len = 0, nmats = 0, mat_n = 0;
+  int *d_ivecs = nullptr, *d_imats = nullptr; /* int32 reference variants */
+  int nivecs = 0, ivec_len = 0, nimats = 0, imat_n = 0;
   /* request state */
   char *d_arena = nullptr;
   size_t arena_bytes = 0;
@@ -207,6 +213,8 @@ static size_t wgm_req_bytes(const wgm_serve *s, int kind, int arg0) {
     b += (size_t)((g.V + 63) & ~63) * 4 + 4 * (size_t)g.cap * 4;
   } else if (kind == WGM_REQ_MATMUL) {
     b += (size_t)s->mat_n * s->mat_n * 4;
+  } else if (kind == WGM_REQ_MATMUL_I32) {
+    b += (size_t)s->imat_n * s->imat_n * 4;
   }
   return b;
 }
@@ -214,11 +222,16 @@ static size_t wgm_req_bytes(const wgm_serve *s, int kind, int arg0) {
 static size_t wgm_req_result_bytes(const wgm_serve *s, int kind, int arg0) {
   if (kind == WGM_REQ_BFS) return (size_t)s->graphs[arg0].V * 4;
   if (kind == WGM_REQ_MATMUL) return (size_t)s->mat_n * s->mat_n * 4;
+  if (kind == WGM_REQ_MATMUL_I32) return 4 + (size_t)s->imat_n * s->imat_n * 4;
   return 4;
 }
 
 static size_t wgm_req_result_off(int kind) {
-  return kind == WGM_REQ_REDUCE ? 5 * WGM_LINE * 4 : WGM_REQ_CTL_BYTES;
+  /* reduce results and the int32 product's hash sit on line 5; the int32
+   * product's C follows the control lines like the other payloads, and its
+   * result is read as hash + C (line 5 is copied with the lines after it) */
+  if (kind == WGM_REQ_REDUCE || kind == WGM_REQ_REDUCE_I32) return 5 * WGM_LINE * 4;
+  return WGM_REQ_CTL_BYTES;
 }
 
 extern "C" int wgm_serve_destroy(wgm_serve *s) {
@@ -226,8 +239,8 @@ extern "C" int wgm_serve_destroy(wgm_serve *s) {
   cudaSetDevice(s->rt->device);
   cudaStreamSynchronize(s->rt->stream);
   if (s->side) cudaStreamSynchronize(s->side);
-  void *dev[] = {s->d_rows, s->d_cols, s->d_graphs, s->d_vecs, s->d_mats,
-                 s->d_arena, s->d_sd, s->d_dreq, s->d_err};
+  void *dev[] = {s->d_rows, s->d_cols, s->d_graphs, s->d_vecs, s->d_mats, s->d_arena,
+                 s->d_sd,   s->d_dreq, s->d_err,    s->d_ivecs, s->d_imats};
   for (void *p : dev)
     if (p) cudaFree(p);
   void *host[] = {s->ring_h, s->comp_h, s->hs_h};
@@ -371,6 +384,35 @@ static void wgm_serve_diag_fill(wgm_serve *s, const char *why, int64_t head, siz
   s->diag = buf;
 }
 
+extern "C" int wgm_serve_set_int_data(wgm_serve *s, int num_ivecs, int ivec_len,
+                                      const int32_t *ivecs, int num_imats, int imat_n,
+                                      const int32_t *imats) {
+  if (!s || num_ivecs < 0 || num_imats < 0 || (num_ivecs && (!ivecs || ivec_len < 1)) ||
+      (num_imats && (!imats || imat_n < 32 || imat_n % 32)))
+    return WGM_ERR_INVALID;
+  cudaSetDevice(s->rt->device);
+  cudaStreamSynchronize(s->rt->stream);
+  if (s->d_ivecs) cudaFree(s->d_ivecs);
+  if (s->d_imats) cudaFree(s->d_imats);
+  s->d_ivecs = s->d_imats = nullptr;
+  cudaError_t e = cudaMalloc((void **)&s->d_ivecs, std::max<size_t>(4, (size_t)num_ivecs * ivec_len * 4));
+  if (e == cudaSuccess)
+    e = cudaMalloc((void **)&s->d_imats,
+                   std::max<size_t>(4, (size_t)num_imats * 2 * imat_n * imat_n * 4));
+  if (e == cudaSuccess && num_ivecs)
+    e = cudaMemcpy(s->d_ivecs, ivecs, (size_t)num_ivecs * ivec_len * 4, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && num_imats)
+    e = cudaMemcpy(s->d_imats, imats, (size_t)num_imats * 2 * imat_n * imat_n * 4,
+                   cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize(); /* pageable sources */
+  if (e != cudaSuccess) return wgm_cuda_fail(s->rt, e);
+  s->nivecs = num_ivecs;
+  s->ivec_len = ivec_len;
+  s->nimats = num_imats;
+  s->imat_n = imat_n;
+  return WGM_OK;
+}
+
 static int wgm_serve_fail_run(wgm_serve *s, int status, const char *why, int64_t head,
                               size_t inflight, size_t waiting, size_t next, size_t narr) {
   wgm_set_abort(s->rt, 1);
@@ -391,6 +433,10 @@ extern "C" int wgm_serve_run(wgm_serve *s, const wgm_serve_config *cfg, wgm_serv
   const double fb = cfg->frac_bfs, fr = cfg->frac_reduce;
   if (cfg->rate_per_s > 0 && ((fb > 0 && s->graphs.empty()) || (fr > 0 && s->nvecs == 0) ||
                               (fb + fr < 1.0 - 1e-9 && s->nmats == 0)))
+    return WGM_ERR_INVALID;
+  if (cfg->frac_int < 0 || cfg->frac_int > 1 ||
+      (cfg->rate_per_s > 0 && cfg->frac_int > 0 &&
+       ((fr > 0 && s->nivecs == 0) || (fb + fr < 1.0 - 1e-9 && s->nimats == 0))))
     return WGM_ERR_INVALID;
   wgm_runtime *rt = s->rt;
   cudaSetDevice(rt->device);
@@ -427,14 +473,20 @@ extern "C" int wgm_serve_run(wgm_serve *s, const wgm_serve_config *cfg, wgm_serv
       a.t = (uint64_t)(t * 1e9);
       double x = u01(rng);
       a.kind = x < fb ? WGM_REQ_BFS : (x < fb + fr ? WGM_REQ_REDUCE : WGM_REQ_MATMUL);
+      if (a.kind != WGM_REQ_BFS && u01(rng) < cfg->frac_int)
+        a.kind = a.kind == WGM_REQ_REDUCE ? WGM_REQ_REDUCE_I32 : WGM_REQ_MATMUL_I32;
       a.arg1 = 0;
       if (a.kind == WGM_REQ_BFS) {
         a.arg0 = (int)(rng() % s->graphs.size());
         a.arg1 = (int)(rng() % (uint64_t)s->graphs[a.arg0].V);
       } else if (a.kind == WGM_REQ_REDUCE) {
         a.arg0 = (int)(rng() % (uint64_t)s->nvecs);
-      } else {
+      } else if (a.kind == WGM_REQ_MATMUL) {
         a.arg0 = (int)(rng() % (uint64_t)s->nmats);
+      } else if (a.kind == WGM_REQ_REDUCE_I32) {
+        a.arg0 = (int)(rng() % (uint64_t)s->nivecs);
+      } else {
+        a.arg0 = (int)(rng() % (uint64_t)s->nimats);
       }
       arr.push_back(a);
     }
@@ -494,6 +546,10 @@ extern "C" int wgm_serve_run(wgm_serve *s, const wgm_serve_config *cfg, wgm_serv
   A.vec_len = s->vec_len;
   A.mats = s->d_mats;
   A.mat_n = s->mat_n;
+  A.ivecs = s->d_ivecs;
+  A.ivec_len = s->ivec_len;
+  A.imats = s->d_imats;
+  A.imat_n = s->imat_n;
   A.err = s->d_err;
   A.reserve = std::max(0, cfg->reserve);
   const uint64_t run_budget = rt->cfg.run_timeout_ns ? rt->cfg.run_timeout_ns : 120000000000ull;
@@ -547,7 +603,9 @@ extern "C" int wgm_serve_run(wgm_serve *s, const wgm_serve_config *cfg, wgm_serv
       lg.kind = a.kind;
       lg.arg0 = a.arg0;
       lg.arg1 = a.arg1;
-      lg.groups = a.kind == WGM_REQ_BFS ? tb : (a.kind == WGM_REQ_REDUCE ? tr : tm);
+      lg.groups = a.kind == WGM_REQ_BFS ? tb
+                  : (a.kind == WGM_REQ_REDUCE || a.kind == WGM_REQ_REDUCE_I32) ? tr
+                                                                               : tm;
       if (a.kind == WGM_REQ_BFS && cfg->bfs_edges_per_group > 0)
         lg.groups = team((int)std::min<long long>(
             tb, (s->gE[a.arg0] + cfg->bfs_edges_per_group - 1) / cfg->bfs_edges_per_group));
@@ -582,9 +640,19 @@ extern "C" int wgm_serve_run(wgm_serve *s, const wgm_serve_config *cfg, wgm_serv
           const size_t rb = wgm_req_result_bytes(s, lg.kind, lg.arg0);
           lg.result_at = (int64_t)s->results.size();
           s->results.resize(s->results.size() + rb);
-          e = cudaMemcpyAsync(s->results.data() + lg.result_at,
-                              s->d_arena + lg.state_off + wgm_req_result_off(lg.kind), rb,
-                              cudaMemcpyDeviceToHost, s->side);
+          if (lg.kind == WGM_REQ_MATMUL_I32) { /* hash (line 5), then C */
+            e = cudaMemcpyAsync(s->results.data() + lg.result_at,
+                                s->d_arena + lg.state_off + 5 * WGM_LINE * 4, 4,
+                                cudaMemcpyDeviceToHost, s->side);
+            if (e == cudaSuccess)
+              e = cudaMemcpyAsync(s->results.data() + lg.result_at + 4,
+                                  s->d_arena + lg.state_off + WGM_REQ_CTL_BYTES, rb - 4,
+                                  cudaMemcpyDeviceToHost, s->side);
+          } else {
+            e = cudaMemcpyAsync(s->results.data() + lg.result_at,
+                                s->d_arena + lg.state_off + wgm_req_result_off(lg.kind), rb,
+                                cudaMemcpyDeviceToHost, s->side);
+          }
           if (e == cudaSuccess) e = cudaStreamSynchronize(s->side);
           if (e != cudaSuccess)
             return wgm_serve_fail_run(s, wgm_cuda_fail(rt, e), "result copy", head,

@@ -31,6 +31,8 @@
 #define WGM_REQ_BFS 1    /* Lonestar BFS on resident graph arg0 from source arg1 */
 #define WGM_REQ_REDUCE 2 /* FP32 min over resident vector arg0 */
 #define WGM_REQ_MATMUL 3 /* FP32 n x n product of resident operand pair arg0 */
+#define WGM_REQ_REDUCE_I32 4 /* reduce.cl: int32 min over resident int vector arg0 */
+#define WGM_REQ_MATMUL_I32 5 /* matmult.cl: int32 product of int pair arg0 + diagonal hash */
 
 #define WGM_TASK_REQ 3 /* task_array value: run request slot_req[slot] */
 
@@ -105,6 +107,10 @@ struct wgm_serve_args {
   int vec_len;
   const float *mats; /* matmul operand pairs: A then B, mat_n^2 floats each */
   int mat_n;
+  const int *ivecs;  /* int32 reduce inputs, ivec_len each */
+  int ivec_len;
+  const int *imats;  /* int32 operand pairs, imat_n^2 each */
+  int imat_n;
   int *err;          /* team waits: first error, site */
   int reserve;       /* free groups the fork leaves for requests */
   unsigned long long idle_ns;
@@ -215,6 +221,98 @@ __device__ void wgm_req_reduce(const wgm_serve_args &A, const wgm_req &r, int ra
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(WGM_FULL, v, o));
     if (threadIdx.x == 0) atomicMin(wgm_req_ctl(A, r) + 5 * WGM_LINE, v);
+  }
+  __syncthreads();
+}
+
+/* int32 min over a resident vector (reduce.cl:3-39): block min, one
+ * atomicMin per group on the result word. */
+__device__ void wgm_req_reduce_i32(const wgm_serve_args &A, const wgm_req &r, int rank) {
+  __shared__ int red[32];
+  const int *x = A.ivecs + (size_t)r.arg0 * A.ivec_len;
+  const int gid = rank * blockDim.x + threadIdx.x, nth = r.groups * blockDim.x;
+  const int len = A.ivec_len;
+  const int pre = min(len, (int)(((16u - ((unsigned)(uintptr_t)x & 15u)) & 15u) >> 2));
+  const int n4 = (len - pre) >> 2;
+  const int4 *x4 = reinterpret_cast<const int4 *>(x + pre);
+  int m = INT_MAX;
+  for (int i = gid; i < pre; i += nth) m = min(m, __ldg(&x[i]));
+  for (int i = gid; i < n4; i += nth) {
+    int4 v = __ldg(x4 + i);
+    m = min(m, min(min(v.x, v.y), min(v.z, v.w)));
+  }
+  for (int i = pre + (n4 << 2) + gid; i < len; i += nth) m = min(m, __ldg(&x[i]));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = min(m, __shfl_xor_sync(WGM_FULL, m, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    int v = threadIdx.x < (int)(blockDim.x >> 5) ? red[threadIdx.x] : INT_MAX;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(WGM_FULL, v, o));
+    if (threadIdx.x == 0) atomicMin(wgm_req_ctl(A, r) + 5 * WGM_LINE, v);
+  }
+  __syncthreads();
+}
+
+/* int32 C = A * B with wrapping arithmetic (matmult.cl:26-67), tiles over
+ * the team; the group that finishes last hashes the diagonal (djb2,
+ * matmult.cl:64, wrapping int32) into the result word. */
+__device__ void wgm_req_matmul_i32(const wgm_serve_args &A, const wgm_req &r, int rank) {
+  __shared__ int ta[32][33], tb[32][33];
+  const int n = A.imat_n, nt = n >> 5;
+  const int *Am = A.imats + (size_t)r.arg0 * 2 * n * n, *Bm = Am + (size_t)n * n;
+  int *ctl = wgm_req_ctl(A, r);
+  int *C = ctl + WGM_REQ_CTL_LINES * WGM_LINE;
+  for (int t = rank; t < nt * nt; t += r.groups) {
+    const int ti = t / nt, tj = t % nt;
+    unsigned acc[4] = {0u, 0u, 0u, 0u};
+    for (int k0 = 0; k0 < n; k0 += 32) {
+      __syncthreads();
+      for (int e = threadIdx.x; e < 1024; e += blockDim.x) {
+        const int y = e >> 5, x = e & 31;
+        ta[y][x] = __ldg(&Am[(size_t)(ti * 32 + y) * n + k0 + x]);
+        tb[y][x] = __ldg(&Bm[(size_t)(k0 + y) * n + tj * 32 + x]);
+      }
+      __syncthreads();
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const int e = threadIdx.x + q * blockDim.x;
+        if (e < 1024) {
+          const int y = e >> 5, x = e & 31;
+          unsigned a = acc[q];
+#pragma unroll 8
+          for (int k = 0; k < 32; k++) a += (unsigned)ta[y][k] * (unsigned)tb[k][x];
+          acc[q] = a;
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const int e = threadIdx.x + q * blockDim.x;
+      if (e < 1024) C[(size_t)(ti * 32 + (e >> 5)) * n + tj * 32 + (e & 31)] = (int)acc[q];
+    }
+  }
+  __shared__ int s_last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    /* the done counter of line 0 is the completion's; count the products
+     * on line 1 (unused by this kind) */
+    s_last = wgm_atom_add_acqrel_gpu(ctl + 1 * WGM_LINE, 1) == r.groups - 1;
+  }
+  __syncthreads();
+  if (s_last && threadIdx.x < 32) {
+    /* djb2 over the diagonal in order: the warp loads it, lane 0 folds */
+    unsigned h = 5381;
+    for (int i0 = 0; i0 < n; i0 += 32) {
+      const int i = i0 + (int)threadIdx.x;
+      const unsigned v = i < n ? (unsigned)__ldcg(&C[(size_t)i * n + i]) : 0u;
+      for (int k = 0; k < 32 && i0 + k < n; k++) h = h * 33u + __shfl_sync(WGM_FULL, v, k);
+    }
+    if (threadIdx.x == 0) {
+      ctl[5 * WGM_LINE] = (int)h;
+      __threadfence();
+    }
   }
   __syncthreads();
 }

@@ -9,7 +9,7 @@ import numpy as np
 
 from ._lib import WgmGraphDesc, WgmServeConfig, WgmServeStats, check, lib
 
-KINDS = {1: "bfs", 2: "reduce", 3: "matmul"}
+KINDS = {1: "bfs", 2: "reduce", 3: "matmul", 4: "reduce_i32", 5: "matmul_i32"}
 
 
 class Serve:
@@ -44,15 +44,25 @@ class Serve:
         self._h = h
         self.mat_n = mn
 
+    def set_int_data(self, ivecs: np.ndarray, imats: np.ndarray) -> None:
+        """int32 reduce inputs (n, len) and operand pairs (n, 2, m, m)."""
+        self.ivecs = np.ascontiguousarray(ivecs, np.int32)
+        self.imats = np.ascontiguousarray(imats, np.int32)
+        check(lib.wgm_serve_set_int_data(self._h, self.ivecs.shape[0], self.ivecs.shape[1],
+                                         self.ivecs.ctypes.data, self.imats.shape[0],
+                                         self.imats.shape[-1], self.imats.ctypes.data),
+              "wgm_serve_set_int_data")
+        self.imat_n = self.imats.shape[-1]
+
     def run(self, rate: float = 0.0, duration_s: float = 0.0, seed: int = 1,
             frac_bfs: float = 0.4, frac_reduce: float = 0.3, reps: int = 0,
             persist_groups: int = 0, reserve: int = 0, bfs_groups: int = 4,
             reduce_groups: int = 4, matmul_groups: int = 4, max_in_flight: int = 256,
             keep_results: bool = False, threads_per_wg: int = 0,
-            bfs_edges_per_group: int = 0) -> dict:
+            bfs_edges_per_group: int = 0, frac_int: float = 0.0) -> dict:
         c = WgmServeConfig(rate, duration_s, seed, frac_bfs, frac_reduce, reps, persist_groups,
                            reserve, bfs_groups, reduce_groups, matmul_groups, max_in_flight,
-                           int(keep_results), threads_per_wg, bfs_edges_per_group)
+                           int(keep_results), threads_per_wg, bfs_edges_per_group, frac_int)
         st = WgmServeStats()
         rc = lib.wgm_serve_run(self._h, C.byref(c), C.byref(st))
         if rc:
@@ -76,8 +86,12 @@ class Serve:
             out = np.empty(self.graphs[arg0].num_nodes, np.uint32)
         elif kind == 2:
             out = np.empty(1, np.float32)
-        else:
+        elif kind == 3:
             out = np.empty((self.mat_n, self.mat_n), np.float32)
+        elif kind == 4:
+            out = np.empty(1, np.int32)
+        else:
+            out = np.empty(1 + self.imat_n * self.imat_n, np.int32)  # hash, then C
         check(lib.wgm_serve_result(self._h, i, out.ctypes.data, out.nbytes), "wgm_serve_result")
         return out
 

@@ -246,6 +246,10 @@ int wgm_batch_configure(wgm_batch *b, int threads_per_cta, int ctas_per_sm, int 
  * max_team.  0 selects the defaults: total edges / grid, a quarter of the grid. */
 int wgm_batch_configure_teams(wgm_batch *b, int64_t team_edges, int max_team);
 int wgm_batch_team_info(wgm_batch *b, int64_t *team_edges, int *max_team);
+/* Warp-local continuation: after its share of a level a warp relaxes the
+ * vertices it just improved for up to `rounds` more rounds (0..12; 0 = plain
+ * levels).  Both give the same distances; the autotuner picks. */
+int wgm_batch_configure_local(wgm_batch *b, int rounds);
 /* Queue one batched launch on the runtime's stream (use_cuda_graph: replay a
  * captured CUDA graph of the queue reset and the launch). */
 int wgm_batch_launch(wgm_batch *b, int use_cuda_graph);
@@ -284,6 +288,8 @@ int wgm_batch_destroy(wgm_batch *b);
 #define WGM_REQ_BFS 1
 #define WGM_REQ_REDUCE 2
 #define WGM_REQ_MATMUL 3
+#define WGM_REQ_REDUCE_I32 4 /* reduce.cl int32 min */
+#define WGM_REQ_MATMUL_I32 5 /* matmult.cl int32 product and its diagonal djb2 hash */
 typedef struct wgm_serve wgm_serve;
 typedef struct wgm_serve_config {
   double rate_per_s;   /* Poisson arrival rate (0: no requests) */
@@ -302,6 +308,8 @@ typedef struct wgm_serve_config {
   int threads_per_wg;  /* 0: the runtime's */
   int64_t bfs_edges_per_group; /* > 0: a BFS query gets ceil(E / this) groups, at
                                   most bfs_groups */
+  double frac_int;     /* share of reduce/matmul requests run as the int32
+                          reference variants (needs wgm_serve_set_int_data) */
 } wgm_serve_config;
 typedef struct wgm_serve_stats {
   int64_t arrived, completed, waited_for_memory;
@@ -322,6 +330,10 @@ int wgm_serve_create(wgm_runtime *rt, wgm_app *color, wgm_app *bfs, int num_grap
                      const wgm_graph_desc *graphs, int num_vecs, int vec_len, const float *vecs,
                      int num_mats, int mat_n, const float *mats, int64_t arena_bytes,
                      wgm_serve **out);
+/* Resident data of the int32 reference variants: num_ivecs x ivec_len int32
+ * reduce inputs, num_imats pairs (A, B) of imat_n x imat_n int32. */
+int wgm_serve_set_int_data(wgm_serve *s, int num_ivecs, int ivec_len, const int32_t *ivecs,
+                           int num_imats, int imat_n, const int32_t *imats);
 int wgm_serve_run(wgm_serve *s, const wgm_serve_config *cfg, wgm_serve_stats *stats);
 /* Requests of the last run, in arrival order: kind, arg0 (graph / vector /
  * pair), arg1 (BFS source), latency (ns, arrival to completion seen by the
@@ -329,7 +341,8 @@ int wgm_serve_run(wgm_serve *s, const wgm_serve_config *cfg, wgm_serve_stats *st
 int wgm_serve_requests(wgm_serve *s, int64_t *count, int32_t *kind, int32_t *arg0,
                        int32_t *arg1, int64_t *latency_ns, int32_t *groups);
 /* Output of request i of the last run (keep_results): BFS dist (uint32 x V),
- * reduce min (one float), matmul C (mat_n^2 floats). */
+ * reduce min (one float / int32), matmul C (mat_n^2 floats), int32 matmul
+ * hash followed by C (1 + imat_n^2 int32). */
 int wgm_serve_result(wgm_serve *s, int64_t i, void *out, int64_t bytes);
 /* Where the last failed run stood (host and device counters), "" if none. */
 int wgm_serve_diag(wgm_serve *s, char *buf, size_t len);

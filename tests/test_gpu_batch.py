@@ -50,6 +50,7 @@ def test_batch_configurations(small_batch, threads, ctas, piece):
     want = _oracle(gs, jobs)
     with Runtime() as rt, Batch(rt, gs, jobs) as b:
         b.configure(threads, ctas, piece)
+        b.configure_local(ctas % 3 * 4)  # 0, 4, 8 local rounds across the cases
         b.run(use_cuda_graph=True)
         for k in range(len(jobs)):
             assert np.array_equal(b.result(k), want[k]), k
@@ -65,6 +66,7 @@ def test_batch_teams(small_batch, team_edges, max_team, threads):
     with Runtime() as rt, Batch(rt, gs, jobs) as b:
         b.configure(threads, 0, 0)
         b.configure_teams(team_edges, max_team)
+        b.configure_local(4 if threads == 256 else 12)  # warp-local continuation
         for rep in range(4):
             b.run(use_cuda_graph=rep > 0)
             allres = b.results()
@@ -108,7 +110,8 @@ def test_batch_autotune_picks_a_valid_config(small_batch):
     want = _oracle(gs, jobs)
     with Runtime() as rt, Batch(rt, gs, jobs) as b:
         best = b.autotune(reps=1)
-        assert best["threads"] in (128, 256, 512) and best["piece"] in (16, 32, 64)
+        # piece 0 = each graph's own max(32, E/V)
+        assert best["threads"] in (128, 256, 512) and best["piece"] in (0, 16, 32, 64)
         b.run()
         for k in range(len(jobs)):
             assert np.array_equal(b.result(k), want[k]), k

@@ -123,3 +123,38 @@ def test_request_larger_than_arena_is_refused(data):
                                       arena_bytes=8192) as sv:
         with pytest.raises(WgmError):
             sv.run(rate=1000, duration_s=0.05, seed=1, frac_bfs=1.0, frac_reduce=0.0)
+
+
+def _djb2_diag(C):
+    h = 5381
+    for i in range(C.shape[0]):
+        h = (h * 33 + int(C[i, i]) % (1 << 32)) % (1 << 32)
+    return h
+
+
+def test_int32_reference_variants(data):
+    """reduce.cl (int32 min) and matmult.cl (wrapping int32 product and the
+    djb2 hash of its diagonal) as served requests, checked exactly."""
+    gs, vecs, mats = data
+    rng = np.random.default_rng(8)
+    ivecs = rng.integers(1, 2**31 - 1, size=(2, (1 << 15) + 5), dtype=np.int64).astype(np.int32)
+    imats = rng.integers(-2**31, 2**31 - 1, size=(2, 2, 64, 64), dtype=np.int64).astype(np.int32)
+    with Runtime(**FAST) as rt, Serve(rt, graphs=gs, vecs=vecs, mats=mats,
+                                      arena_bytes=64 << 20) as sv:
+        sv.set_int_data(ivecs, imats)
+        st = sv.run(rate=3000, duration_s=0.05, seed=4, keep_results=True, frac_bfs=0.0,
+                    frac_reduce=0.5, frac_int=1.0, reduce_groups=3, matmul_groups=2)
+        assert st["completed"] == st["arrived"] > 20
+        rq = sv.requests()
+        assert set(np.unique(rq["kind"])) == {4, 5}
+        for i in range(len(rq["kind"])):
+            k, a0 = int(rq["kind"][i]), int(rq["arg0"][i])
+            out = sv.result(i, k, a0)
+            if k == 4:
+                assert out[0] == ivecs[a0].min(), i
+            else:
+                A = imats[a0, 0].astype(np.int64)
+                B = imats[a0, 1].astype(np.int64)
+                C = ((A @ B) % (1 << 32)).astype(np.uint32).view(np.int32)
+                assert np.array_equal(out[1:].reshape(64, 64), C), i
+                assert (int(out[0]) % (1 << 32)) == _djb2_diag(C), i
