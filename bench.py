@@ -287,7 +287,9 @@ def _served(rt, rates=(1000, 5000, 20000), reps: int = 20, reserve: int = 96) ->
             runs.append({"rate_offered": rate, "achieved_rate": st["achieved_rate"],
                          "completed": st["completed"], "p50_us": st["lat_p50_us"],
                          "p99_us": st["lat_p99_us"], "mean_us": st["lat_mean_us"],
-                         "max_us": st["lat_max_us"], "persist_ms": st["persist_ms"],
+                         "max_us": st["lat_max_us"], "exec_p50_us": st["exec_p50_us"],
+                         "exec_p99_us": st["exec_p99_us"], "wait_p50_us": st["wait_p50_us"],
+                         "wait_p99_us": st["wait_p99_us"], "persist_ms": st["persist_ms"],
                          "persist_kept": alone["persist_ms"] / st["persist_ms"],
                          "kills": st["kills"], "forks": st["forks"],
                          "waited_for_memory": st["waited_for_memory"]})

@@ -63,7 +63,9 @@ class WgmServeStats(C.Structure):
                 ("lat_p99_us", C.c_double), ("lat_mean_us", C.c_double),
                 ("lat_max_us", C.c_double), ("persist_ms", C.c_double),
                 ("persist_reps", C.c_int), ("kills", C.c_int), ("forks", C.c_int),
-                ("groups", C.c_int), ("run_ms", C.c_double)]
+                ("groups", C.c_int), ("run_ms", C.c_double), ("exec_p50_us", C.c_double),
+                ("exec_p99_us", C.c_double), ("wait_p50_us", C.c_double),
+                ("wait_p99_us", C.c_double)]
 
 
 class WgmGraphDesc(C.Structure):
@@ -137,6 +139,7 @@ _PROTOS = {
     "wgm_serve_result": (_I, [_P, C.c_int64, _P, C.c_int64]),
     "wgm_serve_destroy": (_I, [_P]),
     "wgm_serve_set_int_data": (_I, [_P, _I, _I, _P, _I, _I, _P]),
+    "wgm_serve_exec_times": (_I, [_P, C.c_int64, _P]),
     "wgm_serve_diag": (_I, [_P, C.c_char_p, C.c_size_t]),
     "wgm_batch_launch": (_I, [_P, _I]),
     "wgm_batch_run": (_I, [_P, _I, C.POINTER(C.c_double)]),

@@ -111,13 +111,20 @@ static void wgm_build_hubs(const wgm_graph_desc *g, int T, std::vector<int> &ids
       prefix.push_back(prefix.back() + d);
     }
   }
+  /* per window of 32 hub-edge slots: {h0, edge of slot k*32, slots of h0,
+   * first edge of h0+1} (see wgm_hubs) */
   int total = prefix.back();
   int nwin = (total + 31) / 32;
-  wmap.resize(nwin);
+  const int H = (int)ids.size();
+  wmap.resize(4 * (size_t)nwin);
   int h = 0;
   for (int k = 0; k < nwin; k++) {
     while (prefix[h + 1] <= k * 32) h++;
-    wmap[k] = h;
+    const int split = h + 1 < H ? std::min(32, prefix[h + 1] - k * 32) : 32;
+    wmap[4 * (size_t)k + 0] = h;
+    wmap[4 * (size_t)k + 1] = g->row_ptr[ids[h]] + (k * 32 - prefix[h]);
+    wmap[4 * (size_t)k + 2] = split;
+    wmap[4 * (size_t)k + 3] = split < 32 ? g->row_ptr[ids[h + 1]] : 0;
   }
 }
 

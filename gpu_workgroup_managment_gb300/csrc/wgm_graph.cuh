@@ -61,27 +61,35 @@ __device__ __forceinline__ void wgm_for_each_edge(int off, int deg, int base, in
 }
 
 /* Static hub layout (host-built): hub ids, their edge prefix and, for each
- * window of 32 hub-edge slots, the first hub it touches.  Hubs have degree
- * > 32, so a window touches at most two consecutive hubs. */
+ * window of 32 hub-edge slots, a 16-byte record {first hub h0, edge of the
+ * window's first slot, slots belonging to h0, first edge of hub h0+1}.  Hubs
+ * have degree > 32, so a window touches at most two consecutive hubs, and
+ * one load of the record gives every lane its hub and edge. */
 struct wgm_hubs {
   const int *ids;    /* [H] */
   const int *prefix; /* [H+1] */
-  const int *wmap;   /* [ceil(prefix[H]/32)] */
+  const int *wmap;   /* [4 * ceil(prefix[H]/32)] window records */
   int H;
   int total;
 };
+
+/* Hub and edge of this lane's slot in window k. */
+__device__ __forceinline__ void wgm_hub_slot(const int4 &w, int lane, int *h, int *e) {
+  const bool first = lane < w.z;
+  *h = first ? w.x : w.x + 1;
+  *e = first ? w.y + lane : w.w + (lane - w.z);
+}
 
 /* Calls f(valid, hub_index, edge) for one window of hub edges. */
 template <class F>
 __device__ __forceinline__ void wgm_hub_window(const wgm_hubs &hb, const int *row, int k,
                                                F &&f) {
   const int lane = wgm_lane();
-  int slot = k * 32 + lane;
-  bool valid = slot < hb.total;
-  int h0 = __ldg(&hb.wmap[k]);
-  int h = h0;
-  if (h0 + 1 < hb.H && slot >= __ldg(&hb.prefix[h0 + 1])) h = h0 + 1;
-  int e = __ldg(&row[__ldg(&hb.ids[h])]) + (slot - __ldg(&hb.prefix[h]));
+  const bool valid = k * 32 + lane < hb.total;
+  const int4 w = __ldg(reinterpret_cast<const int4 *>(hb.wmap) + k);
+  int h, e;
+  wgm_hub_slot(w, lane, &h, &e);
+  (void)row;
   f(valid, h, e);
 }
 
@@ -1149,19 +1157,41 @@ static __device__ int wgm_phase_pagerank(const wgm_launch &Lc, wgm_cta *c, const
       if (dfull == 0) dl += p;
     }
   }
-  int nwin = (a.hubs.total + 31) >> 5;
-  for (int k = s.gw; k < nwin; k += s.NW) {
-    wgm_hub_window(a.hubs, a.row, k, [&](bool valid, int h, int e) {
-      int h0 = __shfl_sync(WGM_FULL, h, 0);
-      float v = valid ? __ldcg(&cin[__ldg(&a.col[e])]) : 0.f;
+  /* hub edges: four windows per warp step, their records, col loads and
+   * gathers in flight together */
+  const int nwin = (a.hubs.total + 31) >> 5;
+  const int4 *wrec = reinterpret_cast<const int4 *>(a.hubs.wmap);
+  for (int k0 = s.gw * 4; k0 < nwin; k0 += s.NW * 4) {
+    int4 w[4];
+    int hh[4], u[4];
+    bool val[4];
+    float v[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const int k = min(k0 + q, nwin - 1);
+      w[q] = __ldg(wrec + k);
+      val[q] = k0 + q < nwin && (k0 + q) * 32 + lane < a.hubs.total;
+    }
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      int e;
+      wgm_hub_slot(w[q], lane, &hh[q], &e);
+      u[q] = val[q] ? __ldg(&a.col[e]) : 0;
+    }
+#pragma unroll
+    for (int q = 0; q < 4; q++) v[q] = val[q] ? __ldcg(&cin[u[q]]) : 0.f;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      if (k0 + q >= nwin) break; /* warp-uniform */
+      const int h0 = w[q].x;
       int m0, m1;
       float f0, f1;
-      wgm_two_seg_reduce(h == h0, 0, v, 2, &m0, &m1, &f0, &f1);
+      wgm_two_seg_reduce(hh[q] == h0, 0, v[q], 2, &m0, &m1, &f0, &f1);
       if (lane == 0) {
         atomicAdd(&a.hub_sum[h0], f0);
         if (h0 + 1 < a.hubs.H && f1 != 0.f) atomicAdd(&a.hub_sum[h0 + 1], f1);
       }
-    });
+    }
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) dl += __shfl_xor_sync(WGM_FULL, dl, o);

@@ -108,6 +108,8 @@ __global__ void __launch_bounds__(1024) wgm_k_serve(wgm_launch L, wgm_serve_args
         int *ctl = wgm_req_ctl(A, r);
         /* the last group of the team posts the completion */
         if (wgm_atom_add_acqrel_gpu(ctl, 1) == r.groups - 1) {
+          if (A.rtimes && r.id < A.max_requests)
+            A.rtimes[2 * (size_t)r.id + 1] = wgm_globaltimer();
           wgm_st_release_sys(&A.completions[r.id % A.ring_size], r.id + 1);
           wgm_atom_add_acqrel_gpu(&A.sd->completed, 1);
         }
@@ -204,6 +206,9 @@ struct wgm_serve {
   std::vector<wgm_serve_req_log> log;
   std::vector<char> results;
   std::string diag; /* where the last failed run stood */
+  unsigned long long *d_rtimes = nullptr; /* per request: device start, end */
+  int rtimes_cap = 0;
+  std::vector<unsigned long long> rtimes;  /* copy of the last run's */
 };
 
 static size_t wgm_req_bytes(const wgm_serve *s, int kind, int arg0) {
@@ -239,8 +244,8 @@ extern "C" int wgm_serve_destroy(wgm_serve *s) {
   cudaSetDevice(s->rt->device);
   cudaStreamSynchronize(s->rt->stream);
   if (s->side) cudaStreamSynchronize(s->side);
-  void *dev[] = {s->d_rows, s->d_cols, s->d_graphs, s->d_vecs, s->d_mats, s->d_arena,
-                 s->d_sd,   s->d_dreq, s->d_err,    s->d_ivecs, s->d_imats};
+  void *dev[] = {s->d_rows, s->d_cols,   s->d_graphs, s->d_vecs,  s->d_mats,   s->d_arena,
+                 s->d_sd,   s->d_dreq,   s->d_err,    s->d_ivecs, s->d_imats, s->d_rtimes};
   for (void *p : dev)
     if (p) cudaFree(p);
   void *host[] = {s->ring_h, s->comp_h, s->hs_h};
@@ -493,6 +498,14 @@ extern "C" int wgm_serve_run(wgm_serve *s, const wgm_serve_config *cfg, wgm_serv
   }
   for (const arrival &a : arr)
     if (wgm_req_bytes(s, a.kind, a.arg0) > s->arena_bytes) return WGM_ERR_OOM;
+  if ((int)arr.size() > s->rtimes_cap) {
+    if (s->d_rtimes) cudaFree(s->d_rtimes);
+    s->d_rtimes = nullptr;
+    s->rtimes_cap = 0;
+    cudaError_t ea = cudaMalloc((void **)&s->d_rtimes, 16 * arr.size());
+    if (ea != cudaSuccess) return wgm_cuda_fail(rt, ea);
+    s->rtimes_cap = (int)arr.size();
+  }
 
   /* reset the serving words */
   std::memset(s->ring_h, 0, sizeof(wgm_req) * s->ring);
@@ -552,6 +565,8 @@ extern "C" int wgm_serve_run(wgm_serve *s, const wgm_serve_config *cfg, wgm_serv
   A.imat_n = s->imat_n;
   A.err = s->d_err;
   A.reserve = std::max(0, cfg->reserve);
+  A.rtimes = s->d_rtimes;
+  A.max_requests = s->rtimes_cap;
   const uint64_t run_budget = rt->cfg.run_timeout_ns ? rt->cfg.run_timeout_ns : 120000000000ull;
   A.idle_ns = run_budget;
   __atomic_store_n(&rt->hf->persistent_flag, 0, __ATOMIC_RELEASE);
@@ -679,9 +694,30 @@ extern "C" int wgm_serve_run(wgm_serve *s, const wgm_serve_config *cfg, wgm_serv
   wgm_serve_dev sd;
   if (cudaMemcpy(&sd, s->d_sd, sizeof(sd), cudaMemcpyDeviceToHost) != cudaSuccess)
     std::memset(&sd, 0, sizeof(sd));
+  s->rtimes.assign(2 * s->log.size(), 0ull);
+  if (!s->log.empty() && s->d_rtimes)
+    cudaMemcpy(s->rtimes.data(), s->d_rtimes, 16 * s->log.size(), cudaMemcpyDeviceToHost);
   if (st) {
     std::memset(st, 0, sizeof(*st));
-    std::vector<double> lat;
+    std::vector<double> lat, exe, wait;
+    for (size_t i = 0; i < s->log.size(); i++) {
+      const auto &lg = s->log[i];
+      const unsigned long long t0 = s->rtimes[2 * i], t1 = s->rtimes[2 * i + 1];
+      if (!lg.done_ns || !t0 || t1 < t0) continue;
+      const double ex = (double)(t1 - t0) / 1000.0;
+      exe.push_back(ex);
+      wait.push_back(std::max(0.0, (double)(lg.done_ns - lg.arrive_ns) / 1000.0 - ex));
+    }
+    auto pct = [](std::vector<double> &v, double p) {
+      if (v.empty()) return 0.0;
+      std::sort(v.begin(), v.end());
+      size_t i = (size_t)std::ceil(p * (double)v.size()) - 1;
+      return v[std::min(i, v.size() - 1)];
+    };
+    st->exec_p50_us = pct(exe, 0.5);
+    st->exec_p99_us = pct(exe, 0.99);
+    st->wait_p50_us = pct(wait, 0.5);
+    st->wait_p99_us = pct(wait, 0.99);
     uint64_t first = ~0ull, last = 0;
     for (const auto &lg : s->log) {
       if (!lg.done_ns) continue;
@@ -749,5 +785,18 @@ extern "C" int wgm_serve_result(wgm_serve *s, int64_t i, void *out, int64_t byte
 extern "C" int wgm_serve_diag(wgm_serve *s, char *buf, size_t len) {
   if (!s || !buf || len == 0) return WGM_ERR_INVALID;
   std::snprintf(buf, len, "%s", s->diag.c_str());
+  return WGM_OK;
+}
+
+/* Device execution time of each request of the last run (from the moment the
+ * scheduler gave it its team to the moment its last group finished), ns; -1
+ * where not recorded. */
+extern "C" int wgm_serve_exec_times(wgm_serve *s, int64_t n, int64_t *exec_ns) {
+  if (!s || !exec_ns || n < (int64_t)s->log.size()) return WGM_ERR_INVALID;
+  for (size_t i = 0; i < s->log.size(); i++) {
+    const unsigned long long t0 = i * 2 < s->rtimes.size() ? s->rtimes[2 * i] : 0;
+    const unsigned long long t1 = i * 2 + 1 < s->rtimes.size() ? s->rtimes[2 * i + 1] : 0;
+    exec_ns[i] = (t0 && t1 >= t0 && s->log[i].done_ns) ? (int64_t)(t1 - t0) : -1;
+  }
   return WGM_OK;
 }

@@ -112,6 +112,8 @@ struct wgm_serve_args {
   const int *imats;  /* int32 operand pairs, imat_n^2 each */
   int imat_n;
   int *err;          /* team waits: first error, site */
+  unsigned long long *rtimes; /* per request id: start, end (%globaltimer ns) */
+  int max_requests;           /* entries of rtimes */
   int reserve;       /* free groups the fork leaves for requests */
   unsigned long long idle_ns;
 };
@@ -627,6 +629,8 @@ static __device__ bool wgm_serve_scheduler(const wgm_launch &L, const wgm_serve_
         int *ctl = (int *)(A.arena + __ldcg(&A.dreq[ri].state_off));
         for (int l = 0; l < WGM_REQ_CTL_LINES; l++) ctl[l * WGM_LINE] = 0;
         ctl[5 * WGM_LINE] = INT_MAX; /* reduce result */
+        const int id = __ldcg(&A.dreq[ri].id);
+        if (A.rtimes && id < A.max_requests) A.rtimes[2 * (size_t)id] = wgm_globaltimer();
         __threadfence();
       }
       __syncwarp();

@@ -79,7 +79,9 @@ class Serve:
         lat = np.empty(n.value, np.int64)
         check(lib.wgm_serve_requests(self._h, C.byref(n), k.ctypes.data, a0.ctypes.data,
                                      a1.ctypes.data, lat.ctypes.data, g.ctypes.data))
-        return {"kind": k, "arg0": a0, "arg1": a1, "latency_ns": lat, "groups": g}
+        ex = np.empty(n.value, np.int64)
+        check(lib.wgm_serve_exec_times(self._h, n.value, ex.ctypes.data))
+        return {"kind": k, "arg0": a0, "arg1": a1, "latency_ns": lat, "groups": g, "exec_ns": ex}
 
     def result(self, i: int, kind: int, arg0: int) -> np.ndarray:
         if kind == 1:

@@ -321,6 +321,10 @@ typedef struct wgm_serve_stats {
   int kills, forks;      /* groups ceded and taken back by the persistent job */
   int groups;            /* discovered groups (scheduler included) */
   double run_ms;         /* whole launch, host clock */
+  /* the reference communicator's split (cl_communicator.h:296-336): execution
+   * = device time from team assignment to the last group's end; wait = the
+   * rest of the latency (admission, ring, waiting for groups, completion seen) */
+  double exec_p50_us, exec_p99_us, wait_p50_us, wait_p99_us;
 } wgm_serve_stats;
 /* color/bfs: the persistent job's apps (both NULL: requests only), created
  * with wgm_app_create on the same graph.  graphs: BFS query graphs; vecs:
@@ -344,6 +348,8 @@ int wgm_serve_requests(wgm_serve *s, int64_t *count, int32_t *kind, int32_t *arg
  * reduce min (one float / int32), matmul C (mat_n^2 floats), int32 matmul
  * hash followed by C (1 + imat_n^2 int32). */
 int wgm_serve_result(wgm_serve *s, int64_t i, void *out, int64_t bytes);
+/* Device execution time (ns) of each request of the last run, -1 if none. */
+int wgm_serve_exec_times(wgm_serve *s, int64_t n, int64_t *exec_ns);
 /* Where the last failed run stood (host and device counters), "" if none. */
 int wgm_serve_diag(wgm_serve *s, char *buf, size_t len);
 int wgm_serve_destroy(wgm_serve *s);

@@ -49,6 +49,10 @@ def test_requests_only(data):
         for i in range(len(rq["kind"])):
             _check_request(sv, data, i, rq["kind"][i], rq["arg0"][i], rq["arg1"][i])
         assert st["lat_p50_us"] > 0 and st["lat_p99_us"] >= st["lat_p50_us"]
+        # execution (device) is part of the latency (host); both recorded per request
+        assert 0 < st["exec_p50_us"] <= st["lat_p99_us"] and st["wait_p50_us"] >= 0
+        done = rq["latency_ns"] >= 0
+        assert np.all(rq["exec_ns"][done] > 0) and np.all(rq["exec_ns"][done] <= rq["latency_ns"][done])
 
 
 def test_same_alone_and_in_the_mix(data):
