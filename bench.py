@@ -215,7 +215,7 @@ def _reference_arm(args, ws, rank) -> int:
 
 def _barrier_sweep() -> int:
     from gpu_workgroup_managment_gb300 import Runtime
-    kinds = {0: "sense", 1: "xf", 2: "tree", 3: "count", 4: "spread"}
+    kinds = {0: "sense", 1: "xf", 2: "tree", 3: "count", 4: "spread", 5: "auto"}
     with Runtime() as rt:
         for threads in (128, 256, 512, 1024):
             for kind, name in kinds.items():
@@ -442,13 +442,16 @@ def main() -> int:
         st = b.job_stats()
         extra["makespan_ms"] = float(st["end_ns"].max()) / 1e6
         extra["max_team"] = int(st["team"].max())
+        # the default barrier (automatic kind: counting up to 384 CTAs, sense above)
         bb = rt.barrier_bench(iterations=100000, threads_per_wg=256)
         extra["barrier_ns"] = bb["ns_per_barrier"]
         extra["barrier_ctas"] = bb["groups"]
         extra["barrier_count"] = bb["barriers"]
+        extra["barrier_kind"] = "sense" if bb["groups"] > 384 else "count"
         bb = rt.barrier_bench(iterations=100000, threads_per_wg=1024)
         extra["barrier_ns_1024_threads"] = bb["ns_per_barrier"]
         extra["barrier_ctas_1024_threads"] = bb["groups"]
+        extra["barrier_kind_1024_threads"] = "sense" if bb["groups"] > 384 else "count"
         extra["sssp_rmat20"] = _sssp_rmat(rt, 20, 5, 3)
         try:
             extra["served"] = _served(rt)

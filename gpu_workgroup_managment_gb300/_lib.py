@@ -24,7 +24,7 @@ STATUS_CODE = {v: k for k, v in STATUS.items()}
 APP_LONESTAR_BFS, APP_LONESTAR_SSSP, APP_PANNOTIA_COLOR = 1, 2, 3
 APP_PANNOTIA_MIS, APP_PANNOTIA_SSSP, APP_PAGERANK = 4, 5, 6
 DISCOVERY_TICKET, DISCOVERY_REFERENCE = 0, 1
-BARRIER_SENSE, BARRIER_XF, BARRIER_TREE, BARRIER_COUNT, BARRIER_SPREAD = 0, 1, 2, 3, 4
+BARRIER_SENSE, BARRIER_XF, BARRIER_TREE, BARRIER_COUNT, BARRIER_SPREAD, BARRIER_AUTO = 0, 1, 2, 3, 4, 5
 NP_NONE, NP_MATMULT_I32, NP_REDUCE_I32, NP_MATMULT_F32, NP_REDUCE_F32 = 0, 1, 2, 3, 4
 
 

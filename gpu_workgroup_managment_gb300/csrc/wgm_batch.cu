@@ -200,8 +200,11 @@ extern "C" int wgm_batch_create(wgm_runtime *rt, int num_graphs, const wgm_graph
     j.team = 1;
     j.boost = 1;
     j.dist_off = dist_at[k];
-    j.stamp_off = stamp_off; /* every job: claims of the warp-local queues */
-    stamp_off += j.V;
+    /* every job: claims of the warp-local queues, or (SSSP) one 64-bit
+     * {level tag, distance} word per vertex; offsets stay even, so the
+     * words are 8-byte aligned */
+    j.stamp_off = stamp_off;
+    stamp_off += 2LL * j.V;
     b->jobs.push_back(j);
     b->queue_of[k] = q;
   }

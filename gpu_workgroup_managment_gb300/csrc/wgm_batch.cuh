@@ -44,7 +44,7 @@ struct wgm_batch_job {
   long long col_off;  /* col / weights of the graph start here */
   long long dist_off; /* output dist[V] */
   long long wl_off;   /* scratch: 3 x 2 x cap ints (start, cnt, u) */
-  long long stamp_off;/* SSSP scratch: stamp[V] */
+  long long stamp_off;/* scratch: 2V ints (stamps, or SSSP {tag, dist} words) */
   int cap;
   int graph; /* graph index (host bookkeeping) */
   int team;  /* CTAs working on the job */
@@ -183,7 +183,7 @@ __device__ __forceinline__ bool wgm_ls_chunk_async(const int *row, const int *co
     const int ptotal = __shfl_sync(WGM_FULL, pincl, 31);
     if (ptotal == 0) continue;
     int pbase = 0;
-    if (lane == 31) pbase = atomicAdd(o.counter, ptotal);
+    if (lane == 31) pbase = wgm_out_reserve(o, ptotal);
     pbase = __shfl_sync(WGM_FULL, pbase, 31);
     if (pbase + ptotal > o.cap) {
       ok = false;
@@ -259,7 +259,7 @@ __device__ __forceinline__ bool wgm_ls_local_rounds(const int *row, const int *c
   if (n == 0) return ok;
   const bool have = lane < n;
   int base = 0;
-  if (lane == 0) base = atomicAdd(o.counter, n);
+  if (lane == 0) base = wgm_out_reserve(o, n);
   base = __shfl_sync(WGM_FULL, base, 0);
   if (base + n > o.cap) return false;
   if (have) {
@@ -319,9 +319,18 @@ __device__ void wgm_cta_lonestar(const wgm_batch_args &B, const wgm_batch_job &j
   int *wl_cnt = wl_start + 2 * (size_t)cap;
   int *wl_u = wl_cnt + 2 * (size_t)cap;
   const int lane = wgm_lane(), warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  /* SSSP without the local queues relaxes packed {tag, distance} words in
+   * the stamp scratch and copies the distances out at the end */
+  constexpr bool PACK = SSSP && !ASYNC;
+  unsigned *dw = PACK ? reinterpret_cast<unsigned *>(stamp) : dist;
   for (int i = threadIdx.x; i < V; i += blockDim.x) {
-    dist[i] = (i == j.source) ? 0u : WGM_LONESTAR_INF;
-    stamp[i] = 0;
+    if (PACK) {
+      reinterpret_cast<unsigned long long *>(stamp)[i] =
+          (i == j.source) ? 0ull : (unsigned long long)WGM_LONESTAR_INF << 32;
+    } else {
+      dist[i] = (i == j.source) ? 0u : WGM_LONESTAR_INF;
+      stamp[i] = 0;
+    }
   }
   if (threadIdx.x < 3) s_cnt[threadIdx.x] = 0;
   if (lane == 0) q->n[0] = q->n[1] = 0;
@@ -357,19 +366,25 @@ __device__ void wgm_cta_lonestar(const wgm_batch_args &B, const wgm_batch_job &j
         wgm_ls_chunk_async<SSSP>(row, col, wt, dist, stamp, V, j.piece, L, start, deg, src, o,
                                  q, 0);
       else
-        wgm_ls_chunk<SSSP, WGM_BATCH_PRECHECK>(row, col, wt, dist, stamp, V, j.piece, L, start,
-                                               deg, src, o);
+        wgm_ls_chunk<SSSP, WGM_BATCH_PRECHECK, PACK>(row, col, wt, dw, stamp, V, j.piece, L,
+                                                     start, deg, src, o);
     }
     if (ASYNC) wgm_ls_local_rounds<SSSP>(row, col, wt, dist, stamp, V, j.piece, L, o, q,
                                          B.lq_rounds);
     __syncthreads();
     L++;
   }
+  if (PACK)
+    for (int i = threadIdx.x; i < V; i += blockDim.x) dist[i] = dw[2 * i + 1];
   if (threadIdx.x == 0 && B.levels) B.levels[job] = L;
 }
 
-/* Team barrier: a counting barrier on the job's arrival line.  `nb` holds
- * the arrivals this member has waited for so far.  Returns false when the
+/* Team barrier: a counting barrier on the job's arrival line.  An arrival
+ * is one red.release; the waiters poll with ld.acquire, which synchronises
+ * with every arrival through the counter's chain of read-modify-writes (a
+ * relaxed poll followed by a fence measured several hundred ns slower per
+ * barrier on GB300).  `nb` holds the arrivals this member has waited for so
+ * far.  Returns false when the
  * wait ran out (err[0] = WGM_DEV_TIMEOUT, err[1] = site) or another CTA
  * already failed. */
 __device__ __forceinline__ bool wgm_team_barrier(int *err, unsigned long long spin_ns, int *arr,
@@ -383,7 +398,7 @@ __device__ __forceinline__ bool wgm_team_barrier(int *err, unsigned long long sp
     wgm_red_add_release_gpu(arr, 1);
     const unsigned long long deadline = wgm_globaltimer() + spin_ns;
     unsigned it = 0;
-    while ((int)((unsigned)wgm_ld_relaxed_gpu(arr) - target) < 0) {
+    while ((int)((unsigned)wgm_ld_acquire_gpu(arr) - target) < 0) {
       if ((++it & 63u) == 0) {
         if (wgm_ld_relaxed_gpu(err) != 0) {
           ok = 0;
@@ -397,11 +412,54 @@ __device__ __forceinline__ bool wgm_team_barrier(int *err, unsigned long long sp
         if (it > 8192u) __nanosleep(64);
       }
     }
-    wgm_fence_acqrel_gpu();
     s_ok = ok;
   }
   __syncthreads();
   return s_ok != 0;
+}
+
+/* End of a team level: one barrier whose poll also returns the next
+ * level's size.  The level word packs the pieces queued for the next level
+ * (low half, bumped by the pushes) and the team's arrivals (high half);
+ * each member arrives with one 64-bit red.release after all its pushes, so
+ * the ld.acquire that sees G arrivals reads the final piece count in the
+ * same word - no separate counter read after the barrier.  Returns the
+ * count, or -1 when the wait ran out (err[0] = WGM_DEV_TIMEOUT) or another
+ * CTA already failed. */
+__device__ __forceinline__ int wgm_team_level_barrier(int *err, unsigned long long spin_ns,
+                                                      unsigned long long *word, int G) {
+  __shared__ int s_n;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    asm volatile("red.release.gpu.global.add.u64 [%0], %1;" ::"l"(word), "l"(1ull << 32)
+                 : "memory");
+    const unsigned long long deadline = wgm_globaltimer() + spin_ns;
+    unsigned it = 0;
+    unsigned long long v;
+    int n;
+    for (;;) {
+      asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(word) : "memory");
+      if ((int)(v >> 32) >= G) {
+        n = (int)(unsigned)v;
+        break;
+      }
+      if ((++it & 63u) == 0) {
+        if (wgm_ld_relaxed_gpu(err) != 0) {
+          n = -1;
+          break;
+        }
+        if (wgm_globaltimer() > deadline) {
+          if (atomicCAS(err, 0, WGM_DEV_TIMEOUT) == 0) err[1] = WGM_SITE_BARRIER;
+          n = -1;
+          break;
+        }
+        if (it > 8192u) __nanosleep(64);
+      }
+    }
+    s_n = n;
+  }
+  __syncthreads();
+  return s_n;
 }
 
 /* One Lonestar BFS/SSSP job as seen by one member of its team. */
@@ -413,7 +471,7 @@ struct wgm_ls_job {
   unsigned *dist;
   int *stamp;
   int *wl_start, *wl_cnt, *wl_u; /* [2][cap] each */
-  int *cnt;                      /* 3 level-counter lines, zero at start */
+  int *cnt;                      /* 3 level-counter lines, first 8 bytes of each zero at start */
   int *arr;                      /* team barrier arrival line, zero at start */
   int lq_rounds;                 /* warp-local continuation rounds (async runs) */
 };
@@ -430,9 +488,16 @@ __device__ int wgm_team_ls_run(const wgm_ls_job &J, wgm_warp_smem *sm, int *err,
   const int lane = wgm_lane(), warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   unsigned nb = 0;
   const int tid = rank * blockDim.x + threadIdx.x, nth = G * blockDim.x;
+  constexpr bool PACK = SSSP && !ASYNC; /* as in wgm_cta_lonestar */
+  unsigned *dw = PACK ? reinterpret_cast<unsigned *>(J.stamp) : J.dist;
   for (int i = tid; i < V; i += nth) {
-    J.dist[i] = (i == J.source) ? 0u : WGM_LONESTAR_INF;
-    if (SSSP || ASYNC) J.stamp[i] = 0;
+    if (PACK) {
+      reinterpret_cast<unsigned long long *>(J.stamp)[i] =
+          (i == J.source) ? 0ull : (unsigned long long)WGM_LONESTAR_INF << 32;
+    } else {
+      J.dist[i] = (i == J.source) ? 0u : WGM_LONESTAR_INF;
+      if (SSSP || ASYNC) J.stamp[i] = 0;
+    }
   }
   if (ASYNC && lane == 0) q->n[0] = q->n[1] = 0;
   if (rank == 0 && threadIdx.x < 32)
@@ -440,13 +505,18 @@ __device__ int wgm_team_ls_run(const wgm_ls_job &J, wgm_warp_smem *sm, int *err,
                  J.wl_start + cap, J.wl_cnt + cap, J.wl_u ? J.wl_u + cap : nullptr, sm->acc[0]);
   if (!wgm_team_barrier(err, spin_ns, J.arr, G, &nb)) return -1;
   const int gw = rank * nw + warp, NW = G * nw;
+  /* level words: the first 8 bytes of the three counter lines; level L
+   * reads word L%3, pushes into word (L+1)%3 and clears word (L+2)%3, whose
+   * last poll (the barrier ending level L-2) every member has passed */
+  unsigned long long *lw = reinterpret_cast<unsigned long long *>(J.cnt);
+  int n = __ldcg(&J.cnt[1 * WGM_LINE]);
   int L = 1;
   for (;;) {
-    const int n = __ldcg(&J.cnt[(L % 3) * WGM_LINE]);
     if (n == 0 || L > V + 2) break;
-    if (rank == 0 && threadIdx.x == 0) J.cnt[((L + 2) % 3) * WGM_LINE] = 0;
+    if (rank == 0 && threadIdx.x == 0) lw[((L + 2) % 3) * (WGM_LINE / 2)] = 0ull;
     wgm_ls_out o;
-    o.counter = &J.cnt[((L + 1) % 3) * WGM_LINE];
+    o.counter = nullptr;
+    o.counter64 = &lw[((L + 1) % 3) * (WGM_LINE / 2)];
     const size_t io = (size_t)(L & 1) * cap, oo = (size_t)((L + 1) & 1) * cap;
     o.o_start = J.wl_start + oo;
     o.o_cnt = J.wl_cnt + oo;
@@ -466,15 +536,20 @@ __device__ int wgm_team_ls_run(const wgm_ls_job &J, wgm_warp_smem *sm, int *err,
         wgm_ls_chunk_async<SSSP>(J.row, J.col, J.wt, J.dist, J.stamp, V, J.piece, L, start, deg,
                                  src, o, q, 0);
       else
-        wgm_ls_chunk<SSSP, WGM_BATCH_PRECHECK>(J.row, J.col, J.wt, J.dist, J.stamp, V, J.piece,
-                                               L, start, deg, src, o);
+        wgm_ls_chunk<SSSP, WGM_BATCH_PRECHECK, PACK>(J.row, J.col, J.wt, dw, J.stamp, V,
+                                                     J.piece, L, start, deg, src, o);
     }
     if (ASYNC)
       wgm_ls_local_rounds<SSSP>(J.row, J.col, J.wt, J.dist, J.stamp, V, J.piece, L, o, q,
                                 J.lq_rounds);
-    if (!wgm_team_barrier(err, spin_ns, J.arr, G, &nb)) return -1;
+    n = wgm_team_level_barrier(err, spin_ns, o.counter64, G);
+    if (n < 0) return -1;
     L++;
   }
+  /* every member left at the same level, after a barrier that followed the
+   * last relaxation: the words are final, each member copies its share */
+  if (PACK)
+    for (int i = tid; i < V; i += nth) J.dist[i] = dw[2 * i + 1];
   return L;
 }
 

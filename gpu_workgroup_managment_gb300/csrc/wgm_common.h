@@ -70,6 +70,11 @@
 #define WGM_BARRIER_TREE 2  /* two-level counter tree, then generation word */
 #define WGM_BARRIER_COUNT 3 /* monotonic arrival counter, waiters poll it */
 #define WGM_BARRIER_SPREAD 4 /* counter + generation copied on 16 lines */
+/* COUNT when the launch has at most WGM_BARRIER_AUTO_COUNT_MAX groups, else
+ * SENSE: one line that every CTA both updates and polls is the fastest
+ * barrier for a few hundred CTAs and the slowest for a thousand. */
+#define WGM_BARRIER_AUTO 5
+#define WGM_BARRIER_AUTO_COUNT_MAX 384
 
 #define WGM_POLL_CLOSED 0x40000000
 

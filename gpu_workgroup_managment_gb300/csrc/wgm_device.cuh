@@ -345,7 +345,8 @@ __device__ __forceinline__ bool wgm_barrier_sense(const wgm_launch &L, wgm_cta *
  * launch's discovery closer, so it starts at 0) only grows: barrier k of the
  * launch completes when it reaches (k+1)*ngroups.  An arrival is one
  * fire-and-forget red.release (this CTA's writes before the barrier are
- * published by it); the waiters poll the counter itself and then fence, so
+ * published by it); the waiters poll the counter itself with ld.acquire
+ * (a relaxed poll plus a trailing fence is slower on GB300), so
  * the last arriver needs neither a returned value nor a second store - one
  * L2 hop shorter than the generation barrier.  Differences are taken modulo
  * 2^32, which keeps the test right across wrap-around. */
@@ -358,13 +359,12 @@ __device__ __forceinline__ bool wgm_barrier_count(const wgm_launch &L, wgm_cta *
     c->tmp[2] = (int)target;
     wgm_red_add_release_gpu(ctr, 1);
     wgm_spin s = wgm_spin_start(L);
-    while ((int)((unsigned)wgm_ld_relaxed_gpu(ctr) - target) < 0) {
+    while ((int)((unsigned)wgm_ld_acquire_gpu(ctr) - target) < 0) {
       if (wgm_spin_giveup(L, s, WGM_SITE_BARRIER)) {
         c->ok = 0;
         break;
       }
     }
-    wgm_fence_acqrel_gpu();
   }
   __syncthreads();
   return c->ok;
@@ -372,10 +372,8 @@ __device__ __forceinline__ bool wgm_barrier_count(const wgm_launch &L, wgm_cta *
 
 /* Spread barrier: the sense barrier's counter, but the last arriver releases
  * the new generation on 16 lines and CTA i polls line i % 16, so no line has
- * more than ngroups/16 pollers queued on it.  Arrival is a release-only
- * fetch-add; only the last arriver, which must see every other CTA's writes
- * before it releases them, pays for an acquire fence.  Waiters poll with
- * relaxed loads and fence once. */
+ * more than ngroups/16 pollers queued on it.  Arrival is the sense
+ * barrier's acq_rel fetch-add; waiters poll their line with ld.acquire. */
 __device__ __forceinline__ bool wgm_barrier_spread(const wgm_launch &L, wgm_cta *c,
                                                    int ngroups) {
   __syncthreads();
@@ -383,16 +381,10 @@ __device__ __forceinline__ bool wgm_barrier_spread(const wgm_launch &L, wgm_cta 
     const int lane = threadIdx.x;
     const int g = c->gen;
     int last = 0;
-    if (lane == 0) {
-      int old;
-      asm volatile("atom.release.gpu.global.add.s32 %0, [%1], 1;"
-                   : "=r"(old) : "l"(&L.st->bar_count) : "memory");
-      last = old + 1 == ngroups;
-    }
+    if (lane == 0) last = wgm_atom_add_acqrel_gpu(&L.st->bar_count, 1) + 1 == ngroups;
     last = __shfl_sync(0xffffffffu, last, 0);
     if (last) {
       if (lane == 0) {
-        wgm_fence_acqrel_gpu();
         wgm_st_relaxed_gpu(&L.st->bar_count, 0);
         wgm_st_release_gpu(&L.st->bar_gen, g + 1);
       }
@@ -401,13 +393,12 @@ __device__ __forceinline__ bool wgm_barrier_spread(const wgm_launch &L, wgm_cta 
     } else if (lane == 0) {
       const int *line = &L.st->bar_gen_spread[(c->id & 15) * WGM_LINE];
       wgm_spin s = wgm_spin_start(L);
-      while ((int)((unsigned)wgm_ld_relaxed_gpu(line) - (unsigned)(g + 1)) < 0) {
+      while ((int)((unsigned)wgm_ld_acquire_gpu(line) - (unsigned)(g + 1)) < 0) {
         if (wgm_spin_giveup(L, s, WGM_SITE_BARRIER)) {
           c->ok = 0;
           break;
         }
       }
-      wgm_fence_acqrel_gpu();
     }
     if (lane == 0) c->gen = g + 1;
   }
@@ -505,6 +496,9 @@ __device__ __forceinline__ bool wgm_barrier(const wgm_launch &L, wgm_cta *c) {
       return wgm_barrier_count(L, c, c->ngroups);
     case WGM_BARRIER_SPREAD:
       return wgm_barrier_spread(L, c, c->ngroups);
+    case WGM_BARRIER_AUTO:
+      if (c->ngroups <= WGM_BARRIER_AUTO_COUNT_MAX) return wgm_barrier_count(L, c, c->ngroups);
+      return wgm_barrier_sense(L, c, c->ngroups);
     default:
       return wgm_barrier_sense(L, c, c->ngroups);
   }

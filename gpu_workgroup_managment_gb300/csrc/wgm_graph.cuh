@@ -215,12 +215,21 @@ __device__ __forceinline__ int wgm_owner_of(int off, int s) {
   return j;
 }
 
-/* Worklist a chunk pushes to. */
+/* Worklist a chunk pushes to.  The piece count lives in `counter`, or,
+ * when `counter64` is set, in the low half of a 64-bit level word whose
+ * high half counts a team's barrier arrivals. */
 struct wgm_ls_out {
   int *counter; /* pieces queued so far (global or shared memory) */
+  unsigned long long *counter64 = nullptr;
   int *o_start, *o_cnt, *o_u;
   int cap;
 };
+
+/* Reserve n slots of the output list; returns the first. */
+__device__ __forceinline__ int wgm_out_reserve(const wgm_ls_out &o, int n) {
+  if (o.counter64) return (int)(unsigned)atomicAdd(o.counter64, (unsigned long long)n);
+  return atomicAdd(o.counter, n);
+}
 
 /* Edges per lane per batch of the chunk walker: a warp relaxes 32*K edges
  * with every memory step of the K windows issued together, so K chains of
@@ -239,12 +248,21 @@ struct wgm_ls_out {
  *   one warp scan and one counter atomic for every piece of the batch.
  * The relaxation rules are stated above wgm_ls_push; the order of
  * relaxations inside a level does not change the fixpoint. */
-template <bool SSSP, bool PRE = true>
+/* PACK (SSSP only): `dist` points at 64-bit words {low: level tag, high:
+ * distance} instead of a dist[] / stamp[] pair.  One 64-bit atomicMin of
+ * (alt << 32 | L) then both relaxes and deduplicates: it lowered the
+ * distance iff the old high half exceeds alt, and a lowering whose old tag
+ * is already L found the vertex queued for L+1 by another lane this level
+ * (its tag was set by that earlier lowering).  That is the stamp exchange's
+ * rule without its dependent round trip; distances read the high halves. */
+template <bool SSSP, bool PRE = true, bool PACK = false>
 __device__ __forceinline__ bool wgm_ls_chunk(const int *row, const int *col, const unsigned *wt,
                                              unsigned *dist, int *stamp, int V, int P, int L,
                                              int start, int deg, int src,
                                              const wgm_ls_out &o) {
+  static_assert(SSSP || !PACK, "the packed word carries SSSP distances");
   constexpr int K = WGM_LS_K;
+  constexpr int DS = PACK ? 2 : 1, DH = PACK ? 1 : 0; /* distance word of v: DS*v+DH */
   const int lane = wgm_lane();
   const int incl = wgm_warp_incl_scan(deg);
   const int total = __shfl_sync(WGM_FULL, incl, 31);
@@ -270,7 +288,7 @@ __device__ __forceinline__ bool wgm_ls_chunk(const int *row, const int *col, con
       u[k] = f[k] ? __ldg(&col[e[k]]) : -1;
       if (SSSP) {
         unsigned wk = f[k] ? __ldg(&wt[e[k]]) : WGM_LONESTAR_INF;
-        unsigned dvk = f[k] ? __ldcg(&dist[sv[k]]) : 0u;
+        unsigned dvk = f[k] ? __ldcg(&dist[DS * sv[k] + DH]) : 0u;
         f[k] = f[k] && wk < WGM_LONESTAR_INF; /* sssp.cl:120 */
         alt[k] = dvk + wk;
       }
@@ -279,7 +297,7 @@ __device__ __forceinline__ bool wgm_ls_chunk(const int *row, const int *col, con
     for (int k = 0; k < K; k++) {
       f[k] = f[k] && (unsigned)u[k] < (unsigned)V; /* bfs.cl:116 */
       if (PRE && f[k]) {
-        unsigned cur = __ldcg(&dist[u[k]]);
+        unsigned cur = __ldcg(&dist[DS * u[k] + DH]);
         f[k] = SSSP ? (alt[k] < cur) : (cur == WGM_LONESTAR_INF);
       }
     }
@@ -288,7 +306,12 @@ __device__ __forceinline__ bool wgm_ls_chunk(const int *row, const int *col, con
       rs[k] = 0;
       d[k] = 0;
       if (f[k]) {
-        if (SSSP)
+        if (PACK) {
+          const unsigned long long old =
+              atomicMin(reinterpret_cast<unsigned long long *>(dist) + u[k],
+                        ((unsigned long long)alt[k] << 32) | (unsigned)L);
+          f[k] = (unsigned)(old >> 32) > alt[k] && (unsigned)old != (unsigned)L;
+        } else if (SSSP)
           f[k] = alt[k] < atomicMin(&dist[u[k]], alt[k]);
         else
           f[k] = atomicCAS(&dist[u[k]], WGM_LONESTAR_INF, (unsigned)L) == WGM_LONESTAR_INF;
@@ -299,7 +322,7 @@ __device__ __forceinline__ bool wgm_ls_chunk(const int *row, const int *col, con
     int mine = 0;
 #pragma unroll
     for (int k = 0; k < K; k++) {
-      if (SSSP && f[k]) f[k] = atomicExch(&stamp[u[k]], L) != L;
+      if (SSSP && !PACK && f[k]) f[k] = atomicExch(&stamp[u[k]], L) != L;
       d[k] = f[k] ? max(d[k] - rs[k], 0) : 0; /* a vertex without edges is not queued */
       np[k] = (d[k] + P - 1) / P;
       mine += np[k];
@@ -308,7 +331,7 @@ __device__ __forceinline__ bool wgm_ls_chunk(const int *row, const int *col, con
     const int ptotal = __shfl_sync(WGM_FULL, pincl, 31);
     if (ptotal == 0) continue;
     int pbase = 0;
-    if (lane == 31) pbase = atomicAdd(o.counter, ptotal);
+    if (lane == 31) pbase = wgm_out_reserve(o, ptotal);
     pbase = __shfl_sync(WGM_FULL, pbase, 31);
     if (pbase + ptotal > o.cap) {
       ok = false;
@@ -576,7 +599,7 @@ __device__ __forceinline__ bool wgm_frontier_chunk(const int *trow, const int *t
     const int ptotal = __shfl_sync(WGM_FULL, pincl, 31);
     if (ptotal == 0) continue;
     int pbase = 0;
-    if (lane == 31) pbase = atomicAdd(o.counter, ptotal);
+    if (lane == 31) pbase = wgm_out_reserve(o, ptotal);
     pbase = __shfl_sync(WGM_FULL, pbase, 31);
     if (pbase + ptotal > o.cap) {
       ok = false;
@@ -630,7 +653,7 @@ __device__ __forceinline__ bool wgm_frontier_push(const int *trow, int P, bool f
   int total = __shfl_sync(WGM_FULL, incl, 31);
   if (total == 0) return true;
   int base = 0;
-  if (wgm_lane() == 0) base = atomicAdd(o.counter, total);
+  if (wgm_lane() == 0) base = wgm_out_reserve(o, total);
   base = __shfl_sync(WGM_FULL, base, 0);
   if (base + total > o.cap) return false;
   int off = incl - np;
@@ -885,16 +908,31 @@ static __device__ int wgm_phase_mis(const wgm_launch &Lc, wgm_cta *c, const wgm_
     int total = __shfl_sync(WGM_FULL, incl, 31);
     int off = incl - deg;
     __syncwarp();
-    /* mis1: min over neighbours active at round start (mis.cl:44-51). */
-    wgm_for_each_edge(off, deg, start - off, total, 0, 32, sm->tab[warp],
-                      [&](bool valid, int e, int owner) {
-                        if (valid) {
-                          int j = __ldg(&a.col[e]);
-                          if (wgm_active_at(__ldcg(&a.status[j]), r))
-                            atomicMin(&sm->acc[warp][owner],
-                                      __float_as_int(__ldg(&a.node_value[j])));
-                        }
-                      });
+    /* mis1: min over neighbours active at round start (mis.cl:44-51); four
+     * 32-edge windows per step, their col loads and then their status and
+     * value gathers in flight together (a min is exact in any order) */
+    {
+      const int ebase = start - off;
+      for (int w = 0; w < total; w += 128) {
+        int own[4], j[4], stj[4], vj[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          const int sl = w + 32 * q + lane;
+          const int o = wgm_owner_of(off, min(sl, total - 1));
+          own[q] = sl < total ? o : -1;
+          const int e = __shfl_sync(WGM_FULL, ebase, o) + sl;
+          j[q] = own[q] >= 0 ? __ldg(&a.col[e]) : 0;
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          stj[q] = own[q] >= 0 ? __ldcg(&a.status[j[q]]) : 0;
+          vj[q] = own[q] >= 0 ? __float_as_int(__ldg(&a.node_value[j[q]])) : 0;
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+          if (own[q] >= 0 && wgm_active_at(stj[q], r)) atomicMin(&sm->acc[warp][own[q]], vj[q]);
+      }
+    }
     __syncwarp();
     /* mis2: join, then mark the neighbours removed (mis.cl:68-95). */
     bool join = act && __ldg(&a.node_value[i]) < __int_as_float(sm->acc[warp][lane]);
@@ -998,13 +1036,26 @@ static __device__ int wgm_phase_pannotia_sssp(const wgm_launch &Lc, wgm_cta *c,
     int total = __shfl_sync(WGM_FULL, incl, 31);
     int off = incl - deg;
     __syncwarp();
-    wgm_for_each_edge(off, deg, start - off, total, 0, 32, sm->tab[warp],
-                      [&](bool valid, int e, int owner) {
-                        if (valid) {
-                          int cand = __ldg(&a.data[e]) + __ldcg(&a.x[__ldg(&a.col[e])]);
-                          atomicMin(&sm->acc[warp][owner], cand);
-                        }
-                      });
+    /* four 32-edge windows per step: their col and weight loads, then their
+     * x gathers, in flight together (a min is exact in any order) */
+    const int ebase = start - off;
+    for (int w = 0; w < total; w += 128) {
+      int own[4], j[4], wt[4], xj[4];
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const int sl = w + 32 * q + lane;
+        const int o = wgm_owner_of(off, min(sl, total - 1));
+        own[q] = sl < total ? o : -1;
+        const int e = __shfl_sync(WGM_FULL, ebase, o) + sl;
+        j[q] = own[q] >= 0 ? __ldg(&a.col[e]) : 0;
+        wt[q] = own[q] >= 0 ? __ldg(&a.data[e]) : 0;
+      }
+#pragma unroll
+      for (int q = 0; q < 4; q++) xj[q] = own[q] >= 0 ? __ldcg(&a.x[j[q]]) : 0;
+#pragma unroll
+      for (int q = 0; q < 4; q++)
+        if (own[q] >= 0) atomicMin(&sm->acc[warp][own[q]], wt[q] + xj[q]);
+    }
     __syncwarp();
     if (deg > 0) {
       int cand = sm->acc[warp][lane];
@@ -1014,24 +1065,46 @@ static __device__ int wgm_phase_pannotia_sssp(const wgm_launch &Lc, wgm_cta *c,
       }
     }
   }
-  int nwin = (a.hubs.total + 31) >> 5;
-  for (int k = s.gw; k < nwin; k += s.NW) {
-    wgm_hub_window(a.hubs, a.row, k, [&](bool valid, int h, int e) {
-      int h0 = __shfl_sync(WGM_FULL, h, 0);
-      int val = INT_MAX;
-      if (valid) val = __ldg(&a.data[e]) + __ldcg(&a.x[__ldg(&a.col[e])]);
+  /* hub edges: four windows per warp step, their records, col and weight
+   * loads, and x gathers in flight together */
+  const int nwin = (a.hubs.total + 31) >> 5;
+  const int4 *wrec = reinterpret_cast<const int4 *>(a.hubs.wmap);
+  for (int k0 = s.gw * 4; k0 < nwin; k0 += s.NW * 4) {
+    int4 w[4];
+    int hh[4], j[4], wt[4], xj[4];
+    bool val[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const int k = min(k0 + q, nwin - 1);
+      w[q] = __ldg(wrec + k);
+      val[q] = k0 + q < nwin && (k0 + q) * 32 + lane < a.hubs.total;
+    }
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      int e;
+      wgm_hub_slot(w[q], lane, &hh[q], &e);
+      j[q] = val[q] ? __ldg(&a.col[e]) : 0;
+      wt[q] = val[q] ? __ldg(&a.data[e]) : 0;
+    }
+#pragma unroll
+    for (int q = 0; q < 4; q++) xj[q] = val[q] ? __ldcg(&a.x[j[q]]) : 0;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      if (k0 + q >= nwin) break; /* warp-uniform */
+      const int h0 = w[q].x;
       int m0, m1;
       float f0, f1;
-      wgm_two_seg_reduce(h == h0, val, 0.f, 1, &m0, &m1, &f0, &f1);
+      wgm_two_seg_reduce(hh[q] == h0, val[q] ? wt[q] + xj[q] : INT_MAX, 0.f, 1, &m0, &m1,
+                         &f0, &f1);
       if (lane == 0) {
-        int v0 = __ldg(&a.hubs.ids[h0]);
+        const int v0 = __ldg(&a.hubs.ids[h0]);
         if (m0 < __ldcg(&a.x[v0]) && atomicMin(&a.x[v0], m0) > m0) changed = true;
         if (h0 + 1 < a.hubs.H && m1 != INT_MAX) {
-          int v1 = __ldg(&a.hubs.ids[h0 + 1]);
+          const int v1 = __ldg(&a.hubs.ids[h0 + 1]);
           if (m1 < __ldcg(&a.x[v1]) && atomicMin(&a.x[v1], m1) > m1) changed = true;
         }
       }
-    });
+    }
   }
   if (__any_sync(WGM_FULL, changed) && lane == 0) a.stop[(r % 3) * WGM_LINE] = 1;
   *nxt = {1, r + 1};

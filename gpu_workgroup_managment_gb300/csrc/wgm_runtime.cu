@@ -38,7 +38,7 @@ extern "C" void wgm_config_default(wgm_config *cfg) {
   cfg->host_handshake = 0;
   cfg->discovery_mode = WGM_DISCOVERY_TICKET;
   cfg->discovery_extra_rounds = 10;
-  cfg->barrier_kind = WGM_BARRIER_SENSE;
+  cfg->barrier_kind = WGM_BARRIER_AUTO;
   cfg->tree_fanin = 8;
   cfg->hub_threshold = 256;
   cfg->spin_timeout_ns = 2000000000ull;   /* 2 s */

@@ -627,7 +627,12 @@ static __device__ bool wgm_serve_scheduler(const wgm_launch &L, const wgm_serve_
       }
       if (lane == 0) {
         int *ctl = (int *)(A.arena + __ldcg(&A.dreq[ri].state_off));
-        for (int l = 0; l < WGM_REQ_CTL_LINES; l++) ctl[l * WGM_LINE] = 0;
+        /* first 8 bytes of every line: the team Lonestar run keeps 64-bit
+         * level words there */
+        for (int l = 0; l < WGM_REQ_CTL_LINES; l++) {
+          ctl[l * WGM_LINE] = 0;
+          ctl[l * WGM_LINE + 1] = 0;
+        }
         ctl[5 * WGM_LINE] = INT_MAX; /* reduce result */
         const int id = __ldcg(&A.dreq[ri].id);
         if (A.rtimes && id < A.max_requests) A.rtimes[2 * (size_t)id] = wgm_globaltimer();

@@ -112,7 +112,7 @@ class Runtime:
         return g.value
 
     def barrier_bench(self, iterations: int = 1000, threads_per_wg: int = 256,
-                      num_wgs: int = 0, barrier_kind: int = L.BARRIER_SENSE) -> dict:
+                      num_wgs: int = 0, barrier_kind: int = L.BARRIER_AUTO) -> dict:
         """os_freq (test_suite/os_freq): iterations x 10 barriers."""
         ns, ms, g = C.c_double(), C.c_double(), C.c_int()
         check(lib.wgm_barrier_bench(self._h, threads_per_wg, num_wgs, iterations, barrier_kind,

@@ -48,6 +48,7 @@ extern "C" {
 #define WGM_BARRIER_TREE 2
 #define WGM_BARRIER_COUNT 3 /* monotonic arrival counter, waiters poll it */
 #define WGM_BARRIER_SPREAD 4 /* counter, generation released on 16 lines */
+#define WGM_BARRIER_AUTO 5   /* COUNT up to 384 groups, SENSE above (the default) */
 
 /* ---- persistent apps (the reference selects them by macro, skel.cpp:50-77) */
 #define WGM_APP_LONESTAR_BFS 1

@@ -85,6 +85,8 @@ def test_few_groups(rt, num_wgs):
 
 
 @pytest.mark.parametrize("cfg", [
+    dict(barrier_kind=0), dict(barrier_kind=0, threads_per_wg=1024),
+    dict(barrier_kind=5, threads_per_wg=1024),
     dict(barrier_kind=1), dict(barrier_kind=2), dict(barrier_kind=2, tree_fanin=3),
     dict(barrier_kind=3), dict(barrier_kind=3, threads_per_wg=128),
     dict(barrier_kind=4), dict(barrier_kind=4, threads_per_wg=1024),

@@ -28,7 +28,7 @@ def test_reference_mode_discovery(rt):
         assert res["groups"] >= 1
 
 
-@pytest.mark.parametrize("kind", [0, 1, 2, 3, 4])
+@pytest.mark.parametrize("kind", [0, 1, 2, 3, 4, 5])
 def test_barrier_bench(kind):
     with Runtime() as r:
         res = r.barrier_bench(iterations=1000, threads_per_wg=256, barrier_kind=kind)
