@@ -129,6 +129,7 @@ _PROTOS = {
     "wgm_batch_configure_teams": (_I, [_P, C.c_int64, _I]),
     "wgm_batch_team_info": (_I, [_P, _P, _P]),
     "wgm_batch_configure_local": (_I, [_P, _I]),
+    "wgm_batch_configure_sssp": (_I, [_P, C.c_double, _I]),
     "wgm_batch_upload_packed": (_I, [_P, _P, _P, _P]),
     "wgm_batch_graph_offsets": (_I, [_P, _P, _P]),
     "wgm_batch_job_stats": (_I, [_P, _P, _P, _P, _P]),

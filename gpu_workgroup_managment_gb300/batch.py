@@ -85,6 +85,12 @@ class Batch:
         """Warp-local continuation rounds per level (0 = plain levels)."""
         check(lib.wgm_batch_configure_local(self._h, rounds), "configure_local")
 
+    def configure_sssp(self, delta_mult: float = 20.0, far_cap: int = 0) -> None:
+        """Near-far SSSP buckets of delta_mult x the mean edge weight (0 = the
+        Bellman-Ford worklist); far lists of far_cap entries (0 = 2V + 64)."""
+        check(lib.wgm_batch_configure_sssp(self._h, float(delta_mult), int(far_cap)),
+              "configure_sssp")
+
     def launch(self, use_cuda_graph: bool = True) -> None:
         check(lib.wgm_batch_launch(self._h, int(use_cuda_graph)), "wgm_batch_launch")
 

@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <map>
 #include <cstring>
 #include <new>
@@ -22,7 +23,7 @@ __global__ void __launch_bounds__(1024) wgm_k_batch(wgm_batch_args B) {
   __shared__ wgm_warp_smem sm;
   extern __shared__ wgm_lq wgm_lqs[]; /* one local queue per warp */
   wgm_lq *q = &wgm_lqs[threadIdx.x >> 5];
-  __shared__ int s_cnt[4];
+  __shared__ int s_cnt[8];
   __shared__ int s_slot;
   for (;;) {
     if (threadIdx.x == 0) s_slot = atomicAdd(&B.ctl[0], 1);
@@ -82,6 +83,12 @@ struct wgm_batch {
   bool has_weights = false;
   int threads = 256, ctas_per_sm = 0, piece = 0;
   int lq_rounds = 0; /* warp-local continuation rounds per level (0: off) */
+  /* SSSP near-far schedule: bucket width = nf_mult x the graph's mean edge
+   * weight (0: the Bellman-Ford worklist); far lists of far_cap_cfg entries
+   * (0: 2V + 64) */
+  double nf_mult = 20.0;
+  int far_cap_cfg = 0;
+  std::vector<double> gmeanw; /* mean weight per graph (1 without weights) */
   int teams_grid = 0; /* grid the team sizes were computed for (0 = stale) */
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -118,10 +125,24 @@ static void wgm_batch_layout(wgm_batch *b) {
     long long p = b->piece > 0 ? b->piece : std::max(32LL, (E + V - 1) / std::max(V, 1LL));
     j.piece = (int)p;
     j.cap = (int)(V + (E + p - 1) / p + 64);
+    const long long fc = 2 * V + 64;
+    j.far_cap = j.algo ? (int)(b->far_cap_cfg > 0 ? std::min<long long>(b->far_cap_cfg, fc) : fc) : 0;
     j.wl_off = wl;
-    wl += 3LL * 2 * j.cap;
+    wl += 3LL * 2 * j.cap + 2LL * j.far_cap;
   }
   b->scratch_total = wl;
+}
+
+/* Near-far bucket width of every SSSP job from its graph's mean weight. */
+static void wgm_batch_set_deltas(wgm_batch *b) {
+  for (auto &j : b->jobs) {
+    if (!j.algo || b->nf_mult <= 0) {
+      j.delta = 0;
+      continue;
+    }
+    const double w = b->gmeanw.empty() ? 1.0 : b->gmeanw[j.graph];
+    j.delta = (unsigned)std::min(1e9, std::max(1.0, std::round(b->nf_mult * w)));
+  }
 }
 
 extern "C" int wgm_batch_create(wgm_runtime *rt, int num_graphs, const wgm_graph_desc *graphs,
@@ -248,9 +269,24 @@ extern "C" int wgm_batch_upload(wgm_batch *b, const wgm_graph_desc *graphs) {
   cudaSetDevice(b->rt->device);
   cudaStream_t s = b->rt->stream;
   cudaError_t e = cudaSuccess;
-  for (int g = 0; g < b->ngraphs && e == cudaSuccess; g++) {
+  b->gmeanw.assign(b->ngraphs, 1.0);
+  for (int g = 0; g < b->ngraphs; g++) {
     const wgm_graph_desc &d = graphs[g];
     if (d.num_nodes != b->gV[g] || d.num_edges != b->gE[g]) return WGM_ERR_INVALID;
+    if (d.weights && d.num_edges) {
+      double sum = 0;
+      long long cnt = 0;
+      for (long long k = 0; k < d.num_edges; k++)
+        if (d.weights[k] < WGM_LONESTAR_INF) {
+          sum += d.weights[k];
+          cnt++;
+        }
+      if (cnt) b->gmeanw[g] = std::max(1.0, sum / (double)cnt);
+    }
+  }
+  wgm_batch_set_deltas(b);
+  for (int g = 0; g < b->ngraphs && e == cudaSuccess; g++) {
+    const wgm_graph_desc &d = graphs[g];
     e = cudaMemcpyAsync(b->d_rows + b->g_row_off[g], d.row_ptr, (size_t)(d.num_nodes + 1) * 4,
                         cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess && d.num_edges)
@@ -384,6 +420,21 @@ static cudaError_t wgm_batch_enqueue(wgm_batch *b, int grid, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+/* New scratch layout (piece size or far lists changed): reallocate the
+ * scratch and send the jobs again. */
+static int wgm_batch_relayout(wgm_batch *b) {
+  wgm_batch_layout(b);
+  cudaFree(b->d_scratch);
+  b->d_scratch = nullptr;
+  cudaError_t e = cudaMalloc((void **)&b->d_scratch, std::max<long long>(b->scratch_total, 1) * 4);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(b->d_jobs, b->jobs.data(), sizeof(wgm_batch_job) * b->jobs.size(),
+                        cudaMemcpyHostToDevice, b->rt->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(b->rt->stream);
+  if (e != cudaSuccess) return wgm_cuda_fail(b->rt, e);
+  return WGM_OK;
+}
+
 extern "C" int wgm_batch_configure(wgm_batch *b, int threads_per_cta, int ctas_per_sm,
                                    int piece) {
   if (!b || threads_per_cta < 32 || threads_per_cta > 1024 || threads_per_cta % 32 ||
@@ -396,17 +447,23 @@ extern "C" int wgm_batch_configure(wgm_batch *b, int threads_per_cta, int ctas_p
   b->ctas_per_sm = ctas_per_sm;
   b->piece = piece;
   if (relayout) {
-    wgm_batch_layout(b);
-    cudaFree(b->d_scratch);
-    b->d_scratch = nullptr;
-    cudaError_t e = cudaMalloc((void **)&b->d_scratch, std::max<long long>(b->scratch_total, 1) * 4);
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync(b->d_jobs, b->jobs.data(), sizeof(wgm_batch_job) * b->jobs.size(),
-                          cudaMemcpyHostToDevice, b->rt->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(b->rt->stream);
-    if (e != cudaSuccess) return wgm_cuda_fail(b->rt, e);
+    int st = wgm_batch_relayout(b);
+    if (st) return st;
   }
   b->teams_grid = 0;
+  wgm_batch_free_graph(b);
+  return WGM_OK;
+}
+
+extern "C" int wgm_batch_configure_sssp(wgm_batch *b, double delta_mult, int far_cap) {
+  if (!b || !(delta_mult >= 0) || delta_mult > 1e6 || far_cap < 0) return WGM_ERR_INVALID;
+  cudaSetDevice(b->rt->device);
+  cudaStreamSynchronize(b->rt->stream);
+  b->nf_mult = delta_mult;
+  b->far_cap_cfg = far_cap;
+  wgm_batch_set_deltas(b);
+  int st = wgm_batch_relayout(b);
+  if (st) return st;
   wgm_batch_free_graph(b);
   return WGM_OK;
 }

@@ -43,9 +43,12 @@ struct wgm_batch_job {
   long long row_off;  /* row_ptr of the graph: rows[row_off .. row_off+V] */
   long long col_off;  /* col / weights of the graph start here */
   long long dist_off; /* output dist[V] */
-  long long wl_off;   /* scratch: 3 x 2 x cap ints (start, cnt, u) */
+  long long wl_off;   /* scratch: 3 x 2 x cap ints (start, cnt, u), then (SSSP)
+                         2 x far_cap ints: the near-far schedule's far lists */
   long long stamp_off;/* scratch: 2V ints (stamps, or SSSP {tag, dist} words) */
   int cap;
+  unsigned delta; /* SSSP near-far bucket width (0: Bellman-Ford worklist) */
+  int far_cap;    /* entries per far list */
   int graph; /* graph index (host bookkeeping) */
   int team;  /* CTAs working on the job */
   int boost; /* host: team multiplier from the critical-path pass */
@@ -304,7 +307,72 @@ __device__ __forceinline__ void wgm_cta_push(const int *row, int piece, bool fla
   });
 }
 
-/* One job on one CTA.  s_cnt: 3 shared level counters. */
+/* Near-far schedule for batched SSSP (packed words only).  A level relaxes
+ * the near list; an improved vertex whose distance reaches the threshold T
+ * is parked in the far list (vertex ids, one list filled while the other
+ * is drained).  When a level ends with no near work but a non-empty far
+ * list, a split step raises T to max(T, least parked distance) + delta and
+ * queues every parked vertex now below T as pieces (one copy per vertex:
+ * the first to exchange the word's tag to the split's level), moving the
+ * rest to the other far list.  Any order of relaxations that relaxes every
+ * improved vertex again reaches the same fixpoint, so the distances are
+ * those of the Bellman-Ford worklist; only the work changes: on a 512x512
+ * grid with weights U[1,1000] the worklist relaxes every edge ~27 times,
+ * near-far with delta = 20 x the mean weight ~3 times, for ~20 % more
+ * levels.  A far list that is full sends the vertex to the near list. */
+__device__ __forceinline__ bool wgm_nf_split(const int *row, int P, unsigned *dw, int L,
+                                             const int *src, int nsrc, unsigned Tn, int gw,
+                                             int NW, const wgm_ls_out &o, int *dst,
+                                             int *dst_cnt, unsigned *dst_min, int dst_cap) {
+  bool ok = true;
+  const int lane = wgm_lane();
+  for (int b = gw * 32; b < nsrc; b += NW * 32) {
+    const int i = b + lane;
+    int v = 0;
+    unsigned dv = 0;
+    bool keep = false;
+    if (i < nsrc) {
+      v = __ldcg(&src[i]);
+      dv = __ldcg(&dw[2 * v + 1]);
+      keep = dv >= Tn;
+    }
+    const unsigned kb = __ballot_sync(WGM_FULL, keep);
+    if (kb) {
+      int base = 0;
+      if (lane == 0) base = atomicAdd(dst_cnt, __popc(kb));
+      base = __shfl_sync(WGM_FULL, base, 0);
+      const int slot = base + __popc(kb & wgm_lanemask_lt());
+      unsigned m = 0xffffffffu;
+      if (keep) {
+        if (slot < dst_cap) {
+          dst[slot] = v;
+          m = dv;
+        } else {
+          keep = false; /* far list full: relax it now */
+        }
+      }
+#pragma unroll
+      for (int x = 16; x > 0; x >>= 1) m = min(m, __shfl_xor_sync(WGM_FULL, m, x));
+      if (lane == 0 && m != 0xffffffffu) atomicMin(dst_min, m);
+    }
+    bool mv = false;
+    if (i < nsrc && !keep) mv = atomicExch(&dw[2 * v], (unsigned)L) != (unsigned)L;
+    ok &= wgm_out_push_vertices(row, P, mv, v, o);
+  }
+  return ok;
+}
+
+/* Near-far bookkeeping shared by the CTA and team level loops.  Every
+ * member runs it on the same values, so all take the same steps. */
+struct wgm_nf_state {
+  unsigned T;
+  int fb;   /* far list receiving parked vertices */
+  int pend; /* far list drained by the last split: cleared at the next step */
+  bool split_last;
+};
+
+/* One job on one CTA.  s_cnt: 3 shared level counters, then (s_cnt[4..7])
+ * the two far-list counts and least parked distances. */
 template <bool SSSP, bool ASYNC>
 __device__ void wgm_cta_lonestar(const wgm_batch_args &B, const wgm_batch_job &j, int job,
                                  int *s_cnt, wgm_warp_smem *sm, wgm_lq *q) {
@@ -332,19 +400,38 @@ __device__ void wgm_cta_lonestar(const wgm_batch_args &B, const wgm_batch_job &j
       stamp[i] = 0;
     }
   }
-  if (threadIdx.x < 3) s_cnt[threadIdx.x] = 0;
+  if (threadIdx.x < 8) s_cnt[threadIdx.x] = threadIdx.x >= 6 ? (int)0xffffffffu : 0;
   if (lane == 0) q->n[0] = q->n[1] = 0;
   __syncthreads();
   if (threadIdx.x < 32)
     wgm_cta_push(row, j.piece, threadIdx.x == 0, j.source, &s_cnt[1], wl_start + cap,
                  wl_cnt + cap, wl_u ? wl_u + cap : nullptr, sm->acc[0]);
   __syncthreads();
+  const bool nf = PACK && j.delta > 0;
+  int *far = wl_u + 2 * (size_t)cap;
+  int *fctl = s_cnt + 4;
+  wgm_nf_state ns{nf ? j.delta : 0xffffffffu, 0, -1, false};
+  const int Lmax = nf ? 4 * V + 16 : V + 2;
   int L = 1;
   for (;;) {
     const int n = s_cnt[L % 3];
-    if (n == 0 || L > V + 2) break;
+    int step = 0, nfar = 0; /* 0: level, 1: split, 2: clear only */
+    if (n == 0) {
+      if (!nf) break;
+      nfar = fctl[ns.fb];
+      if (nfar == 0) break;
+      step = ns.split_last ? 2 : 1;
+    }
+    if (L > Lmax) break;
     /* the counter of level L-1, read before the previous barrier */
-    if (threadIdx.x == 0) s_cnt[(L + 2) % 3] = 0;
+    if (threadIdx.x == 0) {
+      s_cnt[(L + 2) % 3] = 0;
+      if (ns.pend >= 0) {
+        fctl[ns.pend] = 0;
+        fctl[2 + ns.pend] = (int)0xffffffffu;
+      }
+    }
+    ns.pend = -1;
     wgm_ls_out o;
     o.counter = &s_cnt[(L + 1) % 3];
     const size_t io = (size_t)(L & 1) * cap, oo = (size_t)((L + 1) & 1) * cap;
@@ -352,6 +439,28 @@ __device__ void wgm_cta_lonestar(const wgm_batch_args &B, const wgm_batch_job &j
     o.o_cnt = wl_cnt + oo;
     o.o_u = wl_u ? wl_u + oo : nullptr;
     o.cap = cap;
+    if (nf) {
+      o.far_cnt = &fctl[ns.fb];
+      o.far_min = reinterpret_cast<unsigned *>(&fctl[2 + ns.fb]);
+      o.far_list = far + (size_t)ns.fb * j.far_cap;
+      o.far_cap = j.far_cap;
+      o.T = ns.T;
+    }
+    if (step == 1) {
+      const unsigned fmin = (unsigned)fctl[2 + ns.fb];
+      const unsigned Tn =
+          (unsigned)min(0xffffffffull, (unsigned long long)max(ns.T, fmin) + j.delta);
+      const int nb = ns.fb ^ 1;
+      /* the count also holds pushes that found the list full (never stored) */
+      wgm_nf_split(row, j.piece, dw, L, far + (size_t)ns.fb * j.far_cap, min(nfar, j.far_cap),
+                   Tn, warp, nw, o,
+                   far + (size_t)nb * j.far_cap, &fctl[nb],
+                   reinterpret_cast<unsigned *>(&fctl[2 + nb]), j.far_cap);
+      ns.T = Tn;
+      ns.pend = ns.fb;
+      ns.fb = nb;
+    }
+    ns.split_last = step == 1;
     /* pieces per warp: 32, or fewer when the list is short, so a small
      * frontier spreads over every warp instead of queueing on a few */
     const int per = max(1, min(32, (n + nw - 1) / nw));
@@ -474,6 +583,8 @@ struct wgm_ls_job {
   int *cnt;                      /* 3 level-counter lines, first 8 bytes of each zero at start */
   int *arr;                      /* team barrier arrival line, zero at start */
   int lq_rounds;                 /* warp-local continuation rounds (async runs) */
+  unsigned delta = 0;            /* packed SSSP: near-far bucket width (0: worklist) */
+  int far_cap = 0;               /* entries per far list (after wl_u's 2 x cap) */
 };
 
 /* Run a job on a team of G > 1 CTAs.  The level loop is the persistent
@@ -500,6 +611,11 @@ __device__ int wgm_team_ls_run(const wgm_ls_job &J, wgm_warp_smem *sm, int *err,
     }
   }
   if (ASYNC && lane == 0) q->n[0] = q->n[1] = 0;
+  const bool nf = PACK && J.delta > 0;
+  /* far-list counts [0..1] and least parked distances [2..3], on the
+   * arrival line after its counter */
+  int *fctl = J.arr + 8;
+  if (rank == 0 && threadIdx.x == 0 && nf) fctl[2] = fctl[3] = (int)0xffffffffu;
   if (rank == 0 && threadIdx.x < 32)
     wgm_cta_push(J.row, J.piece, threadIdx.x == 0, J.source, &J.cnt[1 * WGM_LINE],
                  J.wl_start + cap, J.wl_cnt + cap, J.wl_u ? J.wl_u + cap : nullptr, sm->acc[0]);
@@ -510,10 +626,28 @@ __device__ int wgm_team_ls_run(const wgm_ls_job &J, wgm_warp_smem *sm, int *err,
    * last poll (the barrier ending level L-2) every member has passed */
   unsigned long long *lw = reinterpret_cast<unsigned long long *>(J.cnt);
   int n = __ldcg(&J.cnt[1 * WGM_LINE]);
+  int *far = nf ? J.wl_u + 2 * (size_t)cap : nullptr;
+  wgm_nf_state ns{nf ? J.delta : 0xffffffffu, 0, -1, false};
+  const int Lmax = nf ? 4 * V + 16 : V + 2;
   int L = 1;
   for (;;) {
-    if (n == 0 || L > V + 2) break;
-    if (rank == 0 && threadIdx.x == 0) lw[((L + 2) % 3) * (WGM_LINE / 2)] = 0ull;
+    int step = 0, nfar = 0; /* 0: level, 1: split, 2: clear only */
+    if (n == 0) {
+      if (!nf) break;
+      nfar = __ldcg(&fctl[ns.fb]);
+      if (nfar == 0) break;
+      step = ns.split_last ? 2 : 1;
+    }
+    if (L > Lmax) break;
+    if (rank == 0 && threadIdx.x == 0) {
+      lw[((L + 2) % 3) * (WGM_LINE / 2)] = 0ull;
+      /* every member read the drained list's count before the last barrier */
+      if (ns.pend >= 0) {
+        fctl[ns.pend] = 0;
+        fctl[2 + ns.pend] = (int)0xffffffffu;
+      }
+    }
+    ns.pend = -1;
     wgm_ls_out o;
     o.counter = nullptr;
     o.counter64 = &lw[((L + 1) % 3) * (WGM_LINE / 2)];
@@ -522,6 +656,28 @@ __device__ int wgm_team_ls_run(const wgm_ls_job &J, wgm_warp_smem *sm, int *err,
     o.o_cnt = J.wl_cnt + oo;
     o.o_u = J.wl_u ? J.wl_u + oo : nullptr;
     o.cap = cap;
+    if (nf) {
+      o.far_cnt = &fctl[ns.fb];
+      o.far_min = reinterpret_cast<unsigned *>(&fctl[2 + ns.fb]);
+      o.far_list = far + (size_t)ns.fb * J.far_cap;
+      o.far_cap = J.far_cap;
+      o.T = ns.T;
+    }
+    if (step == 1) {
+      const unsigned fmin = (unsigned)__ldcg(&fctl[2 + ns.fb]);
+      const unsigned Tn =
+          (unsigned)min(0xffffffffull, (unsigned long long)max(ns.T, fmin) + J.delta);
+      const int nb2 = ns.fb ^ 1;
+      /* the count also holds pushes that found the list full (never stored) */
+      wgm_nf_split(J.row, J.piece, dw, L, far + (size_t)ns.fb * J.far_cap, min(nfar, J.far_cap),
+                   Tn, gw, NW, o,
+                   far + (size_t)nb2 * J.far_cap, &fctl[nb2],
+                   reinterpret_cast<unsigned *>(&fctl[2 + nb2]), J.far_cap);
+      ns.T = Tn;
+      ns.pend = ns.fb;
+      ns.fb = nb2;
+    }
+    ns.split_last = step == 1;
     /* pieces per warp: 32, or fewer when the list is short, so a small
      * frontier spreads over every warp instead of queueing on a few */
     const int per = max(1, min(32, (n + NW - 1) / NW));
@@ -558,6 +714,8 @@ template <bool SSSP, bool ASYNC>
 __device__ void wgm_team_lonestar(const wgm_batch_args &B, const wgm_batch_job &j, int job,
                                   int rank, wgm_warp_smem *sm, wgm_lq *q) {
   wgm_ls_job J;
+  J.delta = j.delta;
+  J.far_cap = j.far_cap;
   J.V = j.V;
   J.source = j.source;
   J.piece = j.piece;

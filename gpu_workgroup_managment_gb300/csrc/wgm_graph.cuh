@@ -217,18 +217,53 @@ __device__ __forceinline__ int wgm_owner_of(int off, int s) {
 
 /* Worklist a chunk pushes to.  The piece count lives in `counter`, or,
  * when `counter64` is set, in the low half of a 64-bit level word whose
- * high half counts a team's barrier arrivals. */
+ * high half counts a team's barrier arrivals.  With `far_cnt` set (packed
+ * SSSP, near-far schedule) an improved vertex whose new distance is at or
+ * above `T` goes to the far list as a vertex id instead of the next level
+ * as pieces; `far_min` keeps the least distance stored there. */
 struct wgm_ls_out {
   int *counter; /* pieces queued so far (global or shared memory) */
   unsigned long long *counter64 = nullptr;
   int *o_start, *o_cnt, *o_u;
   int cap;
+  int *far_cnt = nullptr;
+  unsigned *far_min = nullptr;
+  int *far_list = nullptr;
+  int far_cap = 0;
+  unsigned T = 0xffffffffu;
 };
 
 /* Reserve n slots of the output list; returns the first. */
 __device__ __forceinline__ int wgm_out_reserve(const wgm_ls_out &o, int n) {
   if (o.counter64) return (int)(unsigned)atomicAdd(o.counter64, (unsigned long long)n);
   return atomicAdd(o.counter, n);
+}
+
+/* Queue the flagged lanes' vertices (with out-edges) as pieces of size P
+ * (warp-collective; each lane writes its own pieces).  False when the list
+ * is full. */
+__device__ __forceinline__ bool wgm_out_push_vertices(const int *row, int P, bool flag, int u,
+                                                      const wgm_ls_out &o) {
+  int rs = 0, dg = 0, np = 0;
+  if (flag) {
+    rs = __ldg(&row[u]);
+    dg = max(__ldg(&row[u + 1]) - rs, 0);
+    np = (dg + P - 1) / P;
+  }
+  const int incl = wgm_warp_incl_scan(np);
+  const int total = __shfl_sync(WGM_FULL, incl, 31);
+  if (total == 0) return true;
+  int base = 0;
+  if (wgm_lane() == 31) base = wgm_out_reserve(o, total);
+  base = __shfl_sync(WGM_FULL, base, 31);
+  if (base + total > o.cap) return false;
+  const int s = base + incl - np;
+  for (int q = 0; q < np; q++) {
+    o.o_start[s + q] = rs + q * P;
+    o.o_cnt[s + q] = min(P, dg - q * P);
+    if (o.o_u) o.o_u[s + q] = u;
+  }
+  return true;
 }
 
 /* Edges per lane per batch of the chunk walker: a warp relaxes 32*K edges
@@ -319,20 +354,61 @@ __device__ __forceinline__ bool wgm_ls_chunk(const int *row, const int *col, con
         d[k] = __ldg(&row[u[k] + 1]);
       }
     }
-    int mine = 0;
+    int mine = 0, fmine = 0;
+    bool fr[K];
 #pragma unroll
     for (int k = 0; k < K; k++) {
       if (SSSP && !PACK && f[k]) f[k] = atomicExch(&stamp[u[k]], L) != L;
       d[k] = f[k] ? max(d[k] - rs[k], 0) : 0; /* a vertex without edges is not queued */
+      /* near-far: a distance at or above the threshold waits in the far list */
+      fr[k] = PACK && d[k] > 0 && alt[k] >= o.T;
+      if (fr[k]) d[k] = 0;
+      fmine += fr[k] ? 1 : 0;
       np[k] = (d[k] + P - 1) / P;
       mine += np[k];
     }
     const int pincl = wgm_warp_incl_scan(mine);
     const int ptotal = __shfl_sync(WGM_FULL, pincl, 31);
-    if (ptotal == 0) continue;
-    int pbase = 0;
-    if (lane == 31) pbase = wgm_out_reserve(o, ptotal);
+    int fincl = 0, ftotal = 0;
+    if (PACK && __any_sync(WGM_FULL, fmine != 0)) {
+      fincl = wgm_warp_incl_scan(fmine);
+      ftotal = __shfl_sync(WGM_FULL, fincl, 31);
+    }
+    if (ptotal == 0 && ftotal == 0) continue;
+    /* the piece and far reservations go out together */
+    int pbase = 0, fbase = 0;
+    if (lane == 31) {
+      if (ptotal) pbase = wgm_out_reserve(o, ptotal);
+      if (PACK && ftotal) fbase = atomicAdd(o.far_cnt, ftotal);
+    }
     pbase = __shfl_sync(WGM_FULL, pbase, 31);
+    if (PACK && ftotal) {
+      fbase = __shfl_sync(WGM_FULL, fbase, 31);
+      int fs = fbase + fincl - fmine;
+      unsigned m = 0xffffffffu;
+      bool spill[K];
+#pragma unroll
+      for (int k = 0; k < K; k++) {
+        spill[k] = false;
+        if (fr[k]) {
+          if (fs < o.far_cap) {
+            o.far_list[fs] = u[k];
+            m = min(m, alt[k]);
+          } else {
+            spill[k] = true; /* far list full: relax it now instead */
+          }
+          fs++;
+        }
+      }
+#pragma unroll
+      for (int x = 16; x > 0; x >>= 1) m = min(m, __shfl_xor_sync(WGM_FULL, m, x));
+      if (lane == 0 && m != 0xffffffffu) atomicMin(o.far_min, m);
+#pragma unroll
+      for (int k = 0; k < K; k++)
+        if (__any_sync(WGM_FULL, spill[k]))
+          ok &= wgm_out_push_vertices(row, P, spill[k], u[k], o);
+    }
+    if (ptotal == 0) continue;
     if (pbase + ptotal > o.cap) {
       ok = false;
       continue;

@@ -251,6 +251,12 @@ int wgm_batch_team_info(wgm_batch *b, int64_t *team_edges, int *max_team);
  * vertices it just improved for up to `rounds` more rounds (0..12; 0 = plain
  * levels).  Both give the same distances; the autotuner picks. */
 int wgm_batch_configure_local(wgm_batch *b, int rounds);
+/* SSSP schedule (no reference counterpart; the reference's sssp.cl runs the
+ * Bellman-Ford worklist): near-far buckets of delta_mult x the graph's mean
+ * edge weight (default 20; 0 = the worklist), far lists of far_cap entries
+ * (0 = 2V + 64; a full list relaxes the vertex at once).  Distances are the
+ * same for every setting; only the work and the level count change. */
+int wgm_batch_configure_sssp(wgm_batch *b, double delta_mult, int far_cap);
 /* Queue one batched launch on the runtime's stream (use_cuda_graph: replay a
  * captured CUDA graph of the queue reset and the launch). */
 int wgm_batch_launch(wgm_batch *b, int use_cuda_graph);

@@ -79,6 +79,29 @@ def test_batch_teams(small_batch, team_edges, max_team, threads):
         assert np.all(st["levels"] >= 1)
 
 
+@pytest.mark.parametrize("mult,far_cap,team_edges", [(0, 0, 0), (20, 0, 0), (2, 0, 1500),
+                                                     (20, 3, 0), (5, 1, 800), (1e5, 0, 0)])
+def test_batch_sssp_schedules(small_batch, mult, far_cap, team_edges):
+    """Near-far SSSP (buckets of mult x the mean weight; 0 = the worklist),
+    on single CTAs and on teams, with far lists so small that most parked
+    vertices take the full-list path: every distance equals the oracle's,
+    across replays of the CUDA graph."""
+    gs, jobs = small_batch
+    want = _oracle(gs, jobs)
+    with Runtime() as rt, Batch(rt, gs, jobs) as b:
+        b.configure(256, 0, 0)
+        b.configure_local(0)
+        b.configure_teams(team_edges, 0)
+        b.configure_sssp(mult, far_cap)
+        for rep in range(3):
+            b.run(use_cuda_graph=rep > 0)
+            allres = b.results()
+            for k in range(len(jobs)):
+                assert np.array_equal(allres[b.offsets[k]:b.offsets[k + 1]], want[k]), (rep, k)
+        if team_edges:
+            assert b.job_stats()["team"].max() > 1
+
+
 def test_batch_edge_cases():
     # single vertex, isolated source, star hub, the Lonestar loader view
     one = graphs.Graph(np.array([0, 0], np.int32), np.zeros(0, np.int32), np.zeros(0, np.uint32))
@@ -102,6 +125,11 @@ def test_batch_edge_cases():
         b.run()
         for k in range(len(jobs)):
             assert np.array_equal(b.result(k), want[k]), ("teams", k)
+        for mult, cap in ((0.5, 2), (0, 0)):  # near-far with tiny buckets and far lists
+            b.configure_sssp(mult, cap)
+            b.run()
+            for k in range(len(jobs)):
+                assert np.array_equal(b.result(k), want[k]), ("near-far", mult, k)
 
 
 def test_batch_autotune_picks_a_valid_config(small_batch):
