@@ -130,6 +130,9 @@ _PROTOS = {
     "wgm_batch_team_info": (_I, [_P, _P, _P]),
     "wgm_batch_configure_local": (_I, [_P, _I]),
     "wgm_batch_configure_sssp": (_I, [_P, C.c_double, _I]),
+    "wgm_batch_sssp_info": (_I, [_P, _P, _P]),
+    "wgm_batch_submit_packed": (_I, [_P, _P, _P, _P, _P]),
+    "wgm_batch_wait": (_I, [_P]),
     "wgm_batch_upload_packed": (_I, [_P, _P, _P, _P]),
     "wgm_batch_graph_offsets": (_I, [_P, _P, _P]),
     "wgm_batch_job_stats": (_I, [_P, _P, _P, _P, _P]),

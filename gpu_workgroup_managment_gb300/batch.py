@@ -73,6 +73,19 @@ class Batch:
         check(lib.wgm_batch_upload_packed(self._h, rows.ctypes.data, cols.ctypes.data,
                                           wts.ctypes.data), "wgm_batch_upload_packed")
 
+    def submit_packed(self, rows: np.ndarray, cols: np.ndarray, wts: np.ndarray,
+                      out: np.ndarray) -> None:
+        """Queue one pipelined step (upload, launch, read-back into `out`);
+        the arrays must stay alive and untouched until wait()."""
+        if out.dtype != np.uint32 or out.shape[0] < int(self.offsets[-1]):
+            raise ValueError("out must hold every job's distances (uint32)")
+        check(lib.wgm_batch_submit_packed(self._h, rows.ctypes.data, cols.ctypes.data,
+                                          wts.ctypes.data, out.ctypes.data),
+              "wgm_batch_submit_packed")
+
+    def wait(self) -> None:
+        check(lib.wgm_batch_wait(self._h), "wgm_batch_wait")
+
     def configure(self, threads: int = 256, ctas_per_sm: int = 0, piece: int = 0) -> None:
         check(lib.wgm_batch_configure(self._h, threads, ctas_per_sm, piece), "batch_configure")
 
@@ -146,8 +159,10 @@ class Batch:
                                      C.byref(ms)), "wgm_batch_autotune")
         te, mt = C.c_int64(), C.c_int()
         check(lib.wgm_batch_team_info(self._h, C.byref(te), C.byref(mt)))
+        dm, fc = C.c_double(), C.c_int()
+        check(lib.wgm_batch_sssp_info(self._h, C.byref(dm), C.byref(fc)))
         return {"threads": t.value, "ctas_per_sm": c.value, "piece": p.value, "ms": ms.value,
-                "team_edges": te.value, "max_team": mt.value}
+                "team_edges": te.value, "max_team": mt.value, "sssp_delta_mult": dm.value}
 
     def close(self):
         if self._h:

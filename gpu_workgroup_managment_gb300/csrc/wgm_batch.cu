@@ -92,6 +92,17 @@ struct wgm_batch {
   int teams_grid = 0; /* grid the team sizes were computed for (0 = stale) */
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
+  /* pipelined submits: two arenas (graphs in, distances out) used in turn;
+   * arena 0 is the batch's own, arena 1 is allocated by the first submit */
+  struct arena {
+    int *rows = nullptr, *cols = nullptr;
+    unsigned *wts = nullptr, *dist = nullptr;
+  } ar[2];
+  cudaGraphExec_t pexec[2] = {nullptr, nullptr};
+  cudaStream_t s_up = nullptr, s_down = nullptr;
+  cudaEvent_t ev_up[2] = {}, ev_run[2] = {}, ev_down[2] = {};
+  bool used[2] = {false, false};
+  long long nsub = 0;
 };
 
 static void wgm_batch_free_graph(wgm_batch *b) {
@@ -99,6 +110,10 @@ static void wgm_batch_free_graph(wgm_batch *b) {
   if (b->graph) cudaGraphDestroy(b->graph);
   b->exec = nullptr;
   b->graph = nullptr;
+  for (int a = 0; a < 2; a++) {
+    if (b->pexec[a]) cudaGraphExecDestroy(b->pexec[a]);
+    b->pexec[a] = nullptr;
+  }
 }
 
 extern "C" int wgm_batch_destroy(wgm_batch *b) {
@@ -106,6 +121,19 @@ extern "C" int wgm_batch_destroy(wgm_batch *b) {
   cudaSetDevice(b->rt->device);
   cudaStreamSynchronize(b->rt->stream);
   wgm_batch_free_graph(b);
+  if (b->s_up) cudaStreamSynchronize(b->s_up);
+  if (b->s_down) cudaStreamSynchronize(b->s_down);
+  cudaFree(b->ar[1].rows);
+  cudaFree(b->ar[1].cols);
+  cudaFree(b->ar[1].wts);
+  cudaFree(b->ar[1].dist);
+  for (int a = 0; a < 2; a++) {
+    if (b->ev_up[a]) cudaEventDestroy(b->ev_up[a]);
+    if (b->ev_run[a]) cudaEventDestroy(b->ev_run[a]);
+    if (b->ev_down[a]) cudaEventDestroy(b->ev_down[a]);
+  }
+  if (b->s_up) cudaStreamDestroy(b->s_up);
+  if (b->s_down) cudaStreamDestroy(b->s_down);
   void *ptrs[] = {b->d_rows, b->d_cols, b->d_wts, b->d_dist, b->d_scratch, b->d_stamp,
                   b->d_levels, b->d_ctl, b->d_err, b->d_slots, b->d_jobs, b->d_cnt,
                   b->d_times};
@@ -264,11 +292,13 @@ extern "C" int wgm_batch_create(wgm_runtime *rt, int num_graphs, const wgm_graph
   return WGM_OK;
 }
 
+static cudaError_t wgm_batch_plain_fence(wgm_batch *b, cudaStream_t s);
+
 extern "C" int wgm_batch_upload(wgm_batch *b, const wgm_graph_desc *graphs) {
   if (!b || !graphs) return WGM_ERR_INVALID;
   cudaSetDevice(b->rt->device);
   cudaStream_t s = b->rt->stream;
-  cudaError_t e = cudaSuccess;
+  cudaError_t e = wgm_batch_plain_fence(b, s);
   b->gmeanw.assign(b->ngraphs, 1.0);
   for (int g = 0; g < b->ngraphs; g++) {
     const wgm_graph_desc &d = graphs[g];
@@ -311,8 +341,9 @@ extern "C" int wgm_batch_upload_packed(wgm_batch *b, const int32_t *rows, const 
   if (!b || !rows || (b->cols_total && !cols)) return WGM_ERR_INVALID;
   cudaSetDevice(b->rt->device);
   cudaStream_t s = b->rt->stream;
-  cudaError_t e = cudaMemcpyAsync(b->d_rows, rows, (size_t)b->rows_total * 4,
-                                  cudaMemcpyHostToDevice, s);
+  cudaError_t e = wgm_batch_plain_fence(b, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(b->d_rows, rows, (size_t)b->rows_total * 4, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess && b->cols_total)
     e = cudaMemcpyAsync(b->d_cols, cols, (size_t)b->cols_total * 4, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess && b->cols_total && weights && b->has_weights)
@@ -412,11 +443,20 @@ static int wgm_batch_check(wgm_batch *b) {
 }
 
 /* Enqueue one batched launch: clear the control block, launch. */
-static cudaError_t wgm_batch_enqueue(wgm_batch *b, int grid, cudaStream_t s) {
+/* Queue reset + batched kernel; arena 1 (pipelined submits) swaps in the
+ * second set of graph and distance buffers. */
+static cudaError_t wgm_batch_enqueue(wgm_batch *b, int grid, cudaStream_t s, int arena = 0) {
   cudaError_t e = cudaMemsetAsync(
       b->d_ctl, 0, (size_t)(1 + WGM_BATCH_CTL_LINES_PER_JOB * b->njobs) * WGM_LINE * 4, s);
   if (e != cudaSuccess) return e;
-  wgm_k_batch<<<grid, b->threads, wgm_batch_dyn_smem(b->threads), s>>>(wgm_batch_kargs(b));
+  wgm_batch_args B = wgm_batch_kargs(b);
+  if (arena == 1) {
+    B.rows = b->ar[1].rows;
+    B.cols = b->ar[1].cols;
+    B.wts = b->ar[1].wts;
+    B.dist = b->ar[1].dist;
+  }
+  wgm_k_batch<<<grid, b->threads, wgm_batch_dyn_smem(b->threads), s>>>(B);
   return cudaGetLastError();
 }
 
@@ -479,21 +519,49 @@ extern "C" int wgm_batch_configure_teams(wgm_batch *b, int64_t team_edges, int m
   return WGM_OK;
 }
 
+/* Grid size and team layout for the current configuration. */
+static int wgm_batch_prepare(wgm_batch *b, int *grid) {
+  int st = wgm_batch_grid(b, grid);
+  if (st) return st;
+  if (b->teams_grid != *grid) {
+    cudaStreamSynchronize(b->rt->stream);
+    wgm_batch_free_graph(b);
+    st = wgm_batch_teams(b, *grid);
+    if (st) return st;
+    b->teams_grid = *grid;
+  }
+  return WGM_OK;
+}
+
+/* A plain launch reuses arena 0: it waits for a pipelined upload or read-back
+ * of that arena still in flight, and marks its own use for later submits. */
+static cudaError_t wgm_batch_plain_fence(wgm_batch *b, cudaStream_t s) {
+  cudaError_t e = cudaSuccess;
+  if (b->s_up && b->used[0]) {
+    e = cudaStreamWaitEvent(s, b->ev_up[0], 0);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, b->ev_down[0], 0);
+  }
+  return e;
+}
+static cudaError_t wgm_batch_plain_mark(wgm_batch *b, cudaStream_t s) {
+  if (!b->s_up) return cudaSuccess;
+  b->used[0] = true;
+  cudaError_t e = cudaEventRecord(b->ev_run[0], s);
+  /* a later read-back of arena 0 must also wait for this launch */
+  if (e == cudaSuccess) e = cudaEventRecord(b->ev_down[0], s);
+  if (e == cudaSuccess) e = cudaEventRecord(b->ev_up[0], s);
+  return e;
+}
+
 extern "C" int wgm_batch_launch(wgm_batch *b, int use_cuda_graph) {
   if (!b) return WGM_ERR_INVALID;
   cudaSetDevice(b->rt->device);
   cudaStream_t s = b->rt->stream;
   int grid = 0;
-  int st = wgm_batch_grid(b, &grid);
+  int st = wgm_batch_prepare(b, &grid);
   if (st) return st;
-  if (b->teams_grid != grid) {
-    cudaStreamSynchronize(s);
-    wgm_batch_free_graph(b);
-    st = wgm_batch_teams(b, grid);
-    if (st) return st;
-    b->teams_grid = grid;
-  }
-  cudaError_t e;
+  cudaError_t e = wgm_batch_plain_fence(b, s);
+  if (e != cudaSuccess) return wgm_cuda_fail(b->rt, e);
   if (use_cuda_graph) {
     if (!b->exec) {
       /* capture once: queue reset + batched kernel */
@@ -511,8 +579,94 @@ extern "C" int wgm_batch_launch(wgm_batch *b, int use_cuda_graph) {
   } else {
     e = wgm_batch_enqueue(b, grid, s);
   }
+  if (e == cudaSuccess) e = wgm_batch_plain_mark(b, s);
   if (e != cudaSuccess) return wgm_cuda_fail(b->rt, e);
   return WGM_OK;
+}
+
+/* Pipelined form of upload_packed + launch + read_all.  Step k uses arena
+ * k & 1: its upload (stream s_up) waits only for the launch that last read
+ * that arena, its launch (the runtime's stream) for its upload and for the
+ * read-back that last emptied the arena's distances, its read-back (stream
+ * s_down) for its launch.  So the upload of step k+1 and the read-back of
+ * step k-1 run under the kernel of step k; every step still copies all of
+ * its graphs in and all of its distances out. */
+extern "C" int wgm_batch_submit_packed(wgm_batch *b, const int32_t *rows, const int32_t *cols,
+                                       const uint32_t *weights, uint32_t *out) {
+  if (!b || !rows || !out || (b->cols_total && !cols)) return WGM_ERR_INVALID;
+  cudaSetDevice(b->rt->device);
+  cudaStream_t s = b->rt->stream;
+  cudaError_t e = cudaSuccess;
+  if (!b->s_up) {
+    e = cudaStreamCreateWithFlags(&b->s_up, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->s_down, cudaStreamNonBlocking);
+    for (int a = 0; a < 2 && e == cudaSuccess; a++) {
+      e = cudaEventCreateWithFlags(&b->ev_up[a], cudaEventDisableTiming);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_run[a], cudaEventDisableTiming);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_down[a], cudaEventDisableTiming);
+    }
+    b->ar[0].rows = b->d_rows;
+    b->ar[0].cols = b->d_cols;
+    b->ar[0].wts = b->d_wts;
+    b->ar[0].dist = b->d_dist;
+    if (e == cudaSuccess) e = cudaMalloc((void **)&b->ar[1].rows, std::max(b->rows_total, 1LL) * 4);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&b->ar[1].cols, std::max(b->cols_total, 1LL) * 4);
+    if (e == cudaSuccess)
+      e = cudaMalloc((void **)&b->ar[1].wts, b->has_weights ? std::max(b->cols_total, 1LL) * 4 : 4);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&b->ar[1].dist, std::max(b->dist_total, 1LL) * 4);
+    /* arena 0's first submit must follow whatever the runtime's stream holds */
+    if (e == cudaSuccess) e = cudaEventRecord(b->ev_run[0], s);
+    if (e == cudaSuccess) e = cudaEventRecord(b->ev_down[0], s);
+    b->used[0] = true;
+    if (e != cudaSuccess) return wgm_cuda_fail(b->rt, e);
+  }
+  int grid = 0;
+  int st = wgm_batch_prepare(b, &grid);
+  if (st) return st;
+  const int a = (int)(b->nsub & 1);
+  if (!b->pexec[a]) {
+    cudaGraph_t g = nullptr;
+    e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) e = wgm_batch_enqueue(b, grid, s, a);
+    cudaError_t e2 = cudaStreamEndCapture(s, &g);
+    if (e == cudaSuccess) e = e2;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&b->pexec[a], g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (e != cudaSuccess) return wgm_cuda_fail(b->rt, e);
+  }
+  const wgm_batch::arena &A = b->ar[a];
+  if (b->used[a]) e = cudaStreamWaitEvent(b->s_up, b->ev_run[a], 0);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(A.rows, rows, (size_t)b->rows_total * 4, cudaMemcpyHostToDevice, b->s_up);
+  if (e == cudaSuccess && b->cols_total)
+    e = cudaMemcpyAsync(A.cols, cols, (size_t)b->cols_total * 4, cudaMemcpyHostToDevice, b->s_up);
+  if (e == cudaSuccess && b->cols_total && weights && b->has_weights)
+    e = cudaMemcpyAsync(A.wts, weights, (size_t)b->cols_total * 4, cudaMemcpyHostToDevice,
+                        b->s_up);
+  if (e == cudaSuccess) e = cudaEventRecord(b->ev_up[a], b->s_up);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(s, b->ev_up[a], 0);
+  if (e == cudaSuccess && b->used[a]) e = cudaStreamWaitEvent(s, b->ev_down[a], 0);
+  if (e == cudaSuccess) e = cudaGraphLaunch(b->pexec[a], s);
+  if (e == cudaSuccess) e = cudaEventRecord(b->ev_run[a], s);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(b->s_down, b->ev_run[a], 0);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(out, A.dist, (size_t)b->dist_total * 4, cudaMemcpyDeviceToHost,
+                        b->s_down);
+  if (e == cudaSuccess) e = cudaEventRecord(b->ev_down[a], b->s_down);
+  if (e != cudaSuccess) return wgm_cuda_fail(b->rt, e);
+  b->used[a] = true;
+  b->nsub++;
+  return WGM_OK;
+}
+
+extern "C" int wgm_batch_wait(wgm_batch *b) {
+  if (!b) return WGM_ERR_INVALID;
+  cudaSetDevice(b->rt->device);
+  cudaError_t e = cudaStreamSynchronize(b->rt->stream);
+  if (e == cudaSuccess && b->s_up) e = cudaStreamSynchronize(b->s_up);
+  if (e == cudaSuccess && b->s_down) e = cudaStreamSynchronize(b->s_down);
+  if (e != cudaSuccess) return wgm_cuda_fail(b->rt, e);
+  return wgm_batch_check(b);
 }
 
 extern "C" int wgm_batch_run(wgm_batch *b, int use_cuda_graph, double *device_ms) {
@@ -726,6 +880,24 @@ extern "C" int wgm_batch_autotune(wgm_batch *b, int reps, int *best_threads,
   }
   int s = wgm_batch_configure_local(b, blq);
   if (s) return s;
+  /* 4b. near-far bucket width (packed SSSP runs without local rounds) */
+  if (blq == 0) {
+    const double m0 = b->nf_mult;
+    double bm = m0;
+    for (double m : {m0 * 0.5, m0 * 2.0}) {
+      if (m0 <= 0) break;
+      s = wgm_batch_configure_sssp(b, m, b->far_cap_cfg);
+      double ms = 0;
+      if (!s) s = point(bt, bc, bp, bte, &ms);
+      if (s) return s;
+      if (ms < best) {
+        best = ms;
+        bm = m;
+      }
+    }
+    s = wgm_batch_configure_sssp(b, bm, b->far_cap_cfg);
+    if (s) return s;
+  }
   /* 5. critical path: the jobs that run longest double their team, while
    * that shortens the launch */
   s = point(bt, bc, bp, bte, &best);
@@ -842,6 +1014,13 @@ extern "C" int wgm_batch_configure_local(wgm_batch *b, int rounds) {
   cudaStreamSynchronize(b->rt->stream);
   b->lq_rounds = rounds;
   wgm_batch_free_graph(b);
+  return WGM_OK;
+}
+
+extern "C" int wgm_batch_sssp_info(wgm_batch *b, double *delta_mult, int *far_cap) {
+  if (!b) return WGM_ERR_INVALID;
+  if (delta_mult) *delta_mult = b->nf_mult;
+  if (far_cap) *far_cap = b->far_cap_cfg;
   return WGM_OK;
 }
 

@@ -257,6 +257,7 @@ int wgm_batch_configure_local(wgm_batch *b, int rounds);
  * (0 = 2V + 64; a full list relaxes the vertex at once).  Distances are the
  * same for every setting; only the work and the level count change. */
 int wgm_batch_configure_sssp(wgm_batch *b, double delta_mult, int far_cap);
+int wgm_batch_sssp_info(wgm_batch *b, double *delta_mult, int *far_cap);
 /* Queue one batched launch on the runtime's stream (use_cuda_graph: replay a
  * captured CUDA graph of the queue reset and the launch). */
 int wgm_batch_launch(wgm_batch *b, int use_cuda_graph);
@@ -264,6 +265,17 @@ int wgm_batch_run(wgm_batch *b, int use_cuda_graph, double *device_ms);
 /* The plain form for comparison: one standalone persistent launch per job. */
 int wgm_batch_launch_per_graph(wgm_batch *b);
 int wgm_batch_run_per_graph(wgm_batch *b, double *device_ms);
+/* Pipelined batches (no reference counterpart): upload_packed + launch +
+ * read_all of one step, queued without waiting.  Steps alternate between two
+ * device copies of the graphs and distances, so the upload of step k+1 and
+ * the read-back of step k-1 overlap the kernel of step k; every step copies
+ * all of its graphs in and all of its distances into `out` (dist_total
+ * values in the caller's job order).  Host buffers should be pinned, and
+ * stay untouched until wgm_batch_wait returns.  The second device copy is
+ * allocated by the first submit. */
+int wgm_batch_submit_packed(wgm_batch *b, const int32_t *rows, const int32_t *cols,
+                            const uint32_t *weights, uint32_t *out);
+int wgm_batch_wait(wgm_batch *b);
 int wgm_batch_read(wgm_batch *b, int job, uint32_t *out, int64_t n);
 int wgm_batch_read_all(wgm_batch *b, uint32_t *out, int64_t n);
 /* Per job (caller's order) of the last batched launch: device start and end

@@ -143,3 +143,46 @@ def test_batch_autotune_picks_a_valid_config(small_batch):
         b.run()
         for k in range(len(jobs)):
             assert np.array_equal(b.result(k), want[k]), k
+
+
+def test_batch_pipelined_submits(small_batch):
+    """submit_packed/wait: steps alternate between two device copies; each
+    step's distances land in its own host buffer and equal the oracle's for
+    the weights that step uploaded (two weight sets, interleaved)."""
+    from gpu_workgroup_managment_gb300.runtime import pinned_copy
+    from gpu_workgroup_managment_gb300._lib import lib
+    gs, jobs = small_batch
+    want_a = _oracle(gs, jobs)
+    gs_b = []
+    for i, g in enumerate(gs):
+        h = graphs.Graph(g.row_ptr, g.col, graphs.uniform_weights(g, 900 + i))
+        gs_b.append(h)
+    want_b = _oracle(gs_b, jobs)
+    with Runtime() as rt, Batch(rt, gs, jobs) as b:
+        ra, ca, wa = b.pack(gs)
+        rb, cb, wb = b.pack(gs_b)
+        bufs, keep = [], []
+        for arr in (ra, ca, wa, rb, cb, wb):
+            x, p = pinned_copy(arr)
+            bufs.append(x)
+            keep.append(p)
+        outs = []
+        for k in range(5):
+            o, p = pinned_copy(np.zeros(int(b.offsets[-1]), np.uint32))
+            outs.append(o)
+            keep.append(p)
+        for k in range(5):
+            src = bufs[:3] if k % 2 == 0 else bufs[3:]
+            b.submit_packed(*src, outs[k])
+        b.wait()
+        for k in range(5):
+            want = want_a if k % 2 == 0 else want_b
+            for j in range(len(jobs)):
+                assert np.array_equal(outs[k][b.offsets[j]:b.offsets[j + 1]], want[j]), (k, j)
+        # a plain launch after pipelined steps uses the first copy again
+        b.upload(gs_b)
+        b.run()
+        for j in range(len(jobs)):
+            assert np.array_equal(b.result(j), want_b[j]), ("plain", j)
+        for p in keep:
+            lib.wgm_host_free(p)
