@@ -131,6 +131,8 @@ _PROTOS = {
     "wgm_batch_configure_local": (_I, [_P, _I]),
     "wgm_batch_configure_sssp": (_I, [_P, C.c_double, _I]),
     "wgm_batch_sssp_info": (_I, [_P, _P, _P]),
+    "wgm_batch_configure_kernel": (_I, [_P, _I]),
+    "wgm_batch_kernel_info": (_I, [_P, _P]),
     "wgm_batch_submit_packed": (_I, [_P, _P, _P, _P, _P]),
     "wgm_batch_wait": (_I, [_P]),
     "wgm_batch_upload_packed": (_I, [_P, _P, _P, _P]),

@@ -89,6 +89,10 @@ class Batch:
     def configure(self, threads: int = 256, ctas_per_sm: int = 0, piece: int = 0) -> None:
         check(lib.wgm_batch_configure(self._h, threads, ctas_per_sm, piece), "batch_configure")
 
+    def configure_kernel(self, max_regs: int) -> None:
+        """Register budget of the batched kernel: 64, 80 or 96 per thread."""
+        check(lib.wgm_batch_configure_kernel(self._h, int(max_regs)), "configure_kernel")
+
     def configure_teams(self, team_edges: int = 0, max_team: int = 0) -> None:
         """A job of E edges runs on ceil(E / team_edges) CTAs, at most max_team
         (0 = defaults: total edges / grid, a quarter of the grid)."""
@@ -159,10 +163,12 @@ class Batch:
                                      C.byref(ms)), "wgm_batch_autotune")
         te, mt = C.c_int64(), C.c_int()
         check(lib.wgm_batch_team_info(self._h, C.byref(te), C.byref(mt)))
-        dm, fc = C.c_double(), C.c_int()
+        dm, fc, rg = C.c_double(), C.c_int(), C.c_int()
         check(lib.wgm_batch_sssp_info(self._h, C.byref(dm), C.byref(fc)))
+        check(lib.wgm_batch_kernel_info(self._h, C.byref(rg)))
         return {"threads": t.value, "ctas_per_sm": c.value, "piece": p.value, "ms": ms.value,
-                "team_edges": te.value, "max_team": mt.value, "sssp_delta_mult": dm.value}
+                "team_edges": te.value, "max_team": mt.value, "sssp_delta_mult": dm.value,
+                "max_regs": rg.value}
 
     def close(self):
         if self._h:

@@ -19,7 +19,13 @@
 #include "wgm_internal.h"
 #include "wgm_kernels.cuh"
 
-__global__ void __launch_bounds__(1024) wgm_k_batch(wgm_batch_args B) {
+/* The batched kernel under three register budgets: launch bounds of 1024,
+ * 768 and 640 threads let ptxas use 64, 80 and 96 registers per thread.
+ * At 64 the K-window walkers spill (hundreds of MB of local-memory traffic
+ * per launch); at 96 nothing spills but fewer warps fit on an SM.  The
+ * autotuner picks (wgm_batch_configure_kernel). */
+template <int MAXT>
+__global__ void __launch_bounds__(MAXT) wgm_k_batch(wgm_batch_args B) {
   __shared__ wgm_warp_smem sm;
   extern __shared__ wgm_lq wgm_lqs[]; /* one local queue per warp */
   wgm_lq *q = &wgm_lqs[threadIdx.x >> 5];
@@ -59,6 +65,24 @@ __global__ void __launch_bounds__(1024) wgm_k_batch(wgm_batch_args B) {
 /* Dynamic shared memory of a launch: one local queue per warp. */
 static size_t wgm_batch_dyn_smem(int threads) { return (size_t)(threads / 32) * sizeof(wgm_lq); }
 
+static const int wgm_batch_kmax[3] = {1024, 768, 640};   /* threads per CTA */
+static const int wgm_batch_kregs[3] = {64, 80, 96};      /* register budget */
+static const void *wgm_batch_kfn(int v) {
+  switch (v) {
+    case 1: return (const void *)wgm_k_batch<768>;
+    case 2: return (const void *)wgm_k_batch<640>;
+    default: return (const void *)wgm_k_batch<1024>;
+  }
+}
+static int wgm_batch_per_sm(int v, int threads) {
+  int per_sm = 0;
+  if (threads > wgm_batch_kmax[v] ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wgm_batch_kfn(v), threads,
+                                                    wgm_batch_dyn_smem(threads)) != cudaSuccess)
+    return 0;
+  return per_sm;
+}
+
 struct wgm_batch {
   wgm_runtime *rt = nullptr;
   int ngraphs = 0, njobs = 0;
@@ -82,6 +106,7 @@ struct wgm_batch {
             stamp_total = 0;
   bool has_weights = false;
   int threads = 256, ctas_per_sm = 0, piece = 0;
+  int kvar = 0; /* register budget of the kernel: wgm_batch_kregs[kvar] */
   int lq_rounds = 0; /* warp-local continuation rounds per level (0: off) */
   /* SSSP near-far schedule: bucket width = nf_mult x the graph's mean edge
    * weight (0: the Bellman-Ford worklist); far lists of far_cap_cfg entries
@@ -383,11 +408,7 @@ static wgm_batch_args wgm_batch_kargs(wgm_batch *b) {
 }
 
 static int wgm_batch_grid(wgm_batch *b, int *grid) {
-  int per_sm = 0;
-  cudaError_t e =
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wgm_k_batch, b->threads,
-                                                    wgm_batch_dyn_smem(b->threads));
-  if (e != cudaSuccess) return wgm_cuda_fail(b->rt, e);
+  const int per_sm = wgm_batch_per_sm(b->kvar, b->threads);
   if (per_sm < 1) return WGM_ERR_INVALID;
   int k = b->ctas_per_sm > 0 ? std::min(b->ctas_per_sm, per_sm) : per_sm;
   *grid = k * b->rt->prop.multiProcessorCount;
@@ -456,7 +477,12 @@ static cudaError_t wgm_batch_enqueue(wgm_batch *b, int grid, cudaStream_t s, int
     B.wts = b->ar[1].wts;
     B.dist = b->ar[1].dist;
   }
-  wgm_k_batch<<<grid, b->threads, wgm_batch_dyn_smem(b->threads), s>>>(B);
+  const size_t smem = wgm_batch_dyn_smem(b->threads);
+  switch (b->kvar) {
+    case 1: wgm_k_batch<768><<<grid, b->threads, smem, s>>>(B); break;
+    case 2: wgm_k_batch<640><<<grid, b->threads, smem, s>>>(B); break;
+    default: wgm_k_batch<1024><<<grid, b->threads, smem, s>>>(B); break;
+  }
   return cudaGetLastError();
 }
 
@@ -483,6 +509,8 @@ extern "C" int wgm_batch_configure(wgm_batch *b, int threads_per_cta, int ctas_p
   cudaSetDevice(b->rt->device);
   cudaStreamSynchronize(b->rt->stream);
   bool relayout = piece != b->piece;
+  /* a block larger than the variant's launch bounds needs the 64-register build */
+  if (threads_per_cta > wgm_batch_kmax[b->kvar]) b->kvar = 0;
   b->threads = threads_per_cta;
   b->ctas_per_sm = ctas_per_sm;
   b->piece = piece;
@@ -807,8 +835,7 @@ extern "C" int wgm_batch_autotune(wgm_batch *b, int reps, int *best_threads,
     return s;
   };
   auto grid_of = [&](int t, int c) {
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wgm_k_batch, t, wgm_batch_dyn_smem(t));
+    int per_sm = wgm_batch_per_sm(b->kvar, t);
     if (c > 0) per_sm = std::min(per_sm, c);
     return std::max(1, per_sm * b->rt->prop.multiProcessorCount);
   };
@@ -828,32 +855,33 @@ extern "C" int wgm_batch_autotune(wgm_batch *b, int reps, int *best_threads,
   }
   /* 2. shape at that team size (team_edges scaled with the grid) */
   const double per_cta = (double)bte * grid_of(256, 0);
-  for (int t : threads_set) {
-    int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wgm_k_batch, t,
-                                                      wgm_batch_dyn_smem(t)) !=
-            cudaSuccess ||
-        per_sm < 1)
-      continue;
-    std::vector<int> ctas;
-    for (int c = 1; c < per_sm; c *= 2) ctas.push_back(c);
-    ctas.push_back(per_sm);
-    for (int c : ctas) {
-      for (int p : piece_set) {
-        long long te = std::max(1LL << 12, (long long)(per_cta / grid_of(t, c)));
-        double ms = 0;
-        int s = point(t, c, p, te, &ms);
-        if (s) return s;
-        if (ms < best) {
-          best = ms;
-          bt = t;
-          bc = c;
-          bp = p;
-          bte = te;
+  int bv = b->kvar;
+  for (int v = 0; v < 3; v++)
+    for (int t : threads_set) {
+      const int per_sm = wgm_batch_per_sm(v, t);
+      if (per_sm < 1) continue;
+      b->kvar = v;
+      std::vector<int> ctas;
+      for (int c = std::max(1, per_sm / 2); c < per_sm; c *= 2) ctas.push_back(c);
+      ctas.push_back(per_sm);
+      for (int c : ctas) {
+        for (int p : piece_set) {
+          long long te = std::max(1LL << 12, (long long)(per_cta / grid_of(t, c)));
+          double ms = 0;
+          int s = point(t, c, p, te, &ms);
+          if (s) return s;
+          if (ms < best) {
+            best = ms;
+            bt = t;
+            bc = c;
+            bp = p;
+            bte = te;
+            bv = v;
+          }
         }
       }
     }
-  }
+  b->kvar = bv;
   /* 3. team size again at the winning shape */
   const long long base = bte;
   for (double f : {0.5, 0.75, 1.5, 2.0}) {
@@ -1014,6 +1042,26 @@ extern "C" int wgm_batch_configure_local(wgm_batch *b, int rounds) {
   cudaStreamSynchronize(b->rt->stream);
   b->lq_rounds = rounds;
   wgm_batch_free_graph(b);
+  return WGM_OK;
+}
+
+extern "C" int wgm_batch_configure_kernel(wgm_batch *b, int max_regs) {
+  if (!b) return WGM_ERR_INVALID;
+  int v = -1;
+  for (int k = 0; k < 3; k++)
+    if (wgm_batch_kregs[k] == max_regs) v = k;
+  if (v < 0 || b->threads > wgm_batch_kmax[v]) return WGM_ERR_INVALID;
+  cudaSetDevice(b->rt->device);
+  cudaStreamSynchronize(b->rt->stream);
+  b->kvar = v;
+  b->teams_grid = 0;
+  wgm_batch_free_graph(b);
+  return WGM_OK;
+}
+
+extern "C" int wgm_batch_kernel_info(wgm_batch *b, int *max_regs) {
+  if (!b) return WGM_ERR_INVALID;
+  if (max_regs) *max_regs = wgm_batch_kregs[b->kvar];
   return WGM_OK;
 }
 

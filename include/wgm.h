@@ -258,6 +258,11 @@ int wgm_batch_configure_local(wgm_batch *b, int rounds);
  * same for every setting; only the work and the level count change. */
 int wgm_batch_configure_sssp(wgm_batch *b, double delta_mult, int far_cap);
 int wgm_batch_sssp_info(wgm_batch *b, double *delta_mult, int *far_cap);
+/* Register budget of the batched kernel (no reference counterpart): 64, 80
+ * or 96 registers per thread (blocks of at most 1024, 768, 640 threads);
+ * fewer registers fit more warps on an SM, more avoid spilling. */
+int wgm_batch_configure_kernel(wgm_batch *b, int max_regs);
+int wgm_batch_kernel_info(wgm_batch *b, int *max_regs);
 /* Queue one batched launch on the runtime's stream (use_cuda_graph: replay a
  * captured CUDA graph of the queue reset and the launch). */
 int wgm_batch_launch(wgm_batch *b, int use_cuda_graph);

@@ -102,6 +102,23 @@ def test_batch_sssp_schedules(small_batch, mult, far_cap, team_edges):
             assert b.job_stats()["team"].max() > 1
 
 
+@pytest.mark.parametrize("regs,threads", [(64, 1024), (80, 768), (96, 640), (96, 128)])
+def test_batch_register_budgets(small_batch, regs, threads):
+    """The kernel built for 64, 80 and 96 registers per thread, at the
+    largest block each allows: identical results."""
+    gs, jobs = small_batch
+    want = _oracle(gs, jobs)
+    with Runtime() as rt, Batch(rt, gs, jobs) as b:
+        b.configure(threads, 0, 0)
+        b.configure_kernel(regs)
+        b.configure_local(0)
+        b.configure_teams(3000, 0)
+        for rep in range(2):
+            b.run(use_cuda_graph=rep > 0)
+            for k in range(len(jobs)):
+                assert np.array_equal(b.result(k), want[k]), (rep, k)
+
+
 def test_batch_edge_cases():
     # single vertex, isolated source, star hub, the Lonestar loader view
     one = graphs.Graph(np.array([0, 0], np.int32), np.zeros(0, np.int32), np.zeros(0, np.uint32))
@@ -140,6 +157,7 @@ def test_batch_autotune_picks_a_valid_config(small_batch):
         best = b.autotune(reps=1)
         # piece 0 = each graph's own max(32, E/V)
         assert best["threads"] in (128, 256, 512) and best["piece"] in (0, 16, 32, 64)
+        assert best["max_regs"] in (64, 80, 96)
         b.run()
         for k in range(len(jobs)):
             assert np.array_equal(b.result(k), want[k]), k
