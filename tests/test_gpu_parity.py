@@ -258,3 +258,36 @@ def test_invalid_inputs_rejected(rt):
             a.set_source(g.num_nodes)
     with pytest.raises(WgmError):
         PersistentApp(rt, "lonestar_sssp", graphs.Graph(g.row_ptr, g.col, None))
+
+
+def _drop_edges(g, keep_frac, seed):
+    """A directed graph: every edge of g kept with probability keep_frac."""
+    rng = np.random.default_rng(seed)
+    src = np.repeat(np.arange(g.num_nodes), np.diff(g.row_ptr))
+    keep = rng.random(g.num_edges) < keep_frac
+    rp = np.zeros(g.num_nodes + 1, np.int32)
+    rp[1:] = np.cumsum(np.bincount(src[keep], minlength=g.num_nodes))
+    return graphs.Graph(rp, g.col[keep].astype(np.int32))
+
+
+@pytest.mark.parametrize("kind", ["symmetric", "directed", "unsorted"])
+def test_color_graph_shapes(kind):
+    """Colour on a symmetric RMAT with hubs, on a directed subgraph (the
+    in-edge transpose differs from the rows) and on the symmetric graph with
+    shuffled rows (its transpose is uploaded instead of shared): the
+    oracle's colours, with and without the hub pass."""
+    g = graphs.rmat(13, 8, seed=21)
+    if kind == "directed":
+        g = _drop_edges(g, 0.7, 4)
+    elif kind == "unsorted":
+        rng = np.random.default_rng(5)
+        col = g.col.copy()
+        for v in range(g.num_nodes):
+            seg = col[g.row_ptr[v]:g.row_ptr[v + 1]]
+            rng.shuffle(seg)
+        g = graphs.Graph(g.row_ptr, col)
+    nv = graphs.seeded_node_values(g.num_nodes, 17)
+    for cfg in (dict(), dict(hub_threshold=16)):
+        with Runtime(**cfg) as r, PersistentApp(r, "color", g, node_values=nv) as a:
+            a.run()
+            assert np.array_equal(a.result(), oracle.color(g, nv)), (kind, cfg)
