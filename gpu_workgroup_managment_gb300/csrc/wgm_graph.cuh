@@ -607,7 +607,8 @@ struct wgm_color_args {
   int hub_threshold;
   int *rounds_out;
   int *pending;  /* [V] larger out-neighbours not yet coloured */
-  int *wl_start, *wl_cnt, *wl_u; /* [2][cap] frontier pieces of in-edges */
+  int *wl_start, *wl_cnt, *wl_u; /* [2][cap] frontier pieces of in-edges; wl_u holds
+                                    the value bits of the piece's vertex */
   int cap, piece;
   int *cnt;      /* [3 lines] frontier sizes by round mod 3 */
 };
@@ -628,10 +629,15 @@ struct wgm_color_args {
  * once per round.
  * Phases: (0) init; (3,0) count larger out-neighbours; (4,0) round-1
  * frontier; (1,r) the vertices coloured r release their in-neighbours. */
-template <class Rel>
+/* pre(w, src, &tag) tests an in-neighbour w without side effects and sets
+ * the word its queue entry will carry; commit(w) claims it (true: queue
+ * it).  The in-edge row bounds of every w that passes `pre` are loaded
+ * beside `commit`'s atomic, not after it. */
+template <class Pre, class Commit>
 __device__ __forceinline__ bool wgm_frontier_chunk(const int *trow, const int *tcol, int P,
                                                    int start, int deg, unsigned sv,
-                                                   const wgm_ls_out &o, Rel &&rel) {
+                                                   const wgm_ls_out &o, Pre &&pre,
+                                                   Commit &&commit) {
   constexpr int K = WGM_LS_K;
   const int lane = wgm_lane();
   const int incl = wgm_warp_incl_scan(deg);
@@ -640,7 +646,7 @@ __device__ __forceinline__ bool wgm_frontier_chunk(const int *trow, const int *t
   const int base = start - off;
   bool ok = true;
   for (int w = 0; w < total; w += 32 * K) {
-    int u[K], rs[K], d[K], np[K];
+    int u[K], rs[K], d[K], np[K], tg[K];
     unsigned src[K];
     bool f[K];
 #pragma unroll
@@ -654,14 +660,17 @@ __device__ __forceinline__ bool wgm_frontier_chunk(const int *trow, const int *t
     }
 #pragma unroll
     for (int k = 0; k < K; k++) {
+      tg[k] = 0;
+      f[k] = f[k] && pre(u[k], src[k], &tg[k]);
+    }
+#pragma unroll
+    for (int k = 0; k < K; k++) {
       rs[k] = 0;
       d[k] = 0;
       if (f[k]) {
-        f[k] = rel(u[k], src[k]);
-        if (f[k]) {
-          rs[k] = __ldg(&trow[u[k]]);
-          d[k] = __ldg(&trow[u[k] + 1]);
-        }
+        rs[k] = __ldg(&trow[u[k]]);
+        d[k] = __ldg(&trow[u[k] + 1]);
+        f[k] = commit(u[k]);
       }
     }
     int mine = 0;
@@ -690,7 +699,7 @@ __device__ __forceinline__ bool wgm_frontier_chunk(const int *trow, const int *t
         for (int q = 0; q < np[k]; q++) {
           o.o_start[slot + q] = rs[k] + q * P;
           o.o_cnt[slot + q] = min(P, d[k] - q * P);
-          o.o_u[slot + q] = u[k];
+          o.o_u[slot + q] = tg[k];
         }
       }
       slot += np[k];
@@ -702,7 +711,7 @@ __device__ __forceinline__ bool wgm_frontier_chunk(const int *trow, const int *t
         const int j = __ffs(big) - 1;
         big &= big - 1;
         const int bs = __shfl_sync(WGM_FULL, rs[k], j), bd = __shfl_sync(WGM_FULL, d[k], j);
-        const int bu = __shfl_sync(WGM_FULL, u[k], j), bsl = __shfl_sync(WGM_FULL, sl[k], j);
+        const int bu = __shfl_sync(WGM_FULL, tg[k], j), bsl = __shfl_sync(WGM_FULL, sl[k], j);
         const int bn = (bd + P - 1) / P;
         for (int q = lane; q < bn; q += 32) {
           o.o_start[bsl + q] = bs + q * P;
@@ -716,9 +725,9 @@ __device__ __forceinline__ bool wgm_frontier_chunk(const int *trow, const int *t
 }
 
 /* Queue the in-edge pieces of the lanes' flagged vertices (one vertex per
- * lane, the whole warp writes). */
+ * lane, the whole warp writes); the entries carry `tag`. */
 __device__ __forceinline__ bool wgm_frontier_push(const int *trow, int P, bool flag, int v,
-                                                  const wgm_ls_out &o, int *tab) {
+                                                  int tag, const wgm_ls_out &o, int *tab) {
   int start = 0, deg = 0, np = 0;
   if (flag) {
     start = __ldg(&trow[v]);
@@ -736,7 +745,7 @@ __device__ __forceinline__ bool wgm_frontier_push(const int *trow, int P, bool f
   wgm_for_each_edge(off, np, -off, total, 0, 32, tab, [&](bool valid, int k, int owner) {
     int s = __shfl_sync(WGM_FULL, start, owner);
     int d = __shfl_sync(WGM_FULL, deg, owner);
-    int x = __shfl_sync(WGM_FULL, v, owner);
+    int x = __shfl_sync(WGM_FULL, tag, owner);
     int oo = __shfl_sync(WGM_FULL, off, owner);
     if (valid) {
       int slot = base + oo + k;
@@ -823,8 +832,12 @@ static __device__ int wgm_phase_color(const wgm_launch &Lc, wgm_cta *c, const wg
     for (int b = s.gw * 32; b < V; b += s.NW * 32) {
       const int i = b + lane;
       const bool f = i < V && __ldcg(&a.pending[i]) == 0;
-      if (f) a.color[i] = 1;
-      ok &= wgm_frontier_push(a.trow, a.piece, f, i, o, sm->tab[warp]);
+      int tag = 0;
+      if (f) {
+        a.color[i] = 1;
+        tag = __float_as_int(__ldg(&a.node_value[i]));
+      }
+      ok &= wgm_frontier_push(a.trow, a.piece, f, i, tag, o, sm->tab[warp]);
     }
     if (!ok) wgm_fail(Lc, WGM_DEV_OVERFLOW, WGM_SITE_QUEUE, 1);
     *nxt = {1, 1};
@@ -856,16 +869,21 @@ static __device__ int wgm_phase_color(const wgm_launch &Lc, wgm_cta *c, const wg
     if (lane < per && i < n) {
       start = __ldcg(&a.wl_start[io + i]);
       deg = __ldcg(&a.wl_cnt[io + i]);
-      sv = __float_as_uint(__ldg(&a.node_value[__ldcg(&a.wl_u[io + i])]));
+      sv = (unsigned)__ldcg(&a.wl_u[io + i]); /* the coloured vertex's value bits */
     }
-    ok &= wgm_frontier_chunk(a.trow, a.tcol, a.piece, start, deg, sv, o,
-                             [&](int w, unsigned src) {
-                               /* w has the coloured vertex as a larger out-neighbour */
-                               if (!(__ldg(&a.node_value[w]) < __uint_as_float(src))) return false;
-                               if (atomicSub(&a.pending[w], 1) != 1) return false;
-                               a.color[w] = next_colour;
-                               return true;
-                             });
+    ok &= wgm_frontier_chunk(
+        a.trow, a.tcol, a.piece, start, deg, sv, o,
+        [&](int w, unsigned src, int *tag) {
+          /* w has the coloured vertex as a larger out-neighbour */
+          const float vw = __ldg(&a.node_value[w]);
+          *tag = __float_as_int(vw);
+          return vw < __uint_as_float(src);
+        },
+        [&](int w) {
+          if (atomicSub(&a.pending[w], 1) != 1) return false;
+          a.color[w] = next_colour;
+          return true;
+        });
   }
   if (!ok) wgm_fail(Lc, WGM_DEV_OVERFLOW, WGM_SITE_QUEUE, r);
   *nxt = {1, r + 1};
