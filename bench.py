@@ -251,6 +251,21 @@ def _sssp_rmat(rt, scale: int, steps: int, warmup: int) -> dict:
             "bytes_alg": 12 * et + 36 * vr + 8 * g.num_nodes}
 
 
+def _octree(rt) -> dict:
+    """The work-stealing octree build at the reference's defaults
+    (octree.h: 3,000,000 particles, maxChildren 5, pool size 50,000):
+    standalone persistent launches, CUDA events, best of 3 after a warm-up,
+    the reference's check on the last one."""
+    from gpu_workgroup_managment_gb300.octree import Octree, clustered_particles
+    pts = clustered_particles(3_000_000, seed=1)
+    with Octree(rt, pts) as oc:
+        oc.run()
+        runs = [oc.run() for _ in range(3)]
+        _, done, tasks = oc.tree()
+        return {"particles": oc.n, "ms": min(r.kernel_ms for r in runs), "tasks": tasks,
+                "groups": runs[0].groups, "check": oc.check()}
+
+
 def _sssp_kernel_only(args) -> int:
     """The command profiled with ncu for the persistent SSSP kernel."""
     from gpu_workgroup_managment_gb300 import Runtime
@@ -474,6 +489,10 @@ def main() -> int:
         extra["barrier_ctas_1024_threads"] = bb["groups"]
         extra["barrier_kind_1024_threads"] = "sense" if bb["groups"] > 384 else "count"
         extra["sssp_rmat20"] = _sssp_rmat(rt, 20, 5, 3)
+        try:
+            extra["octree"] = _octree(rt)
+        except Exception as exc:  # reported, not hidden
+            extra["octree"] = {"error": repr(exc)}
         try:
             extra["served"] = _served(rt)
         except Exception as exc:  # reported, not hidden

@@ -10,6 +10,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <cstring>
 #include <new>
 #include <vector>
@@ -27,6 +28,7 @@ int wgm_kind_to_kernel(int kind) {
     case WGM_APP_PANNOTIA_MIS: return WGM_K_MIS;
     case WGM_APP_PANNOTIA_SSSP: return WGM_K_PSSSP;
     case WGM_APP_PAGERANK: return WGM_K_PAGERANK;
+    case WGM_APP_OCTREE: return WGM_K_OCTREE;
     default: return -1;
   }
 }
@@ -39,6 +41,7 @@ extern "C" const char *wgm_persistent_app_name(int kind) {
     case WGM_APP_PANNOTIA_MIS: return "mis";            /* mis.h:23 */
     case WGM_APP_PANNOTIA_SSSP: return "sssp";          /* pannotia sssp.h:25 */
     case WGM_APP_PAGERANK: return "pagerank";
+    case WGM_APP_OCTREE: return "octree";               /* octree.h:79 */
     default: return nullptr;
   }
 }
@@ -51,6 +54,7 @@ extern "C" const char *wgm_persistent_kernel_name(int kind) {
     case WGM_APP_PANNOTIA_MIS: return "mis_combined";
     case WGM_APP_PANNOTIA_SSSP: return "sssp_combined";
     case WGM_APP_PAGERANK: return "pagerank_pull";
+    case WGM_APP_OCTREE: return "octree_main";          /* octree.h:85 */
     default: return nullptr;
   }
 }
@@ -133,7 +137,9 @@ static void wgm_app_free_buffers(wgm_app *a) {
                   a->d_wl_start, a->d_wl_cnt,   a->d_wl_u,
                   a->d_cnt,       a->d_stamp,   a->d_stop,       a->d_hub_acc,
                   a->d_status,  a->d_contrib,   a->d_dang,    a->d_hub_sum,    a->d_rounds,
-                  a->hubs.ids,  a->hubs.prefix, a->hubs.wmap, a->d_trow, a->d_tcol};
+                  a->hubs.ids,  a->hubs.prefix, a->hubs.wmap, a->d_trow, a->d_tcol,
+                  a->d_oct_input, a->d_oct_second, a->d_oct_pools, a->d_oct_tree,
+                  a->d_oct_ctr, a->d_oct_locks, a->d_oct_heads};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   a->hubs = wgm_dev_hubs();
@@ -220,7 +226,7 @@ static int wgm_upload_transpose(wgm_app *a, const wgm_graph_desc *g) {
 }
 
 extern "C" int wgm_app_upload(wgm_app *a, const wgm_graph_desc *g) {
-  if (!a) return WGM_ERR_INVALID;
+  if (!a || a->kind == WGM_APP_OCTREE) return WGM_ERR_INVALID;
   int s = wgm_validate_graph(a->kind, g);
   if (s) return s;
   if (g->num_nodes != a->V || g->num_edges != a->E) return WGM_ERR_INVALID;
@@ -254,7 +260,8 @@ extern "C" int wgm_app_create(wgm_runtime *rt, int kind, const wgm_graph_desc *g
                               wgm_app **out) {
   if (!rt || !out) return WGM_ERR_INVALID;
   *out = nullptr;
-  if (wgm_kind_to_kernel(kind) < 0) return WGM_ERR_INVALID;
+  /* the octree has particles, not a graph: wgm_octree_create */
+  if (wgm_kind_to_kernel(kind) < 0 || kind == WGM_APP_OCTREE) return WGM_ERR_INVALID;
   int s = wgm_validate_graph(kind, g);
   if (s) return s;
   cudaSetDevice(rt->device);
@@ -345,7 +352,7 @@ extern "C" int wgm_app_create(wgm_runtime *rt, int kind, const wgm_graph_desc *g
 }
 
 extern "C" int wgm_app_set_source(wgm_app *a, int32_t source) {
-  if (!a || source < 0 || source >= a->V) return WGM_ERR_INVALID;
+  if (!a || a->kind == WGM_APP_OCTREE || source < 0 || source >= a->V) return WGM_ERR_INVALID;
   a->source = source;
   return WGM_OK;
 }
@@ -393,6 +400,26 @@ static wgm_hubs wgm_hubs_view(const wgm_app *a) {
 int wgm_app_fill_mega(wgm_app *a, wgm_mega_args *A) {
   A->app = wgm_kind_to_kernel(a->kind);
   switch (a->kind) {
+    case WGM_APP_OCTREE: {
+      wgm_octree_args &x = A->oct;
+      x.input = (const float4 *)a->d_oct_input;
+      x.particles = (float4 *)a->d_out;
+      x.newparticles = (float4 *)a->d_oct_second;
+      x.tree = a->d_oct_tree;
+      x.tree_cap = a->oct_tree_cap;
+      x.tree_size = a->d_oct_ctr;
+      x.done = a->d_oct_ctr + 32; /* its own 128-byte line */
+      x.n = a->V;
+      x.maxchilds = a->oct_maxchilds;
+      x.pools = (wgm_octree_task *)a->d_oct_pools;
+      x.locks = a->d_oct_locks;
+      x.heads = a->d_oct_heads;
+      x.num_pools = a->oct_num_pools;
+      x.pool_size = a->oct_pool_size;
+      x.tasks_out = a->d_rounds;
+      x.rlock = (int *)(a->d_oct_ctr + 64); /* a third line */
+      return WGM_OK;
+    }
     case WGM_APP_LONESTAR_BFS:
     case WGM_APP_LONESTAR_SSSP: {
       wgm_lonestar_args &x = A->ls;
@@ -502,6 +529,8 @@ static cudaError_t wgm_app_enqueue(wgm_app *a, const wgm_launch &L, int grid, in
       return wgm_launch_psssp(L, A.psssp, grid, block, stream);
     case WGM_APP_PAGERANK:
       return wgm_launch_pagerank(L, A.pr, grid, block, stream);
+    case WGM_APP_OCTREE:
+      return wgm_launch_octree(L, A.oct, grid, block, stream);
   }
   return cudaErrorInvalidValue;
 }
@@ -596,6 +625,103 @@ extern "C" int wgm_run_persistent(wgm_runtime *rt, wgm_app *a, int num_wgs,
   if (s == WGM_OK && hs_status != WGM_OK) s = hs_status;
   if (s == WGM_OK && ws != WGM_OK) s = ws;
   return s;
+}
+
+/* Octree app (octree.h:98-132 init_persistent_app_for_real): the input
+ * particles stay on the device and every run starts from them; pools are
+ * min(occupancy bound, 128) stacks of pool_size tasks. */
+extern "C" int wgm_octree_create(wgm_runtime *rt, int32_t num_particles, const float *xyzw,
+                                 int32_t maxchilds, int32_t pool_size, int64_t tree_cap,
+                                 wgm_app **out) {
+  if (!rt || !out || !xyzw || num_particles < 1 || maxchilds < 1 || pool_size < 1 ||
+      tree_cap < (int64_t)WGM_OCTREE_ROOT_FREE + 8 || tree_cap > (1LL << 31))
+    return WGM_ERR_INVALID;
+  for (int64_t i = 0; i < 4LL * num_particles; i++)
+    if (!(std::fabs(xyzw[i]) < 1.0e30f)) return WGM_ERR_INVALID; /* finite */
+  *out = nullptr;
+  cudaSetDevice(rt->device);
+  wgm_app *a = new (std::nothrow) wgm_app();
+  if (!a) return WGM_ERR_OOM;
+  a->rt = rt;
+  a->kind = WGM_APP_OCTREE;
+  a->V = num_particles;
+  a->oct_maxchilds = maxchilds;
+  a->oct_pool_size = pool_size;
+  a->oct_tree_cap = tree_cap;
+  int hw = 0;
+  int s = wgm_hw_bound_for(rt, WGM_K_OCTREE, wgm_block_size(rt), &hw);
+  if (s) {
+    delete a;
+    return s;
+  }
+  a->oct_num_pools = std::max(1, std::min(hw, 128));
+  const size_t n = (size_t)num_particles;
+  a->out_bytes = n * 16;
+  cudaError_t e = cudaMalloc(&a->d_out, n * 16);
+  if (e == cudaSuccess) e = cudaMalloc(&a->d_oct_input, n * 16);
+  if (e == cudaSuccess) e = cudaMalloc(&a->d_oct_second, n * 16);
+  if (e == cudaSuccess)
+    e = cudaMalloc(&a->d_oct_pools, (size_t)a->oct_num_pools * pool_size * sizeof(wgm_octree_task));
+  if (e == cudaSuccess) e = wgm_dmalloc(&a->d_oct_tree, (size_t)tree_cap);
+  if (e == cudaSuccess) e = wgm_dmalloc(&a->d_oct_ctr, 96);
+  if (e == cudaSuccess) e = wgm_dmalloc(&a->d_oct_locks, (size_t)a->oct_num_pools);
+  if (e == cudaSuccess) e = wgm_dmalloc(&a->d_oct_heads, (size_t)a->oct_num_pools);
+  if (e == cudaSuccess) e = wgm_dmalloc(&a->d_rounds, 1);
+  if (e == cudaSuccess) e = cudaMemset(a->d_oct_tree, 0, (size_t)tree_cap * 4);
+  if (e == cudaSuccess) e = cudaMemset(a->d_oct_ctr, 0, 96 * 4);
+  if (e == cudaSuccess) e = cudaMemset(a->d_rounds, 0, 4);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(a->d_oct_input, xyzw, n * 16, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(a->d_out, xyzw, n * 16, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    int st = wgm_cuda_fail(rt, e);
+    wgm_app_free_buffers(a);
+    delete a;
+    return st;
+  }
+  *out = a;
+  return WGM_OK;
+}
+
+/* The built tree: entries [0, tree_size), particles done, tasks run. */
+extern "C" int wgm_octree_read(wgm_app *a, uint32_t *tree_out, int64_t tree_len,
+                               uint32_t *tree_size, uint32_t *done, int32_t *tasks) {
+  if (!a || a->kind != WGM_APP_OCTREE) return WGM_ERR_INVALID;
+  cudaSetDevice(a->rt->device);
+  uint32_t ctr[64];
+  int t = 0;
+  cudaError_t e = cudaStreamSynchronize(a->rt->stream);
+  if (e == cudaSuccess) e = cudaMemcpy(ctr, a->d_oct_ctr, sizeof(ctr), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(&t, a->d_rounds, 4, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return wgm_cuda_fail(a->rt, e);
+  const int64_t used = std::min<int64_t>(ctr[0], a->oct_tree_cap);
+  if (tree_size) *tree_size = ctr[0];
+  if (done) *done = ctr[32];
+  if (tasks) *tasks = t;
+  if (tree_out) {
+    if (tree_len < used) return WGM_ERR_INVALID;
+    e = cudaMemcpy(tree_out, a->d_oct_tree, (size_t)used * 4, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return wgm_cuda_fail(a->rt, e);
+  }
+  return WGM_OK;
+}
+
+/* check_persistent_task (octree.h:190-236): the leaf counts of the tree add
+ * up to the particle count, and so does particlesDone. */
+extern "C" int wgm_octree_check(wgm_app *a, int32_t *ok) {
+  if (!a || !ok || a->kind != WGM_APP_OCTREE) return WGM_ERR_INVALID;
+  uint32_t size = 0, done = 0;
+  int s = wgm_octree_read(a, nullptr, 0, &size, &done, nullptr);
+  if (s) return s;
+  const int64_t used = std::min<int64_t>(size, a->oct_tree_cap);
+  std::vector<uint32_t> tree((size_t)std::max<int64_t>(used, 1));
+  s = wgm_octree_read(a, tree.data(), used, nullptr, nullptr, nullptr);
+  if (s) return s;
+  uint64_t sum = 0;
+  for (int64_t i = 0; i < used; i++)
+    if (tree[i] & 0x80000000u) sum += tree[i] & 0x7fffffffu;
+  *ok = (sum == (uint64_t)a->V && done == (uint32_t)a->V) ? 1 : 0;
+  return WGM_OK;
 }
 
 extern "C" int wgm_app_read_result(wgm_app *a, void *host_out, size_t bytes) {

@@ -62,6 +62,12 @@ struct wgm_app {
   float dang0 = 0.f;
   int iterations = 20;
   bool has_node_values = false;
+  /* octree (WGM_APP_OCTREE): d_out holds the particles, V their count */
+  void *d_oct_input = nullptr, *d_oct_second = nullptr, *d_oct_pools = nullptr;
+  unsigned *d_oct_tree = nullptr, *d_oct_ctr = nullptr; /* ctr: tree size, done */
+  int *d_oct_locks = nullptr, *d_oct_heads = nullptr;
+  long long oct_tree_cap = 0;
+  int oct_maxchilds = 5, oct_num_pools = 0, oct_pool_size = 0;
 };
 
 int wgm_cuda_fail(wgm_runtime *rt, cudaError_t e);

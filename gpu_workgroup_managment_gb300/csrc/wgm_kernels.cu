@@ -85,6 +85,16 @@ __global__ void __launch_bounds__(1024) wgm_k_barrier_bench(wgm_launch L,
   }
 }
 
+/* Standalone octree build (octree.cl:150-320 without a scheduler): init,
+ * one barrier, then the task loop; nothing is offered to kill or fork. */
+__global__ void __launch_bounds__(1024) wgm_k_octree(wgm_launch L, wgm_octree_args a) {
+  WGM_PERSISTENT_PROLOGUE
+  (void)sm;
+  wgm_octree_init(L, &c, a);
+  if (wgm_barrier(L, &c)) wgm_octree_loop(L, &c, a, [](wgm_cta *) { return false; });
+  WGM_PERSISTENT_EPILOGUE
+}
+
 const void *wgm_kernel_fn(int kid) {
   switch (kid) {
     case WGM_K_BFS: return (const void *)wgm_k_bfs;
@@ -94,6 +104,7 @@ const void *wgm_kernel_fn(int kid) {
     case WGM_K_PSSSP: return (const void *)wgm_k_psssp;
     case WGM_K_PAGERANK: return (const void *)wgm_k_pagerank;
     case WGM_K_BARRIER_BENCH: return (const void *)wgm_k_barrier_bench;
+    case WGM_K_OCTREE: return (const void *)wgm_k_octree;
     default: return nullptr;
   }
 }
@@ -124,6 +135,11 @@ cudaError_t wgm_launch_psssp(const wgm_launch &L, const wgm_psssp_args &a, int g
 cudaError_t wgm_launch_pagerank(const wgm_launch &L, const wgm_pr_args &a, int grid, int block,
                                 cudaStream_t s) {
   wgm_k_pagerank<<<grid, block, 0, s>>>(L, a);
+  return cudaGetLastError();
+}
+cudaError_t wgm_launch_octree(const wgm_launch &L, const wgm_octree_args &a, int grid, int block,
+                              cudaStream_t s) {
+  wgm_k_octree<<<grid, block, 0, s>>>(L, a);
   return cudaGetLastError();
 }
 cudaError_t wgm_launch_barrier_bench(const wgm_launch &L, const wgm_barrier_bench_args &a,

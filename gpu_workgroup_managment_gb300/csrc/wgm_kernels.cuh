@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include "wgm_graph.cuh"
+#include "wgm_octree.cuh"
 
 enum wgm_kernel_id {
   WGM_K_BFS = 0,
@@ -22,6 +23,7 @@ enum wgm_kernel_id {
   WGM_K_PSSSP,
   WGM_K_PAGERANK,
   WGM_K_BARRIER_BENCH,
+  WGM_K_OCTREE,
   WGM_K_COUNT
 };
 
@@ -44,6 +46,8 @@ cudaError_t wgm_launch_psssp(const wgm_launch &L, const wgm_psssp_args &a, int g
                              cudaStream_t s);
 cudaError_t wgm_launch_pagerank(const wgm_launch &L, const wgm_pr_args &a, int grid, int block,
                                 cudaStream_t s);
+cudaError_t wgm_launch_octree(const wgm_launch &L, const wgm_octree_args &a, int grid, int block,
+                              cudaStream_t s);
 cudaError_t wgm_launch_barrier_bench(const wgm_launch &L, const wgm_barrier_bench_args &a,
                                      int grid, int block, cudaStream_t s);
 

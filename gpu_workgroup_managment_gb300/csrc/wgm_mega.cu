@@ -69,6 +69,35 @@ __device__ __forceinline__ void wgm_mega_run_app(const wgm_launch &L, const wgm_
         return wgm_phase_pagerank(L, pc, A.pr, sm, cur, nxt);
       });
       break;
+    case WGM_K_OCTREE:
+      /* octree.cl:170-180: init and one resizing barrier, then a task loop
+       * with no barrier in which persistent group 0 offers forks and every
+       * other group offers to be killed before it takes a task.  With no
+       * barrier to separate them, a kill could land between a fork's read of
+       * the group count and its growth and leave a hole in the group ids, so
+       * kills and forks both hold the app's own lock (try-lock: a busy lock
+       * only defers the offer).  Not the scheduler's pool lock: the scheduler
+       * holds that while it waits for the kills. */
+      if (start.target == 0) {
+        wgm_octree_init(L, pc, A.oct);
+        if (!sync(L, pc, wgm_step{1, 0})) break;
+      }
+      wgm_octree_loop(L, pc, A.oct, [&](wgm_cta *cx) {
+        if (!wgm_try_lock(A.oct.rlock)) return false;
+        bool killed = false;
+        if (cx->id == 0) {
+          wgm_rctx rc;
+          for (int k = 0; k < WGM_RCTX_WORDS; k++) rc.w[k] = 0;
+          rc.w[WGM_RC_TARGET] = 1;
+          rc.w[WGM_RC_GEN] = cx->gen;
+          wgm_offer_fork(L, -1, rc);
+        } else {
+          killed = wgm_offer_kill(L, cx->id);
+        }
+        wgm_unlock(A.oct.rlock);
+        return killed;
+      });
+      break;
     default:
       break;
   }

@@ -20,6 +20,7 @@
 #define WGM_MEGA_CUH
 
 #include "wgm_graph.cuh"
+#include "wgm_octree.cuh"
 
 /* Non-persistent task kinds. */
 #define WGM_NP_MATMULT_I32 1 /* matmult.cl: int32 C = A*B, djb2 hash of the diagonal */
@@ -49,6 +50,7 @@ struct wgm_mega_args {
   wgm_mis_args mis;
   wgm_psssp_args psssp;
   wgm_pr_args pr;
+  wgm_octree_args oct;
   wgm_np_args np;
   unsigned long long idle_ns; /* budget of host-driven waits */
   int use_query_barrier;
@@ -162,11 +164,14 @@ __device__ __forceinline__ bool wgm_offer_kill(const wgm_launch &L, int kid) {
 /* offer_fork (scheduler_1.cl:10-57), master thread 0 only, after every live
  * group arrived: take every free group, give each the restoration record
  * `rc` (the next phase, the barrier generation and the new group count),
- * then grow the persistent group count. */
+ * then grow the persistent group count.  n < 0: read the group count under
+ * the pool lock (a task loop without barriers that keeps kills out while it
+ * forks). */
 __device__ __forceinline__ int wgm_offer_fork(const wgm_launch &L, int n, wgm_rctx rc) {
   wgm_dev_state *st = L.st;
   if (wgm_ld_acquire_gpu(&st->available_workgroups) <= 0) return n;
   if (!wgm_try_lock(&st->pool_lock)) return n;
+  if (n < 0) n = wgm_ld_acquire_gpu(&st->k_num_groups[1][0]);
   int snap = wgm_ld_acquire_gpu(&st->available_workgroups);
   int got = 0;
   rc.w[WGM_RC_NGROUPS] = n + snap;

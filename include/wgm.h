@@ -57,6 +57,7 @@ extern "C" {
 #define WGM_APP_PANNOTIA_MIS 4
 #define WGM_APP_PANNOTIA_SSSP 5
 #define WGM_APP_PAGERANK 6
+#define WGM_APP_OCTREE 7 /* work-stealing octree build (test_suite/final_octree) */
 
 typedef struct wgm_runtime wgm_runtime;
 typedef struct wgm_app wgm_app;
@@ -173,6 +174,24 @@ int wgm_app_result_device_ptr(wgm_app *app, void **device_ptr, size_t *bytes);
 int wgm_app_rounds(wgm_app *app, int *rounds);
 /* clean_persistent_task (bfs.h:330-334). */
 int wgm_app_destroy(wgm_app *app);
+
+/* Octree app (test_suite/final_octree/octree.h:98-132 init_persistent_app_for_real,
+ * octree.cl:150-320): num_particles float4 positions (xyzw, host), boxes of
+ * more than maxchilds particles split (FLAGS_maxChildren), task pools of
+ * pool_size tasks (FLAGS_pool_size), tree_cap tree entries (MAXTREESIZE).
+ * Runs with wgm_run_persistent or as the megakernel's persistent app; every
+ * run starts from the same particles.  wgm_app_read_result returns the
+ * particles in leaf order (16 bytes each). */
+int wgm_octree_create(wgm_runtime *rt, int32_t num_particles, const float *xyzw,
+                      int32_t maxchilds, int32_t pool_size, int64_t tree_cap, wgm_app **out);
+/* The tree of the last run: entries [0, *tree_size) into tree_out (an entry
+ * is a child block's first index, or 0x80000000 | leaf particle count),
+ * particlesDone and the number of tasks run. */
+int wgm_octree_read(wgm_app *app, uint32_t *tree_out, int64_t tree_len, uint32_t *tree_size,
+                    uint32_t *done, int32_t *tasks);
+/* check_persistent_task (octree.h:190-236): leaf counts and particlesDone
+ * both equal the particle count. */
+int wgm_octree_check(wgm_app *app, int32_t *ok);
 
 /* ---- megakernel and communicator --------------------------------------- */
 /* One persistent launch in which discovered group 0 runs the device-side

@@ -134,3 +134,28 @@ def test_pagerank_f32_close_to_f64():
     p32 = oracle.pagerank_f32_omp(g)
     assert abs(p64.sum() - 1.0) < 1e-9
     assert np.max(np.abs(p32 - p64)) / np.max(np.abs(p64)) < 1e-5
+
+
+def test_octree_oracle_properties():
+    """The octree restatement: leaves tile [0, n) in order, every leaf holds
+    at most maxchilds particles (a box is split above that), every particle
+    of a leaf lies in its octant of the parent box, and the output is a
+    permutation of the input."""
+    from gpu_workgroup_managment_gb300.octree import clustered_particles
+    from oracle import octree_oracle
+    p = clustered_particles(20_000, seed=2)
+    out, lv = octree_oracle.build(p, 5)
+    pos = 0
+    for beg, end, (mx, my, mz, _w), o in lv:
+        if end == beg:
+            continue
+        assert beg == pos and end - beg <= 5
+        pts = out[beg:end]
+        assert np.all((pts[:, 0] >= np.float32(mx)) == bool(o & 1))
+        assert np.all((pts[:, 1] >= np.float32(my)) == bool(o & 2))
+        assert np.all((pts[:, 2] >= np.float32(mz)) == bool(o & 4))
+        pos = end
+    assert pos == len(p)
+    a = np.sort(p.view(np.uint32).reshape(-1, 4), axis=0)
+    b = np.sort(out.view(np.uint32).reshape(-1, 4), axis=0)
+    assert np.array_equal(a, b)
