@@ -29,6 +29,7 @@ int wgm_kind_to_kernel(int kind) {
     case WGM_APP_PANNOTIA_SSSP: return WGM_K_PSSSP;
     case WGM_APP_PAGERANK: return WGM_K_PAGERANK;
     case WGM_APP_OCTREE: return WGM_K_OCTREE;
+    case WGM_APP_CONNECT_FOUR: return WGM_K_C4;
     default: return -1;
   }
 }
@@ -42,6 +43,7 @@ extern "C" const char *wgm_persistent_app_name(int kind) {
     case WGM_APP_PANNOTIA_SSSP: return "sssp";          /* pannotia sssp.h:25 */
     case WGM_APP_PAGERANK: return "pagerank";
     case WGM_APP_OCTREE: return "octree";               /* octree.h:79 */
+    case WGM_APP_CONNECT_FOUR: return "connect_four";   /* connect_four.h:113 */
     default: return nullptr;
   }
 }
@@ -55,6 +57,7 @@ extern "C" const char *wgm_persistent_kernel_name(int kind) {
     case WGM_APP_PANNOTIA_SSSP: return "sssp_combined";
     case WGM_APP_PAGERANK: return "pagerank_pull";
     case WGM_APP_OCTREE: return "octree_main";          /* octree.h:85 */
+    case WGM_APP_CONNECT_FOUR: return "connect_four";
     default: return nullptr;
   }
 }
@@ -139,7 +142,9 @@ static void wgm_app_free_buffers(wgm_app *a) {
                   a->d_status,  a->d_contrib,   a->d_dang,    a->d_hub_sum,    a->d_rounds,
                   a->hubs.ids,  a->hubs.prefix, a->hubs.wmap, a->d_trow, a->d_tcol,
                   a->d_oct_input, a->d_oct_second, a->d_oct_pools, a->d_oct_tree,
-                  a->d_oct_ctr, a->d_oct_locks, a->d_oct_heads};
+                  a->d_oct_ctr, a->d_oct_locks, a->d_oct_heads,
+                  a->d_c4_board, a->d_c4_nodes, a->d_c4_pool, a->d_c4_locks,
+                  a->d_c4_heads, a->d_c4_ctr};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   a->hubs = wgm_dev_hubs();
@@ -226,7 +231,7 @@ static int wgm_upload_transpose(wgm_app *a, const wgm_graph_desc *g) {
 }
 
 extern "C" int wgm_app_upload(wgm_app *a, const wgm_graph_desc *g) {
-  if (!a || a->kind == WGM_APP_OCTREE) return WGM_ERR_INVALID;
+  if (!a || a->kind == WGM_APP_OCTREE || a->kind == WGM_APP_CONNECT_FOUR) return WGM_ERR_INVALID;
   int s = wgm_validate_graph(a->kind, g);
   if (s) return s;
   if (g->num_nodes != a->V || g->num_edges != a->E) return WGM_ERR_INVALID;
@@ -261,7 +266,8 @@ extern "C" int wgm_app_create(wgm_runtime *rt, int kind, const wgm_graph_desc *g
   if (!rt || !out) return WGM_ERR_INVALID;
   *out = nullptr;
   /* the octree has particles, not a graph: wgm_octree_create */
-  if (wgm_kind_to_kernel(kind) < 0 || kind == WGM_APP_OCTREE) return WGM_ERR_INVALID;
+  if (wgm_kind_to_kernel(kind) < 0 || kind == WGM_APP_OCTREE || kind == WGM_APP_CONNECT_FOUR)
+    return WGM_ERR_INVALID;
   int s = wgm_validate_graph(kind, g);
   if (s) return s;
   cudaSetDevice(rt->device);
@@ -352,7 +358,9 @@ extern "C" int wgm_app_create(wgm_runtime *rt, int kind, const wgm_graph_desc *g
 }
 
 extern "C" int wgm_app_set_source(wgm_app *a, int32_t source) {
-  if (!a || a->kind == WGM_APP_OCTREE || source < 0 || source >= a->V) return WGM_ERR_INVALID;
+  if (!a || a->kind == WGM_APP_OCTREE || a->kind == WGM_APP_CONNECT_FOUR || source < 0 ||
+      source >= a->V)
+    return WGM_ERR_INVALID;
   a->source = source;
   return WGM_OK;
 }
@@ -418,6 +426,24 @@ int wgm_app_fill_mega(wgm_app *a, wgm_mega_args *A) {
       x.pool_size = a->oct_pool_size;
       x.tasks_out = a->d_rounds;
       x.rlock = (int *)(a->d_oct_ctr + 64); /* a third line */
+      return WGM_OK;
+    }
+    case WGM_APP_CONNECT_FOUR: {
+      wgm_c4_args &x = A->c4;
+      x.base_board = a->d_c4_board;
+      x.maxlevel = a->c4_maxlevel;
+      x.nodes = (wgm_c4_node *)a->d_c4_nodes;
+      x.num_nodes = a->c4_num_nodes;
+      x.node_head = a->d_c4_ctr;
+      x.root_done = a->d_c4_ctr + 32;
+      x.rlock = a->d_c4_ctr + 64;
+      x.pool = a->d_c4_pool;
+      x.locks = a->d_c4_locks;
+      x.heads = a->d_c4_heads;
+      x.num_pools = a->c4_num_pools;
+      x.pool_size = a->c4_pool_size;
+      x.next_move_value = (int *)a->d_out;
+      x.tasks_out = a->d_rounds;
       return WGM_OK;
     }
     case WGM_APP_LONESTAR_BFS:
@@ -531,6 +557,8 @@ static cudaError_t wgm_app_enqueue(wgm_app *a, const wgm_launch &L, int grid, in
       return wgm_launch_pagerank(L, A.pr, grid, block, stream);
     case WGM_APP_OCTREE:
       return wgm_launch_octree(L, A.oct, grid, block, stream);
+    case WGM_APP_CONNECT_FOUR:
+      return wgm_launch_c4(L, A.c4, grid, block, stream);
   }
   return cudaErrorInvalidValue;
 }
@@ -673,6 +701,62 @@ extern "C" int wgm_octree_create(wgm_runtime *rt, int32_t num_particles, const f
   if (e == cudaSuccess)
     e = cudaMemcpy(a->d_oct_input, xyzw, n * 16, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(a->d_out, xyzw, n * 16, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    int st = wgm_cuda_fail(rt, e);
+    wgm_app_free_buffers(a);
+    delete a;
+    return st;
+  }
+  *out = a;
+  return WGM_OK;
+}
+
+/* Connect-four app (connect_four.h:198-230): nodes for every move sequence
+ * up to maxlevel (compute_num_node, connect_four.h:70-77), pools of node ids
+ * (min(occupancy bound, 128) of them). */
+extern "C" int wgm_c4_create(wgm_runtime *rt, const uint8_t *board, int32_t maxlevel,
+                             int32_t pool_size, wgm_app **out) {
+  if (!rt || !out || !board || maxlevel < 1 || maxlevel > WGM_C4_MAX_LOOKAHEAD || pool_size < 1)
+    return WGM_ERR_INVALID;
+  for (int i = 0; i < WGM_C4_CELLS; i++)
+    if (board[i] > WGM_C4_COMPUTER) return WGM_ERR_INVALID;
+  *out = nullptr;
+  cudaSetDevice(rt->device);
+  wgm_app *a = new (std::nothrow) wgm_app();
+  if (!a) return WGM_ERR_OOM;
+  a->rt = rt;
+  a->kind = WGM_APP_CONNECT_FOUR;
+  a->V = WGM_C4_COLS;
+  a->c4_maxlevel = maxlevel;
+  a->c4_pool_size = pool_size;
+  long long nodes = 1, p7 = 1;
+  for (int i = 1; i <= maxlevel; i++) {
+    p7 *= 7;
+    nodes += p7;
+  }
+  a->c4_num_nodes = (int)nodes;
+  int hw = 0;
+  int s = wgm_hw_bound_for(rt, WGM_K_C4, wgm_block_size(rt), &hw);
+  if (s) {
+    delete a;
+    return s;
+  }
+  a->c4_num_pools = std::max(1, std::min(hw, 128));
+  a->out_bytes = WGM_C4_COLS * 4;
+  cudaError_t e = cudaMalloc(&a->d_out, a->out_bytes);
+  if (e == cudaSuccess) e = wgm_dmalloc(&a->d_c4_board, WGM_C4_CELLS);
+  if (e == cudaSuccess) e = cudaMalloc(&a->d_c4_nodes, (size_t)nodes * sizeof(wgm_c4_node));
+  if (e == cudaSuccess) e = wgm_dmalloc(&a->d_c4_pool, (size_t)a->c4_num_pools * pool_size);
+  if (e == cudaSuccess) e = wgm_dmalloc(&a->d_c4_locks, (size_t)a->c4_num_pools);
+  if (e == cudaSuccess) e = wgm_dmalloc(&a->d_c4_heads, (size_t)a->c4_num_pools);
+  if (e == cudaSuccess) e = wgm_dmalloc(&a->d_c4_ctr, 96);
+  if (e == cudaSuccess) e = wgm_dmalloc(&a->d_rounds, 1);
+  if (e == cudaSuccess) e = cudaMemset(a->d_c4_ctr, 0, 96 * 4);
+  if (e == cudaSuccess) e = cudaMemset(a->d_rounds, 0, 4);
+  if (e == cudaSuccess) e = cudaMemset(a->d_out, 0, a->out_bytes);
+  if (e == cudaSuccess) e = cudaMemset(a->d_c4_nodes, 0, (size_t)nodes * sizeof(wgm_c4_node));
+  if (e == cudaSuccess)
+    e = cudaMemcpy(a->d_c4_board, board, WGM_C4_CELLS, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
     int st = wgm_cuda_fail(rt, e);
     wgm_app_free_buffers(a);

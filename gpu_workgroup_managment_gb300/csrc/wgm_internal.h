@@ -68,6 +68,12 @@ struct wgm_app {
   int *d_oct_locks = nullptr, *d_oct_heads = nullptr;
   long long oct_tree_cap = 0;
   int oct_maxchilds = 5, oct_num_pools = 0, oct_pool_size = 0;
+  /* connect four (WGM_APP_CONNECT_FOUR): d_out holds next_move_value[7] */
+  unsigned char *d_c4_board = nullptr;
+  void *d_c4_nodes = nullptr;
+  int *d_c4_pool = nullptr, *d_c4_locks = nullptr, *d_c4_heads = nullptr;
+  int *d_c4_ctr = nullptr; /* node head, root done, offer lock: one line each */
+  int c4_maxlevel = 6, c4_num_nodes = 0, c4_num_pools = 0, c4_pool_size = 0;
 };
 
 int wgm_cuda_fail(wgm_runtime *rt, cudaError_t e);

@@ -95,6 +95,16 @@ __global__ void __launch_bounds__(1024) wgm_k_octree(wgm_launch L, wgm_octree_ar
   WGM_PERSISTENT_EPILOGUE
 }
 
+/* Standalone connect-four look-ahead (connect_four.cl:350-487 without a
+ * scheduler). */
+__global__ void __launch_bounds__(1024) wgm_k_c4(wgm_launch L, wgm_c4_args a) {
+  WGM_PERSISTENT_PROLOGUE
+  (void)sm;
+  wgm_c4_init(L, &c, a);
+  if (wgm_barrier(L, &c)) wgm_c4_loop(L, &c, a, [](wgm_cta *) { return false; });
+  WGM_PERSISTENT_EPILOGUE
+}
+
 const void *wgm_kernel_fn(int kid) {
   switch (kid) {
     case WGM_K_BFS: return (const void *)wgm_k_bfs;
@@ -105,6 +115,7 @@ const void *wgm_kernel_fn(int kid) {
     case WGM_K_PAGERANK: return (const void *)wgm_k_pagerank;
     case WGM_K_BARRIER_BENCH: return (const void *)wgm_k_barrier_bench;
     case WGM_K_OCTREE: return (const void *)wgm_k_octree;
+    case WGM_K_C4: return (const void *)wgm_k_c4;
     default: return nullptr;
   }
 }
@@ -140,6 +151,11 @@ cudaError_t wgm_launch_pagerank(const wgm_launch &L, const wgm_pr_args &a, int g
 cudaError_t wgm_launch_octree(const wgm_launch &L, const wgm_octree_args &a, int grid, int block,
                               cudaStream_t s) {
   wgm_k_octree<<<grid, block, 0, s>>>(L, a);
+  return cudaGetLastError();
+}
+cudaError_t wgm_launch_c4(const wgm_launch &L, const wgm_c4_args &a, int grid, int block,
+                          cudaStream_t s) {
+  wgm_k_c4<<<grid, block, 0, s>>>(L, a);
   return cudaGetLastError();
 }
 cudaError_t wgm_launch_barrier_bench(const wgm_launch &L, const wgm_barrier_bench_args &a,

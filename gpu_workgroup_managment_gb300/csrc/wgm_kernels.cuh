@@ -14,6 +14,7 @@
 
 #include "wgm_graph.cuh"
 #include "wgm_octree.cuh"
+#include "wgm_c4.cuh"
 
 enum wgm_kernel_id {
   WGM_K_BFS = 0,
@@ -24,6 +25,7 @@ enum wgm_kernel_id {
   WGM_K_PAGERANK,
   WGM_K_BARRIER_BENCH,
   WGM_K_OCTREE,
+  WGM_K_C4,
   WGM_K_COUNT
 };
 
@@ -48,6 +50,8 @@ cudaError_t wgm_launch_pagerank(const wgm_launch &L, const wgm_pr_args &a, int g
                                 cudaStream_t s);
 cudaError_t wgm_launch_octree(const wgm_launch &L, const wgm_octree_args &a, int grid, int block,
                               cudaStream_t s);
+cudaError_t wgm_launch_c4(const wgm_launch &L, const wgm_c4_args &a, int grid, int block,
+                          cudaStream_t s);
 cudaError_t wgm_launch_barrier_bench(const wgm_launch &L, const wgm_barrier_bench_args &a,
                                      int grid, int block, cudaStream_t s);
 

@@ -32,6 +32,32 @@
 /* Kernel                                                                    */
 /* ------------------------------------------------------------------------ */
 
+/* Offers of a task loop without barriers (octree.cl:172-181,
+ * connect_four.cl:401-407), thread 0 at the top of every iteration:
+ * persistent group 0 offers a fork into the loop (restoration target 1),
+ * the others offer to be killed.  With no barrier to separate them, a kill
+ * could land between a fork's read of the group count and its growth and
+ * leave a hole in the group ids (no group would ever again be "the highest",
+ * and the scheduler would wait for kills forever), so both hold the app's
+ * own lock (a busy lock only defers the offer).  Not the scheduler's pool
+ * lock: the scheduler holds that while it waits for the kills.  Returns true
+ * when this group must leave. */
+__device__ __forceinline__ bool wgm_task_offer(const wgm_launch &L, wgm_cta *cx, int *rlock) {
+  if (!wgm_try_lock(rlock)) return false;
+  bool killed = false;
+  if (cx->id == 0) {
+    wgm_rctx rc;
+    for (int k = 0; k < WGM_RCTX_WORDS; k++) rc.w[k] = 0;
+    rc.w[WGM_RC_TARGET] = 1;
+    rc.w[WGM_RC_GEN] = cx->gen;
+    wgm_offer_fork(L, -1, rc);
+  } else {
+    killed = wgm_offer_kill(L, cx->id);
+  }
+  wgm_unlock(rlock);
+  return killed;
+}
+
 template <class Sync>
 __device__ __forceinline__ void wgm_mega_run_app(const wgm_launch &L, const wgm_mega_args &A,
                                                  wgm_cta *pc, wgm_warp_smem *sm, wgm_step start,
@@ -70,33 +96,20 @@ __device__ __forceinline__ void wgm_mega_run_app(const wgm_launch &L, const wgm_
       });
       break;
     case WGM_K_OCTREE:
-      /* octree.cl:170-180: init and one resizing barrier, then a task loop
-       * with no barrier in which persistent group 0 offers forks and every
-       * other group offers to be killed before it takes a task.  With no
-       * barrier to separate them, a kill could land between a fork's read of
-       * the group count and its growth and leave a hole in the group ids, so
-       * kills and forks both hold the app's own lock (try-lock: a busy lock
-       * only defers the offer).  Not the scheduler's pool lock: the scheduler
-       * holds that while it waits for the kills. */
+      /* octree.cl:170-180: init and one resizing barrier, then the task
+       * loop with an offer at the top of every iteration */
       if (start.target == 0) {
         wgm_octree_init(L, pc, A.oct);
         if (!sync(L, pc, wgm_step{1, 0})) break;
       }
-      wgm_octree_loop(L, pc, A.oct, [&](wgm_cta *cx) {
-        if (!wgm_try_lock(A.oct.rlock)) return false;
-        bool killed = false;
-        if (cx->id == 0) {
-          wgm_rctx rc;
-          for (int k = 0; k < WGM_RCTX_WORDS; k++) rc.w[k] = 0;
-          rc.w[WGM_RC_TARGET] = 1;
-          rc.w[WGM_RC_GEN] = cx->gen;
-          wgm_offer_fork(L, -1, rc);
-        } else {
-          killed = wgm_offer_kill(L, cx->id);
-        }
-        wgm_unlock(A.oct.rlock);
-        return killed;
-      });
+      wgm_octree_loop(L, pc, A.oct, [&](wgm_cta *cx) { return wgm_task_offer(L, cx, A.oct.rlock); });
+      break;
+    case WGM_K_C4: /* connect_four.cl:397-415: the same shape as the octree */
+      if (start.target == 0) {
+        wgm_c4_init(L, pc, A.c4);
+        if (!sync(L, pc, wgm_step{1, 0})) break;
+      }
+      wgm_c4_loop(L, pc, A.c4, [&](wgm_cta *cx) { return wgm_task_offer(L, cx, A.c4.rlock); });
       break;
     default:
       break;

@@ -21,6 +21,7 @@
 
 #include "wgm_graph.cuh"
 #include "wgm_octree.cuh"
+#include "wgm_c4.cuh"
 
 /* Non-persistent task kinds. */
 #define WGM_NP_MATMULT_I32 1 /* matmult.cl: int32 C = A*B, djb2 hash of the diagonal */
@@ -51,6 +52,7 @@ struct wgm_mega_args {
   wgm_psssp_args psssp;
   wgm_pr_args pr;
   wgm_octree_args oct;
+  wgm_c4_args c4;
   wgm_np_args np;
   unsigned long long idle_ns; /* budget of host-driven waits */
   int use_query_barrier;

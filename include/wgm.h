@@ -58,6 +58,7 @@ extern "C" {
 #define WGM_APP_PANNOTIA_SSSP 5
 #define WGM_APP_PAGERANK 6
 #define WGM_APP_OCTREE 7 /* work-stealing octree build (test_suite/final_octree) */
+#define WGM_APP_CONNECT_FOUR 8 /* work-stealing look-ahead (test_suite/connect_four) */
 
 typedef struct wgm_runtime wgm_runtime;
 typedef struct wgm_app wgm_app;
@@ -192,6 +193,14 @@ int wgm_octree_read(wgm_app *app, uint32_t *tree_out, int64_t tree_len, uint32_t
 /* check_persistent_task (octree.h:190-236): leaf counts and particlesDone
  * both equal the particle count. */
 int wgm_octree_check(wgm_app *app, int32_t *ok);
+
+/* Connect-four app (test_suite/connect_four/connect_four.h:148-230): the 42
+ * cells of the base board row by row from the top (0 empty, 1 human "o", 2
+ * computer "x"), maxlevel moves of look-ahead (1..7, FLAGS_maxlevel), task
+ * pools of pool_size node ids (FLAGS_pool_size).  wgm_app_read_result returns
+ * next_move_value[7] (int32), the value of each first move. */
+int wgm_c4_create(wgm_runtime *rt, const uint8_t *board, int32_t maxlevel, int32_t pool_size,
+                  wgm_app **out);
 
 /* ---- megakernel and communicator --------------------------------------- */
 /* One persistent launch in which discovered group 0 runs the device-side

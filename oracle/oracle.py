@@ -53,6 +53,7 @@ def lib() -> C.CDLL:
             "oracle_hash_diag": [P, I, I],
             "oracle_matmult_f32": [P, I, I, P, I, P],
             "oracle_batch_lonestar": [I, P, P, P, P, P, P, P, P, P, P],
+            "oracle_connect_four": [P, I, P],
         }
         for name, args in protos.items():
             fn = getattr(_lib, name)
@@ -116,6 +117,16 @@ class BatchArena:
                                     _p(self.dist_off), _p(self.algo), _p(self.source),
                                     _p(self.rows), _p(self.cols), _p(self.wts), _p(self.dist))
         return self.dist
+
+
+def connect_four(board: np.ndarray, maxlevel: int = 6) -> np.ndarray:
+    """next_move_value[7] of the reference's connect-four look-ahead
+    (test_suite/connect_four/device/connect_four.cl) from a 42-cell board."""
+    b = np.ascontiguousarray(board, dtype=np.uint8).reshape(42)
+    out = np.empty(7, np.int32)
+    if lib().oracle_connect_four(_p(b), maxlevel, _p(out)) != 0:
+        raise ValueError("maxlevel must be 1..7")
+    return out
 
 
 def lonestar_bfs(g, source: int = 0, omp: bool = False) -> np.ndarray:

@@ -605,3 +605,104 @@ void oracle_batch_lonestar(int32_t njobs, const int32_t *V, const int64_t *row_o
       oracle_lonestar_sssp(V[k], rp, cl, wts + col_off[k], source[k], d);
   }
 }
+
+/* ---- connect four (src/test_suite/connect_four/device/connect_four.cl) ---- */
+
+/* chain_value (connect_four.cl:70-80): 2 = computer, 1 = human, 0 empty. */
+static void c4_chain(int *v, int player, int chain) {
+  if (player != 0) {
+    if (chain >= 4)
+      *v = player == 2 ? 666 : -666;
+    else if (chain >= 2)
+      *v += player == 2 ? 1 : -1;
+  }
+}
+
+/* scan_board (connect_four.cl:84-130). */
+static int c4_scan(const uint8_t *b, int row, int col, int dr, int dc) {
+  int res = 0, player = 0, chain = 0;
+  do {
+    int cell = b[row * 7 + col];
+    if (cell == player) {
+      chain++;
+    } else {
+      c4_chain(&res, player, chain);
+      if (res == 666 || res == -666) return res;
+      player = cell;
+      chain = 1;
+    }
+    row += dr;
+    col += dc;
+  } while (0 <= row && row < 6 && 0 <= col && col < 7);
+  c4_chain(&res, player, chain);
+  return res;
+}
+
+/* board_value with one work-item per line (work-groups of 25 or more
+ * items, connect_four.cl:135-176) and the master's reduction in item order
+ * (connect_four.cl:433-441): the first +-666 wins, else the sum. */
+static int c4_board_value(const uint8_t *b) {
+  int value = 0;
+  for (int i = 0; i < 25; i++) {
+    int t;
+    if (i < 6)
+      t = c4_scan(b, i, 0, 0, 1);
+    else if (i < 13)
+      t = c4_scan(b, 0, i - 6, 1, 0);
+    else if (i < 19)
+      t = (i - 13) < 3 ? c4_scan(b, i - 13, 0, 1, 1) : c4_scan(b, 0, i - 13 - 2, 1, 1);
+    else
+      t = (i - 19) < 3 ? c4_scan(b, i - 19, 6, 1, -1) : c4_scan(b, 0, i - 19, 1, -1);
+    if (t == 666 || t == -666) return t;
+    value += t;
+  }
+  return value;
+}
+
+/* update_board (connect_four.cl:180-220): the computer moves first; a move
+ * into a full column is skipped and does not change the player. */
+static void c4_replay(const uint8_t *base, const uint8_t *moves, int level, uint8_t *b) {
+  memcpy(b, base, 42);
+  int player = 2;
+  for (int i = 0; i < level; i++) {
+    int col = moves[i];
+    if (b[col] != 0) continue;
+    int row = 0;
+    while (row < 6 && b[row * 7 + col] == 0) row++;
+    b[(row - 1) * 7 + col] = (uint8_t)player;
+    player = player == 2 ? 1 : 2;
+  }
+}
+
+/* A node's final value (connect_four.cl:443-485 with wgm_update_parent,
+ * :305-340): its own board value, then, unless it is a leaf (maxlevel or a
+ * +-666 score), combined with its 7 children's - min at an even level, max
+ * at an odd one. */
+static int c4_node(const uint8_t *base, uint8_t *moves, int level, int maxlevel) {
+  uint8_t b[42];
+  c4_replay(base, moves, level, b);
+  int v = c4_board_value(b);
+  if (level >= maxlevel || v == 666 || v == -666) return v;
+  int acc = v;
+  for (int i = 0; i < 7; i++) {
+    moves[level] = (uint8_t)i;
+    int c = c4_node(base, moves, level + 1, maxlevel);
+    if (level % 2 == 0)
+      acc = c < acc ? c : acc;
+    else
+      acc = c > acc ? c : acc;
+  }
+  return acc;
+}
+
+/* next_move_value[7] of the look-ahead from `board` (connect_four.h:336-351). */
+int oracle_connect_four(const uint8_t *board, int32_t maxlevel, int32_t *next_move_value) {
+  if (maxlevel < 1 || maxlevel > 7) return -1;
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int r = 0; r < 7; r++) {
+    uint8_t moves[8] = {0};
+    moves[0] = (uint8_t)r;
+    next_move_value[r] = c4_node(board, moves, 1, maxlevel);
+  }
+  return 0;
+}

@@ -118,6 +118,11 @@ void oracle_batch_lonestar(int32_t njobs, const int32_t *V, const int64_t *row_o
 
 int oracle_omp_threads(void);
 
+/* connect four (test_suite/connect_four/device/connect_four.cl): the value
+ * of each of the 7 first moves from a 42-cell board (0 empty, 1 human, 2
+ * computer), maxlevel moves of look-ahead (1..7).  Returns 0, or -1. */
+int oracle_connect_four(const uint8_t *board, int32_t maxlevel, int32_t *next_move_value);
+
 #ifdef __cplusplus
 }
 #endif

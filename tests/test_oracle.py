@@ -159,3 +159,13 @@ def test_octree_oracle_properties():
     a = np.sort(p.view(np.uint32).reshape(-1, 4), axis=0)
     b = np.sort(out.view(np.uint32).reshape(-1, 4), axis=0)
     assert np.array_equal(a, b)
+
+
+def test_connect_four_oracle_known_answer():
+    """The restatement reproduces the reference's own check values on its
+    committed board (connect_four.h:344-351, via tests/golden)."""
+    import json
+    with open(os.path.join(os.path.dirname(__file__), "golden", "connect_four.json")) as f:
+        d = json.load(f)
+    got = oracle.connect_four(np.array(d["board"], np.uint8), d["maxlevel"])
+    assert got.tolist() == d["next_move_value"]
