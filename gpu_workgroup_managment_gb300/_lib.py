@@ -25,6 +25,7 @@ APP_LONESTAR_BFS, APP_LONESTAR_SSSP, APP_PANNOTIA_COLOR = 1, 2, 3
 APP_PANNOTIA_MIS, APP_PANNOTIA_SSSP, APP_PAGERANK = 4, 5, 6
 APP_OCTREE = 7
 APP_CONNECT_FOUR = 8
+APP_PANNOTIA_BC = 9
 DISCOVERY_TICKET, DISCOVERY_REFERENCE = 0, 1
 BARRIER_SENSE, BARRIER_XF, BARRIER_TREE, BARRIER_COUNT, BARRIER_SPREAD, BARRIER_AUTO = 0, 1, 2, 3, 4, 5
 NP_NONE, NP_MATMULT_I32, NP_REDUCE_I32, NP_MATMULT_F32, NP_REDUCE_F32 = 0, 1, 2, 3, 4
@@ -98,6 +99,7 @@ _PROTOS = {
     "wgm_octree_read": (_I, [_P, _P, C.c_int64, _P, _P, _P]),
     "wgm_octree_check": (_I, [_P, _P]),
     "wgm_c4_create": (_I, [_P, _P, C.c_int32, C.c_int32, C.POINTER(_P)]),
+    "wgm_app_set_bc_sources": (_I, [_P, C.c_int32]),
     "wgm_app_upload": (_I, [_P, C.POINTER(WgmGraphDesc)]),
     "wgm_app_set_source": (_I, [_P, C.c_int32]),
     "wgm_app_set_node_values": (_I, [_P, _P]),

@@ -30,6 +30,7 @@ int wgm_kind_to_kernel(int kind) {
     case WGM_APP_PAGERANK: return WGM_K_PAGERANK;
     case WGM_APP_OCTREE: return WGM_K_OCTREE;
     case WGM_APP_CONNECT_FOUR: return WGM_K_C4;
+    case WGM_APP_PANNOTIA_BC: return WGM_K_BC;
     default: return -1;
   }
 }
@@ -44,6 +45,7 @@ extern "C" const char *wgm_persistent_app_name(int kind) {
     case WGM_APP_PAGERANK: return "pagerank";
     case WGM_APP_OCTREE: return "octree";               /* octree.h:79 */
     case WGM_APP_CONNECT_FOUR: return "connect_four";   /* connect_four.h:113 */
+    case WGM_APP_PANNOTIA_BC: return "bc";              /* bc.h */
     default: return nullptr;
   }
 }
@@ -58,6 +60,7 @@ extern "C" const char *wgm_persistent_kernel_name(int kind) {
     case WGM_APP_PAGERANK: return "pagerank_pull";
     case WGM_APP_OCTREE: return "octree_main";          /* octree.h:85 */
     case WGM_APP_CONNECT_FOUR: return "connect_four";
+    case WGM_APP_PANNOTIA_BC: return "bc_combined";     /* bc.cl:144 */
     default: return nullptr;
   }
 }
@@ -248,7 +251,7 @@ extern "C" int wgm_app_upload(wgm_app *a, const wgm_graph_desc *g) {
     s = wgm_upload_hubs(a, g);
     if (s) return s;
   }
-  if (a->kind == WGM_APP_PANNOTIA_COLOR) {
+  if (a->kind == WGM_APP_PANNOTIA_COLOR || a->kind == WGM_APP_PANNOTIA_BC) {
     s = wgm_upload_transpose(a, g);
     if (s) return s;
   }
@@ -332,6 +335,17 @@ extern "C" int wgm_app_create(wgm_runtime *rt, int kind, const wgm_graph_desc *g
       if (e == cudaSuccess) e = wgm_dmalloc(&a->d_contrib, 2 * V);
       if (e == cudaSuccess) e = wgm_dmalloc(&a->d_dang, 3 * WGM_LINE);
       break;
+    case WGM_APP_PANNOTIA_BC:
+      /* bc (out), dist, rho and sigma, the level lists and their starts */
+      a->out_bytes = V * 4;
+      a->bc_sources = a->V;
+      if (e == cudaSuccess) e = cudaMalloc(&a->d_out, a->out_bytes);
+      if (e == cudaSuccess) e = wgm_dmalloc(&a->d_stamp, V);
+      if (e == cudaSuccess) e = wgm_dmalloc(&a->d_contrib, 2 * V);
+      if (e == cudaSuccess) e = wgm_dmalloc(&a->d_wl_u, V);
+      if (e == cudaSuccess) e = wgm_dmalloc(&a->d_wl_start, V + 2);
+      if (e == cudaSuccess) e = wgm_dmalloc(&a->d_cnt, 3 * WGM_LINE);
+      break;
   }
   if (e != cudaSuccess) {
     s = wgm_cuda_fail(rt, e);
@@ -386,6 +400,13 @@ extern "C" int wgm_app_set_node_values(wgm_app *a, const float *nv) {
   return WGM_OK;
 }
 
+extern "C" int wgm_app_set_bc_sources(wgm_app *a, int32_t num_sources) {
+  if (!a || a->kind != WGM_APP_PANNOTIA_BC || num_sources < 0 || num_sources > a->V)
+    return WGM_ERR_INVALID;
+  a->bc_sources = num_sources;
+  return WGM_OK;
+}
+
 extern "C" int wgm_app_set_pagerank(wgm_app *a, float damping, int iterations) {
   if (!a || a->kind != WGM_APP_PAGERANK || iterations < 0 || !(damping >= 0.f && damping <= 1.f))
     return WGM_ERR_INVALID;
@@ -426,6 +447,24 @@ int wgm_app_fill_mega(wgm_app *a, wgm_mega_args *A) {
       x.pool_size = a->oct_pool_size;
       x.tasks_out = a->d_rounds;
       x.rlock = (int *)(a->d_oct_ctr + 64); /* a third line */
+      return WGM_OK;
+    }
+    case WGM_APP_PANNOTIA_BC: {
+      wgm_bc_args &x = A->bc;
+      x.V = a->V;
+      x.row = a->d_row;
+      x.col = a->d_col;
+      x.trow = a->d_trow ? a->d_trow : a->d_row;
+      x.tcol = a->d_tcol ? a->d_tcol : a->d_col;
+      x.bc = (float *)a->d_out;
+      x.dist = a->d_stamp;
+      x.rho = a->d_contrib;
+      x.sigma = a->d_contrib + a->V;
+      x.order = a->d_wl_u;
+      x.level_start = a->d_wl_start;
+      x.cnt = a->d_cnt;
+      x.num_sources = a->bc_sources;
+      x.rounds_out = a->d_rounds;
       return WGM_OK;
     }
     case WGM_APP_CONNECT_FOUR: {
@@ -559,6 +598,8 @@ static cudaError_t wgm_app_enqueue(wgm_app *a, const wgm_launch &L, int grid, in
       return wgm_launch_octree(L, A.oct, grid, block, stream);
     case WGM_APP_CONNECT_FOUR:
       return wgm_launch_c4(L, A.c4, grid, block, stream);
+    case WGM_APP_PANNOTIA_BC:
+      return wgm_launch_bc(L, A.bc, grid, block, stream);
   }
   return cudaErrorInvalidValue;
 }

@@ -1355,4 +1355,163 @@ static __device__ int wgm_phase_pagerank(const wgm_launch &Lc, wgm_cta *c, const
   return WGM_PHASE_NEXT;
 }
 
+/* ------------------------------------------------------------------------ */
+/* Pannotia betweenness centrality                                           */
+/* ------------------------------------------------------------------------ */
+
+struct wgm_bc_args {
+  int V;
+  const int *row, *col;   /* out-edges */
+  const int *trow, *tcol; /* in-edges (the transpose; the graph when symmetric) */
+  float *bc;              /* [V] output */
+  int *dist;              /* [V] BFS level from the current source, -1 unreached */
+  float *rho;             /* [V] shortest-path counts x 10000 */
+  float *sigma;           /* [V] dependencies x 10000 */
+  int *order;             /* [V] reached vertices, level by level */
+  int *level_start;       /* [V + 2] first position of each level in order[] */
+  int *cnt;               /* [3 lines] vertices found for a level, by level mod 3 */
+  int num_sources;        /* sources 0 .. num_sources-1 (the reference: all V) */
+  int *rounds_out;
+};
+
+#define WGM_BC_SCALE 10000.0f /* bc.cl:230 and :131: "scaling by 10000" */
+
+/* bc.cl:1-235 (bc_combined: for every source s, clear, BFS with path
+ * counts, backtrack with dependencies).  The reference scans every vertex
+ * at every level for d[i] == level; here each level is a frontier list:
+ * BFS level L relaxes the out-edges of order[level_start[L] ..] and appends
+ * the vertices it discovers (one CAS each) as level L+1, so the backtrack
+ * walks the same lists in reverse.  Arithmetic is the reference's: rho in
+ * float scaled by 10000, rho[w] += rho[i] for every edge from level L to
+ * L+1 (bc.cl:52-56), sigma[w] += rho[w] / rho[i] * (10000 + sigma[i]) for
+ * every in-edge from level L-1 (bc.cl:122-124), bc[i] += sigma[i] / 10000
+ * for every vertex but the source (bc.cl:131); only the order of the float
+ * atomic adds differs (as between two runs of the reference).
+ * Phases: target = kind | level << 2, round = source: kind 0 clears bc,
+ * 1 clears the per-source state, 2 is a BFS level, 3 a backtrack level. */
+static __device__ int wgm_phase_bc(const wgm_launch &Lc, wgm_cta *c, const wgm_bc_args &a,
+                                   wgm_warp_smem *sm, wgm_step cur, wgm_step *nxt) {
+  const wgm_split s(c);
+  const int V = a.V, kind = cur.target & 3, L = cur.target >> 2, src = cur.round;
+  const int lane = s.lane, warp = s.warp;
+  if (kind == 0) {
+    for (int i = s.tid; i < V; i += s.nth) a.bc[i] = 0.f;
+    if (a.num_sources <= 0) {
+      if (c->id == 0 && threadIdx.x == 0 && a.rounds_out) *a.rounds_out = 0;
+      return WGM_PHASE_DONE;
+    }
+    *nxt = {1, 0};
+    return WGM_PHASE_NEXT;
+  }
+  if (kind == 1) {
+    /* clean_1d_array (bc.cl:165-181) */
+    for (int i = s.tid; i < V; i += s.nth) {
+      a.sigma[i] = 0.f;
+      a.rho[i] = i == src ? WGM_BC_SCALE : 0.f;
+      a.dist[i] = i == src ? 0 : -1;
+    }
+    if (c->id == 0 && threadIdx.x == 0) {
+      a.order[0] = src;
+      a.level_start[0] = 0;
+      a.level_start[1] = 1;
+      a.cnt[0] = 1;
+      a.cnt[1 * WGM_LINE] = 0;
+      a.cnt[2 * WGM_LINE] = 0;
+    }
+    *nxt = {2, src};
+    return WGM_PHASE_NEXT;
+  }
+  if (kind == 2) {
+    /* BFS level L (mega_bfs_kernel_func, bc.cl:16-92) */
+    const int n = __ldcg(&a.cnt[(L % 3) * WGM_LINE]);
+    const int S = __ldcg(&a.level_start[L]);
+    if (n == 0) {
+      /* no level L: the deepest is L-1, backtrack from it */
+      *nxt = {3 | ((L - 1) << 2), src};
+      return WGM_PHASE_NEXT;
+    }
+    if (L + 2 > V + 1) {
+      wgm_fail(Lc, WGM_DEV_BAD_INPUT, WGM_SITE_QUEUE, L);
+      return WGM_PHASE_DONE;
+    }
+    const int S1 = S + n;
+    if (c->id == 0 && threadIdx.x == 0) {
+      a.level_start[L + 1] = S1;
+      a.cnt[((L + 2) % 3) * WGM_LINE] = 0;
+    }
+    int *ncnt = &a.cnt[((L + 1) % 3) * WGM_LINE];
+    for (int b = s.gw * 32; b < n; b += s.NW * 32) {
+      const int k = b + lane;
+      int v = 0, start = 0, deg = 0;
+      float rv = 0.f;
+      if (k < n) {
+        v = __ldcg(&a.order[S + k]);
+        start = __ldg(&a.row[v]);
+        deg = __ldg(&a.row[v + 1]) - start;
+        rv = __ldcg(&a.rho[v]);
+      }
+      const int incl = wgm_warp_incl_scan(deg);
+      const int total = __shfl_sync(WGM_FULL, incl, 31);
+      const int off = incl - deg;
+      wgm_for_each_edge(off, deg, start - off, total, 0, 32, sm->tab[warp],
+                        [&](bool valid, int e, int owner) {
+                          const float ro = __shfl_sync(WGM_FULL, rv, owner);
+                          bool found = false;
+                          int w = 0;
+                          if (valid) {
+                            w = __ldg(&a.col[e]);
+                            int d = __ldcg(&a.dist[w]);
+                            if (d < 0) {
+                              d = atomicCAS(&a.dist[w], -1, L + 1);
+                              found = d == -1;
+                              if (found) d = L + 1;
+                            }
+                            if (d == L + 1) atomicAdd(&a.rho[w], ro);
+                          }
+                          wgm_warp_push(found, w, ncnt, a.order + S1, V - S1, false);
+                        });
+    }
+    *nxt = {2 | ((L + 1) << 2), src};
+    return WGM_PHASE_NEXT;
+  }
+  /* backtrack level L (mega_backtrack_kernel_func, bc.cl:96-140) */
+  const int S = __ldcg(&a.level_start[L]), E = __ldcg(&a.level_start[L + 1]);
+  for (int b = S + s.gw * 32; b < E; b += s.NW * 32) {
+    const int k = b + lane;
+    int v = 0, start = 0, deg = 0;
+    float rv = 1.f, sv = 0.f;
+    if (k < E) {
+      v = __ldcg(&a.order[k]);
+      start = __ldg(&a.trow[v]);
+      deg = L > 0 ? __ldg(&a.trow[v + 1]) - start : 0;
+      rv = __ldcg(&a.rho[v]);
+      sv = __ldcg(&a.sigma[v]);
+    }
+    const int incl = wgm_warp_incl_scan(deg);
+    const int total = __shfl_sync(WGM_FULL, incl, 31);
+    const int off = incl - deg;
+    wgm_for_each_edge(off, deg, start - off, total, 0, 32, sm->tab[warp],
+                      [&](bool valid, int e, int owner) {
+                        const float ri = __shfl_sync(WGM_FULL, rv, owner);
+                        const float si = __shfl_sync(WGM_FULL, sv, owner);
+                        if (valid) {
+                          const int w = __ldg(&a.tcol[e]);
+                          if (__ldcg(&a.dist[w]) == L - 1)
+                            atomicAdd(&a.sigma[w], __ldcg(&a.rho[w]) / ri * (WGM_BC_SCALE + si));
+                        }
+                      });
+    if (k < E && v != src) a.bc[v] = a.bc[v] + sv / WGM_BC_SCALE;
+  }
+  if (L > 0) {
+    *nxt = {3 | ((L - 1) << 2), src};
+    return WGM_PHASE_NEXT;
+  }
+  if (src + 1 >= a.num_sources) {
+    if (c->id == 0 && threadIdx.x == 0 && a.rounds_out) *a.rounds_out = src + 1;
+    return WGM_PHASE_DONE;
+  }
+  *nxt = {1, src + 1};
+  return WGM_PHASE_NEXT;
+}
+
 #endif

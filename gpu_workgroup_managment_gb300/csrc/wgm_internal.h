@@ -61,6 +61,7 @@ struct wgm_app {
   float damping = 0.85f;
   float dang0 = 0.f;
   int iterations = 20;
+  int bc_sources = 0; /* betweenness centrality: sources 0 .. bc_sources-1 */
   bool has_node_values = false;
   /* octree (WGM_APP_OCTREE): d_out holds the particles, V their count */
   void *d_oct_input = nullptr, *d_oct_second = nullptr, *d_oct_pools = nullptr;

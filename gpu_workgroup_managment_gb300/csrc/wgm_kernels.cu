@@ -95,6 +95,12 @@ __global__ void __launch_bounds__(1024) wgm_k_octree(wgm_launch L, wgm_octree_ar
   WGM_PERSISTENT_EPILOGUE
 }
 
+__global__ void __launch_bounds__(1024) wgm_k_bc(wgm_launch L, wgm_bc_args a) {
+  WGM_PERSISTENT_PROLOGUE
+  WGM_DRIVE(wgm_phase_bc(L, &c, a, &sm, cur, nxt));
+  WGM_PERSISTENT_EPILOGUE
+}
+
 /* Standalone connect-four look-ahead (connect_four.cl:350-487 without a
  * scheduler). */
 __global__ void __launch_bounds__(1024) wgm_k_c4(wgm_launch L, wgm_c4_args a) {
@@ -116,6 +122,7 @@ const void *wgm_kernel_fn(int kid) {
     case WGM_K_BARRIER_BENCH: return (const void *)wgm_k_barrier_bench;
     case WGM_K_OCTREE: return (const void *)wgm_k_octree;
     case WGM_K_C4: return (const void *)wgm_k_c4;
+    case WGM_K_BC: return (const void *)wgm_k_bc;
     default: return nullptr;
   }
 }
@@ -151,6 +158,11 @@ cudaError_t wgm_launch_pagerank(const wgm_launch &L, const wgm_pr_args &a, int g
 cudaError_t wgm_launch_octree(const wgm_launch &L, const wgm_octree_args &a, int grid, int block,
                               cudaStream_t s) {
   wgm_k_octree<<<grid, block, 0, s>>>(L, a);
+  return cudaGetLastError();
+}
+cudaError_t wgm_launch_bc(const wgm_launch &L, const wgm_bc_args &a, int grid, int block,
+                          cudaStream_t s) {
+  wgm_k_bc<<<grid, block, 0, s>>>(L, a);
   return cudaGetLastError();
 }
 cudaError_t wgm_launch_c4(const wgm_launch &L, const wgm_c4_args &a, int grid, int block,

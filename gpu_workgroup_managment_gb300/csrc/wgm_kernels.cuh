@@ -26,6 +26,7 @@ enum wgm_kernel_id {
   WGM_K_BARRIER_BENCH,
   WGM_K_OCTREE,
   WGM_K_C4,
+  WGM_K_BC,
   WGM_K_COUNT
 };
 
@@ -50,6 +51,8 @@ cudaError_t wgm_launch_pagerank(const wgm_launch &L, const wgm_pr_args &a, int g
                                 cudaStream_t s);
 cudaError_t wgm_launch_octree(const wgm_launch &L, const wgm_octree_args &a, int grid, int block,
                               cudaStream_t s);
+cudaError_t wgm_launch_bc(const wgm_launch &L, const wgm_bc_args &a, int grid, int block,
+                          cudaStream_t s);
 cudaError_t wgm_launch_c4(const wgm_launch &L, const wgm_c4_args &a, int grid, int block,
                           cudaStream_t s);
 cudaError_t wgm_launch_barrier_bench(const wgm_launch &L, const wgm_barrier_bench_args &a,

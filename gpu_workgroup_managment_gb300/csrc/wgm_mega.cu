@@ -95,6 +95,11 @@ __device__ __forceinline__ void wgm_mega_run_app(const wgm_launch &L, const wgm_
         return wgm_phase_pagerank(L, pc, A.pr, sm, cur, nxt);
       });
       break;
+    case WGM_K_BC:
+      wgm_drive(L, pc, start, sync, [&](wgm_step cur, wgm_step *nxt) {
+        return wgm_phase_bc(L, pc, A.bc, sm, cur, nxt);
+      });
+      break;
     case WGM_K_OCTREE:
       /* octree.cl:170-180: init and one resizing barrier, then the task
        * loop with an offer at the top of every iteration */

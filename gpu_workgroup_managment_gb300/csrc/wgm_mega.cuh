@@ -51,6 +51,7 @@ struct wgm_mega_args {
   wgm_mis_args mis;
   wgm_psssp_args psssp;
   wgm_pr_args pr;
+  wgm_bc_args bc;
   wgm_octree_args oct;
   wgm_c4_args c4;
   wgm_np_args np;

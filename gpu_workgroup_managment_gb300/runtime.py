@@ -22,11 +22,13 @@ APPS = {
     "mis": L.APP_PANNOTIA_MIS,
     "sssp": L.APP_PANNOTIA_SSSP,
     "pagerank": L.APP_PAGERANK,
+    "bc": L.APP_PANNOTIA_BC,
 }
 _RESULT_DTYPE = {
     L.APP_LONESTAR_BFS: np.uint32, L.APP_LONESTAR_SSSP: np.uint32,
     L.APP_PANNOTIA_COLOR: np.int32, L.APP_PANNOTIA_MIS: np.int32,
     L.APP_PANNOTIA_SSSP: np.int32, L.APP_PAGERANK: np.float32,
+    L.APP_PANNOTIA_BC: np.float32,
 }
 
 
@@ -167,7 +169,7 @@ class PersistentApp:
 
     def __init__(self, rt: Runtime, app: str | int, graph: Graph, source: int = 0,
                  node_values: np.ndarray | None = None, damping: float = 0.85,
-                 iterations: int = 20):
+                 iterations: int = 20, bc_sources: int | None = None):
         self.rt = rt
         self.kind = APPS[app] if isinstance(app, str) else app
         self.graph = graph
@@ -182,6 +184,8 @@ class PersistentApp:
             self.set_node_values(node_values)
         if self.kind == L.APP_PAGERANK:
             check(lib.wgm_app_set_pagerank(self._h, damping, iterations))
+        if self.kind == L.APP_PANNOTIA_BC and bc_sources is not None:
+            check(lib.wgm_app_set_bc_sources(self._h, bc_sources))
 
     @property
     def name(self) -> str:

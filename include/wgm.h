@@ -59,6 +59,7 @@ extern "C" {
 #define WGM_APP_PAGERANK 6
 #define WGM_APP_OCTREE 7 /* work-stealing octree build (test_suite/final_octree) */
 #define WGM_APP_CONNECT_FOUR 8 /* work-stealing look-ahead (test_suite/connect_four) */
+#define WGM_APP_PANNOTIA_BC 9  /* betweenness centrality (pannotia/graph_apps/bc) */
 
 typedef struct wgm_runtime wgm_runtime;
 typedef struct wgm_app wgm_app;
@@ -156,6 +157,9 @@ int wgm_app_set_source(wgm_app *app, int32_t source);
 /* Colour/MIS priorities node_value[V] (color.h:49-55, mis.h:52-56). */
 int wgm_app_set_node_values(wgm_app *app, const float *node_value);
 int wgm_app_set_pagerank(wgm_app *app, float damping, int iterations);
+/* Betweenness centrality from sources 0 .. num_sources-1 (bc.cl:160-235
+ * loops over every vertex; a smaller count bounds the run on big graphs). */
+int wgm_app_set_bc_sources(wgm_app *app, int32_t num_sources);
 /* One iteration of run_persistent (skel.cpp:316-355): launch the persistent
  * kernel on up to num_wgs groups (<=0: all co-resident) and wait. */
 int wgm_run_persistent(wgm_runtime *rt, wgm_app *app, int num_wgs, wgm_run_stats *stats);

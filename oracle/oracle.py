@@ -54,6 +54,7 @@ def lib() -> C.CDLL:
             "oracle_matmult_f32": [P, I, I, P, I, P],
             "oracle_batch_lonestar": [I, P, P, P, P, P, P, P, P, P, P],
             "oracle_connect_four": [P, I, P],
+            "oracle_pannotia_bc_f64": [I, P, P, I, P],
         }
         for name, args in protos.items():
             fn = getattr(_lib, name)
@@ -117,6 +118,17 @@ class BatchArena:
                                     _p(self.dist_off), _p(self.algo), _p(self.source),
                                     _p(self.rows), _p(self.cols), _p(self.wts), _p(self.dist))
         return self.dist
+
+
+def pannotia_bc_f64(g, num_sources: int | None = None) -> np.ndarray:
+    """Betweenness centrality of pannotia bc.cl in float64, sources
+    0 .. num_sources-1 (all by default)."""
+    V = g.num_nodes
+    out = np.empty(V, np.float64)
+    n = V if num_sources is None else num_sources
+    if lib().oracle_pannotia_bc_f64(V, _p(g.row_ptr), _p(g.col), n, _p(out)) != 0:
+        raise MemoryError("oracle_pannotia_bc_f64")
+    return out
 
 
 def connect_four(board: np.ndarray, maxlevel: int = 6) -> np.ndarray:

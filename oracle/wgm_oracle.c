@@ -706,3 +706,69 @@ int oracle_connect_four(const uint8_t *board, int32_t maxlevel, int32_t *next_mo
   }
   return 0;
 }
+
+/* ---- Pannotia betweenness centrality (pannotia/graph_apps/bc/device/bc.cl) ---- */
+
+/* bc_combined in double precision: for every source s < num_sources a BFS
+ * over out-edges counting shortest paths (rho), then levels in reverse:
+ * every vertex i at level L adds rho[w]/rho[i] * (1 + sigma[i]) to sigma[w]
+ * of each in-neighbour w at level L-1 (bc.cl:122-124) and, unless it is s,
+ * sigma[i] to bc[i] (bc.cl:131).  The reference's factor 10000 on rho and
+ * sigma cancels.  The GPU computes in float; tests compare within a
+ * stated tolerance. */
+int oracle_pannotia_bc_f64(int32_t V, const int32_t *row, const int32_t *col,
+                           int32_t num_sources, double *bc) {
+  const int64_t E = row[V];
+  int32_t *trow = calloc((size_t)V + 1, sizeof(int32_t));
+  int32_t *tcol = malloc(sizeof(int32_t) * (size_t)(E > 0 ? E : 1));
+  int32_t *fill = malloc(sizeof(int32_t) * (size_t)V + 4);
+  int32_t *dist = malloc(sizeof(int32_t) * (size_t)V + 4);
+  int32_t *order = malloc(sizeof(int32_t) * (size_t)V + 4);
+  double *rho = malloc(sizeof(double) * (size_t)V + 8);
+  double *sigma = malloc(sizeof(double) * (size_t)V + 8);
+  if (!trow || !tcol || !fill || !dist || !order || !rho || !sigma) return -1;
+  for (int64_t e = 0; e < E; e++) trow[col[e] + 1]++;
+  for (int32_t v = 0; v < V; v++) trow[v + 1] += trow[v];
+  for (int32_t v = 0; v < V; v++) fill[v] = trow[v];
+  for (int32_t v = 0; v < V; v++)
+    for (int32_t e = row[v]; e < row[v + 1]; e++) tcol[fill[col[e]]++] = v;
+  for (int32_t v = 0; v < V; v++) bc[v] = 0.0;
+  for (int32_t s = 0; s < num_sources && s < V; s++) {
+    for (int32_t v = 0; v < V; v++) {
+      dist[v] = -1;
+      rho[v] = 0.0;
+      sigma[v] = 0.0;
+    }
+    dist[s] = 0;
+    rho[s] = 1.0;
+    int32_t head = 0, tail = 0;
+    order[tail++] = s;
+    while (head < tail) {
+      const int32_t i = order[head++];
+      for (int32_t e = row[i]; e < row[i + 1]; e++) {
+        const int32_t w = col[e];
+        if (dist[w] < 0) {
+          dist[w] = dist[i] + 1;
+          order[tail++] = w;
+        }
+        if (dist[w] == dist[i] + 1) rho[w] += rho[i];
+      }
+    }
+    for (int32_t k = tail - 1; k >= 0; k--) {
+      const int32_t i = order[k];
+      for (int32_t e = trow[i]; e < trow[i + 1]; e++) {
+        const int32_t w = tcol[e];
+        if (dist[w] == dist[i] - 1) sigma[w] += rho[w] / rho[i] * (1.0 + sigma[i]);
+      }
+      if (i != s) bc[i] += sigma[i];
+    }
+  }
+  free(trow);
+  free(tcol);
+  free(fill);
+  free(dist);
+  free(order);
+  free(rho);
+  free(sigma);
+  return 0;
+}

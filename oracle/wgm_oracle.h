@@ -123,6 +123,11 @@ int oracle_omp_threads(void);
  * computer), maxlevel moves of look-ahead (1..7).  Returns 0, or -1. */
 int oracle_connect_four(const uint8_t *board, int32_t maxlevel, int32_t *next_move_value);
 
+/* Pannotia betweenness centrality (bc.cl) in double precision, sources
+ * 0 .. num_sources-1.  Returns 0, or -1 when memory runs out. */
+int oracle_pannotia_bc_f64(int32_t V, const int32_t *row, const int32_t *col,
+                           int32_t num_sources, double *bc);
+
 #ifdef __cplusplus
 }
 #endif

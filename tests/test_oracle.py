@@ -169,3 +169,19 @@ def test_connect_four_oracle_known_answer():
         d = json.load(f)
     got = oracle.connect_four(np.array(d["board"], np.uint8), d["maxlevel"])
     assert got.tolist() == d["next_move_value"]
+
+
+def test_bc_oracle_matches_networkx():
+    """The float64 restatement of bc.cl is Brandes' betweenness over ordered
+    pairs: networkx on the same directed graph agrees."""
+    nx = pytest.importorskip("networkx")
+    for g in (graphs.rmat(7, 4, seed=3), graphs.grid(6, 9)):
+        G = nx.DiGraph()
+        G.add_nodes_from(range(g.num_nodes))
+        src = np.repeat(np.arange(g.num_nodes), np.diff(g.row_ptr))
+        G.add_edges_from(zip(src.tolist(), g.col.tolist()))
+        want = nx.betweenness_centrality(G, normalized=False)
+        got = oracle.pannotia_bc_f64(g)
+        assert np.allclose(got, [want[v] for v in range(g.num_nodes)], rtol=1e-9, atol=1e-9)
+        part = oracle.pannotia_bc_f64(g, 5)  # the first 5 sources only
+        assert np.all(part <= got + 1e-9)
