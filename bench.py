@@ -266,6 +266,24 @@ def _octree(rt) -> dict:
                 "groups": runs[0].groups, "check": oc.check()}
 
 
+def _bc(rt) -> dict:
+    """Pannotia betweenness centrality on RMAT-12 (edge factor 16, seed 1),
+    every vertex a source: sources over CTAs (shared-memory state) and one
+    source at a time over the grid (bc.cl's shape); best of 3, CUDA events.
+    Rate = sources x edges / time (each source walks every reached edge
+    twice)."""
+    from gpu_workgroup_managment_gb300 import PersistentApp, graphs
+    g = graphs.rmat(12, 16, seed=1)
+    out = {"vertices": g.num_nodes, "edges": g.num_edges, "sources": g.num_nodes}
+    for mode, name in ((1, "sources_over_ctas"), (0, "levels_over_grid")):
+        with PersistentApp(rt, "bc", g, bc_mode=mode) as a:
+            a.run()
+            ms = min(a.run().kernel_ms for _ in range(3 if mode else 1))
+        out[name + "_ms"] = ms
+        out[name + "_gteps"] = g.num_nodes * g.num_edges / (ms * 1e-3) / 1e9
+    return out
+
+
 def _sssp_kernel_only(args) -> int:
     """The command profiled with ncu for the persistent SSSP kernel."""
     from gpu_workgroup_managment_gb300 import Runtime
@@ -493,6 +511,10 @@ def main() -> int:
             extra["octree"] = _octree(rt)
         except Exception as exc:  # reported, not hidden
             extra["octree"] = {"error": repr(exc)}
+        try:
+            extra["bc_rmat12"] = _bc(rt)
+        except Exception as exc:  # reported, not hidden
+            extra["bc_rmat12"] = {"error": repr(exc)}
         try:
             extra["served"] = _served(rt)
         except Exception as exc:  # reported, not hidden

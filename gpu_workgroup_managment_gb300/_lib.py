@@ -100,6 +100,7 @@ _PROTOS = {
     "wgm_octree_check": (_I, [_P, _P]),
     "wgm_c4_create": (_I, [_P, _P, C.c_int32, C.c_int32, C.POINTER(_P)]),
     "wgm_app_set_bc_sources": (_I, [_P, C.c_int32]),
+    "wgm_app_set_bc_mode": (_I, [_P, C.c_int32]),
     "wgm_app_upload": (_I, [_P, C.POINTER(WgmGraphDesc)]),
     "wgm_app_set_source": (_I, [_P, C.c_int32]),
     "wgm_app_set_node_values": (_I, [_P, _P]),

@@ -339,6 +339,7 @@ extern "C" int wgm_app_create(wgm_runtime *rt, int kind, const wgm_graph_desc *g
       /* bc (out), dist, rho and sigma, the level lists and their starts */
       a->out_bytes = V * 4;
       a->bc_sources = a->V;
+      a->bc_mode = a->V <= WGM_BC_CTA_MAX_V ? 1 : 0;
       if (e == cudaSuccess) e = cudaMalloc(&a->d_out, a->out_bytes);
       if (e == cudaSuccess) e = wgm_dmalloc(&a->d_stamp, V);
       if (e == cudaSuccess) e = wgm_dmalloc(&a->d_contrib, 2 * V);
@@ -397,6 +398,28 @@ extern "C" int wgm_app_set_node_values(wgm_app *a, const float *nv) {
   if (e == cudaSuccess) e = cudaStreamSynchronize(a->rt->stream);
   if (e != cudaSuccess) return wgm_cuda_fail(a->rt, e);
   a->has_node_values = true;
+  return WGM_OK;
+}
+
+extern "C" int wgm_app_set_bc_mode(wgm_app *a, int32_t mode) {
+  if (!a || a->kind != WGM_APP_PANNOTIA_BC || mode < 0 || mode > 1 ||
+      (mode == 1 && a->V > WGM_BC_CTA_MAX_V))
+    return WGM_ERR_INVALID;
+  a->bc_mode = mode;
+  return WGM_OK;
+}
+
+static int wgm_block_size(const wgm_runtime *rt);
+
+/* Sources spread over CTAs (bc_mode 1): a plain launch of resident CTAs, no
+ * discovery and no host handshake, so the launch generation is untouched. */
+static int wgm_bc_cta_launch(wgm_runtime *rt, wgm_app *a, cudaStream_t s) {
+  wgm_mega_args A;
+  std::memset(&A, 0, sizeof(A));
+  int st = wgm_app_fill_mega(a, &A);
+  if (st) return st;
+  cudaError_t e = wgm_launch_bc_cta(A.bc, a->d_cnt + 2 * WGM_LINE, wgm_block_size(rt), s);
+  if (e != cudaSuccess) return wgm_cuda_fail(rt, e);
   return WGM_OK;
 }
 
@@ -622,6 +645,8 @@ static int wgm_block_size(const wgm_runtime *rt) {
 extern "C" int wgm_launch_persistent(wgm_runtime *rt, wgm_app *a, int num_wgs, void *stream) {
   if (!rt || !a || a->rt != rt) return WGM_ERR_INVALID;
   cudaSetDevice(rt->device);
+  if (a->kind == WGM_APP_PANNOTIA_BC && a->bc_mode == 1)
+    return wgm_bc_cta_launch(rt, a, stream ? (cudaStream_t)stream : rt->stream);
   int block = wgm_block_size(rt), grid = 0;
   int s = wgm_pick_grid(a, num_wgs, block, &grid);
   if (s) return s;
@@ -639,6 +664,26 @@ extern "C" int wgm_run_persistent(wgm_runtime *rt, wgm_app *a, int num_wgs,
                                   wgm_run_stats *stats) {
   if (!rt || !a || a->rt != rt) return WGM_ERR_INVALID;
   cudaSetDevice(rt->device);
+  if (a->kind == WGM_APP_PANNOTIA_BC && a->bc_mode == 1) {
+    cudaError_t e = cudaEventRecord(rt->ev0, rt->stream);
+    if (e != cudaSuccess) return wgm_cuda_fail(rt, e);
+    int s = wgm_bc_cta_launch(rt, a, rt->stream);
+    if (s) return s;
+    e = cudaEventRecord(rt->ev1, rt->stream);
+    if (e != cudaSuccess) return wgm_cuda_fail(rt, e);
+    s = wgm_stream_wait(rt, rt->stream);
+    if (s) return s;
+    if (stats) {
+      std::memset(stats, 0, sizeof(*stats));
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, rt->ev0, rt->ev1);
+      stats->kernel_ms = ms;
+      int rounds = 0;
+      if (cudaMemcpy(&rounds, a->d_rounds, 4, cudaMemcpyDeviceToHost) == cudaSuccess)
+        stats->rounds = rounds;
+    }
+    return WGM_OK;
+  }
   int block = wgm_block_size(rt), grid = 0;
   int s = wgm_pick_grid(a, num_wgs, block, &grid);
   if (s) return s;

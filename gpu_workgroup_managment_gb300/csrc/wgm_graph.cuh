@@ -1514,4 +1514,108 @@ static __device__ int wgm_phase_bc(const wgm_launch &Lc, wgm_cta *c, const wgm_b
   return WGM_PHASE_NEXT;
 }
 
+/* Betweenness centrality with the sources spread over CTAs: a CTA takes a
+ * source from a queue and runs its BFS and backtrack alone, with dist, rho,
+ * sigma, the level lists and their starts in shared memory (20 bytes per
+ * vertex) and __syncthreads as the level barrier; bc gathers the
+ * dependencies with global float atomics.  Same arithmetic as wgm_phase_bc,
+ * no grid barrier at all: sources, not levels, are the parallel units.  For
+ * graphs of at most WGM_BC_CTA_MAX_V vertices. */
+#define WGM_BC_CTA_MAX_V 10240
+
+
+static __device__ void wgm_bc_cta_source(const wgm_bc_args &a, int src, int *dist, float *rho,
+                                  float *sig, int *order, int *ls, int *s_cnt, int *tab) {
+  const int V = a.V, lane = wgm_lane(), warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int i = threadIdx.x; i < V; i += blockDim.x) {
+    dist[i] = i == src ? 0 : -1;
+    rho[i] = i == src ? WGM_BC_SCALE : 0.f;
+    sig[i] = 0.f;
+  }
+  if (threadIdx.x == 0) {
+    order[0] = src;
+    ls[0] = 0;
+    ls[1] = 1;
+    *s_cnt = 0;
+  }
+  __syncthreads();
+  int L = 0, S = 0, n = 1;
+  for (;;) {
+    const int S1 = S + n;
+    for (int b = warp * 32; b < n; b += nw * 32) {
+      const int k = b + lane;
+      int v = 0, start = 0, deg = 0;
+      float rv = 0.f;
+      if (k < n) {
+        v = order[S + k];
+        start = __ldg(&a.row[v]);
+        deg = __ldg(&a.row[v + 1]) - start;
+        rv = rho[v];
+      }
+      const int incl = wgm_warp_incl_scan(deg);
+      const int total = __shfl_sync(WGM_FULL, incl, 31);
+      const int off = incl - deg;
+      wgm_for_each_edge(off, deg, start - off, total, 0, 32, tab + warp * 32,
+                        [&](bool valid, int e, int owner) {
+                          const float ro = __shfl_sync(WGM_FULL, rv, owner);
+                          bool found = false;
+                          int w = 0;
+                          if (valid) {
+                            w = __ldg(&a.col[e]);
+                            int d = dist[w];
+                            if (d < 0) {
+                              d = atomicCAS(&dist[w], -1, L + 1);
+                              found = d == -1;
+                              if (found) d = L + 1;
+                            }
+                            if (d == L + 1) atomicAdd(&rho[w], ro);
+                          }
+                          wgm_warp_push(found, w, s_cnt, order + S1, V - S1, false);
+                        });
+    }
+    __syncthreads();
+    const int n2 = *s_cnt;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      *s_cnt = 0;
+      ls[L + 2] = S1 + n2;
+    }
+    if (n2 == 0) break;
+    S = S1;
+    n = n2;
+    L++;
+  }
+  __syncthreads();
+  for (int l = L; l >= 0; l--) {
+    const int B = ls[l], E = ls[l + 1];
+    for (int b = B + warp * 32; b < E; b += nw * 32) {
+      const int k = b + lane;
+      int v = 0, start = 0, deg = 0;
+      float rv = 1.f, sv = 0.f;
+      if (k < E) {
+        v = order[k];
+        start = __ldg(&a.trow[v]);
+        deg = l > 0 ? __ldg(&a.trow[v + 1]) - start : 0;
+        rv = rho[v];
+        sv = sig[v];
+      }
+      const int incl = wgm_warp_incl_scan(deg);
+      const int total = __shfl_sync(WGM_FULL, incl, 31);
+      const int off = incl - deg;
+      wgm_for_each_edge(off, deg, start - off, total, 0, 32, tab + warp * 32,
+                        [&](bool valid, int e, int owner) {
+                          const float ri = __shfl_sync(WGM_FULL, rv, owner);
+                          const float si = __shfl_sync(WGM_FULL, sv, owner);
+                          if (valid) {
+                            const int w = __ldg(&a.tcol[e]);
+                            if (dist[w] == l - 1)
+                              atomicAdd(&sig[w], rho[w] / ri * (WGM_BC_SCALE + si));
+                          }
+                        });
+      if (k < E && v != src && sv != 0.f) atomicAdd(&a.bc[v], sv / WGM_BC_SCALE);
+    }
+    __syncthreads();
+  }
+}
+
 #endif

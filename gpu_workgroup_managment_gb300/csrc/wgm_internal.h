@@ -62,6 +62,7 @@ struct wgm_app {
   float dang0 = 0.f;
   int iterations = 20;
   int bc_sources = 0; /* betweenness centrality: sources 0 .. bc_sources-1 */
+  int bc_mode = 0;    /* 0: one source at a time over the grid, 1: sources over CTAs */
   bool has_node_values = false;
   /* octree (WGM_APP_OCTREE): d_out holds the particles, V their count */
   void *d_oct_input = nullptr, *d_oct_second = nullptr, *d_oct_pools = nullptr;

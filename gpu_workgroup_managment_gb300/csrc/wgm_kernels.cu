@@ -101,6 +101,29 @@ __global__ void __launch_bounds__(1024) wgm_k_bc(wgm_launch L, wgm_bc_args a) {
   WGM_PERSISTENT_EPILOGUE
 }
 
+/* Betweenness centrality, sources spread over CTAs (wgm_bc_cta_source):
+ * a plain grid of resident CTAs pulling sources from a queue, no discovery
+ * and no grid barrier. */
+__global__ void __launch_bounds__(1024) wgm_k_bc_cta(wgm_bc_args a, int *queue) {
+  extern __shared__ int wgm_bc_dyn[];
+  __shared__ int tab[32 * 32];
+  __shared__ int s_cnt, s_src;
+  int *dist = wgm_bc_dyn;
+  float *rho = reinterpret_cast<float *>(dist + a.V);
+  float *sig = rho + a.V;
+  int *order = reinterpret_cast<int *>(sig + a.V);
+  int *ls = order + a.V;
+  for (;;) {
+    if (threadIdx.x == 0) s_src = atomicAdd(queue, 1);
+    __syncthreads();
+    const int src = s_src;
+    __syncthreads();
+    if (src >= a.num_sources) break;
+    wgm_bc_cta_source(a, src, dist, rho, sig, order, ls, &s_cnt, tab);
+    if (threadIdx.x == 0 && a.rounds_out) atomicAdd(a.rounds_out, 1);
+  }
+}
+
 /* Standalone connect-four look-ahead (connect_four.cl:350-487 without a
  * scheduler). */
 __global__ void __launch_bounds__(1024) wgm_k_c4(wgm_launch L, wgm_c4_args a) {
@@ -163,6 +186,23 @@ cudaError_t wgm_launch_octree(const wgm_launch &L, const wgm_octree_args &a, int
 cudaError_t wgm_launch_bc(const wgm_launch &L, const wgm_bc_args &a, int grid, int block,
                           cudaStream_t s) {
   wgm_k_bc<<<grid, block, 0, s>>>(L, a);
+  return cudaGetLastError();
+}
+cudaError_t wgm_launch_bc_cta(const wgm_bc_args &a, int *queue, int block, cudaStream_t s) {
+  const size_t smem = (size_t)a.V * 20 + 16;
+  cudaError_t e = cudaFuncSetAttribute(wgm_k_bc_cta, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  int per_sm = 0, dev = 0, sms = 0;
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wgm_k_bc_cta, block, smem);
+  if (e == cudaSuccess) e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  e = cudaMemsetAsync(a.bc, 0, (size_t)a.V * 4, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(queue, 0, 4, s);
+  if (e == cudaSuccess && a.rounds_out) e = cudaMemsetAsync(a.rounds_out, 0, 4, s);
+  if (e != cudaSuccess) return e;
+  wgm_k_bc_cta<<<per_sm * sms, block, smem, s>>>(a, queue);
   return cudaGetLastError();
 }
 cudaError_t wgm_launch_c4(const wgm_launch &L, const wgm_c4_args &a, int grid, int block,

@@ -53,6 +53,7 @@ cudaError_t wgm_launch_octree(const wgm_launch &L, const wgm_octree_args &a, int
                               cudaStream_t s);
 cudaError_t wgm_launch_bc(const wgm_launch &L, const wgm_bc_args &a, int grid, int block,
                           cudaStream_t s);
+cudaError_t wgm_launch_bc_cta(const wgm_bc_args &a, int *queue, int block, cudaStream_t s);
 cudaError_t wgm_launch_c4(const wgm_launch &L, const wgm_c4_args &a, int grid, int block,
                           cudaStream_t s);
 cudaError_t wgm_launch_barrier_bench(const wgm_launch &L, const wgm_barrier_bench_args &a,

@@ -160,6 +160,12 @@ int wgm_app_set_pagerank(wgm_app *app, float damping, int iterations);
 /* Betweenness centrality from sources 0 .. num_sources-1 (bc.cl:160-235
  * loops over every vertex; a smaller count bounds the run on big graphs). */
 int wgm_app_set_bc_sources(wgm_app *app, int32_t num_sources);
+/* How a standalone run spreads the work (no reference counterpart): 0 one
+ * source at a time over every group, a barrier per level (bc.cl's shape;
+ * the megakernel always runs this); 1 the sources over the CTAs, each
+ * source's state in shared memory, no grid barrier (graphs of at most
+ * 10240 vertices; the default there).  Same arithmetic, same tolerance. */
+int wgm_app_set_bc_mode(wgm_app *app, int32_t mode);
 /* One iteration of run_persistent (skel.cpp:316-355): launch the persistent
  * kernel on up to num_wgs groups (<=0: all co-resident) and wait. */
 int wgm_run_persistent(wgm_runtime *rt, wgm_app *app, int num_wgs, wgm_run_stats *stats);
