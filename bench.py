@@ -266,6 +266,65 @@ def _octree(rt) -> dict:
                 "groups": runs[0].groups, "check": oc.check()}
 
 
+def _best(app, k: int = 5):
+    app.run()
+    return min((app.run() for _ in range(k)), key=lambda s: s.kernel_ms)
+
+
+def _c1(rt, barrier_ns) -> dict:
+    """C1: plain persistent BFS on the 256x256 4-neighbour grid from vertex 0
+    (Lonestar view), one launch per run, CUDA events, best of 5.  Bytes_alg
+    = 8 E_t + 20 V_r; ns per level and the barrier's share of it."""
+    from gpu_workgroup_managment_gb300 import PersistentApp, graphs
+    g = graphs.lonestar_view(graphs.grid(256, 256))
+    with PersistentApp(rt, "lonestar_bfs", g) as a:
+        st = _best(a)
+        d = a.result()
+    reached = d != INF
+    et, vr = int(np.diff(g.row_ptr)[reached].clip(min=0).sum()), int(reached.sum())
+    peak, kind = _peak_hbm()
+    s = st.kernel_ms * 1e-3
+    out = {"ms": st.kernel_ms, "levels": st.rounds, "groups": st.groups,
+           "gteps": et / s / 1e9, "gteps_undirected": et / 2 / s / 1e9,
+           "ns_per_level": st.kernel_ms * 1e6 / max(st.rounds, 1),
+           "gbs_alg": (8 * et + 20 * vr) / s / 1e9,
+           "frac_of_" + kind: (8 * et + 20 * vr) / s / 1e9 / peak}
+    if barrier_ns:
+        out["barrier_share"] = barrier_ns * st.rounds / (st.kernel_ms * 1e6)
+    return out
+
+
+def _c2(rt, _barrier_ns) -> dict:
+    """C2: RMAT-20 (edge factor 16, seed 1) persistent Lonestar SSSP from
+    the max-degree vertex, Pannotia colour and MIS with seeded priorities;
+    best of 5 launches each."""
+    from gpu_workgroup_managment_gb300 import PersistentApp, graphs
+    g = graphs.rmat(20, 16, seed=1)
+    nv = graphs.seeded_node_values(g.num_nodes, 1)
+    src = graphs.max_degree_vertex(g)
+    out = {}
+    for app, kw in (("lonestar_sssp", {"source": src}), ("color", {"node_values": nv}),
+                    ("mis", {"node_values": nv})):
+        with PersistentApp(rt, app, g, **kw) as a:
+            st = _best(a)
+        out[app] = {"ms": st.kernel_ms, "rounds": st.rounds, "groups": st.groups}
+    return out
+
+
+def _c3(rt, _barrier_ns) -> dict:
+    """C3: PageRank on RMAT-22 (edge factor 16, seed 1), 20 iterations, best
+    of 3; Bytes_alg per iteration = 8 E + 16 V."""
+    from gpu_workgroup_managment_gb300 import PersistentApp, graphs
+    g = graphs.rmat(22, 16, seed=1)
+    with PersistentApp(rt, "pagerank", g, iterations=20) as a:
+        st = _best(a, 3)
+    s = st.kernel_ms * 1e-3
+    peak, kind = _peak_hbm()
+    gbs = 20 * (8 * g.num_edges + 16 * g.num_nodes) / s / 1e9
+    return {"ms": st.kernel_ms, "iterations": 20, "groups": st.groups, "gbs_alg": gbs,
+            "frac_of_" + kind: gbs / peak}
+
+
 def _bc(rt) -> dict:
     """Pannotia betweenness centrality on RMAT-12 (edge factor 16, seed 1),
     every vertex a source: sources over CTAs (shared-memory state) and one
@@ -515,6 +574,11 @@ def main() -> int:
             extra["bc_rmat12"] = _bc(rt)
         except Exception as exc:  # reported, not hidden
             extra["bc_rmat12"] = {"error": repr(exc)}
+        for key, fn in (("c1_bfs_grid256", _c1), ("c2_rmat20", _c2), ("c3_pagerank_rmat22", _c3)):
+            try:
+                extra[key] = fn(rt, extra.get("barrier_ns_1024_threads"))
+            except Exception as exc:  # reported, not hidden
+                extra[key] = {"error": repr(exc)}
         try:
             extra["served"] = _served(rt)
         except Exception as exc:  # reported, not hidden
