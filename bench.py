@@ -251,13 +251,13 @@ def _sssp_rmat(rt, scale: int, steps: int, warmup: int) -> dict:
             "bytes_alg": 12 * et + 36 * vr + 8 * g.num_nodes}
 
 
-def _octree(rt) -> dict:
+def _octree(rt, n: int = 3_000_000) -> dict:
     """The work-stealing octree build at the reference's defaults
     (octree.h: 3,000,000 particles, maxChildren 5, pool size 50,000):
     standalone persistent launches, CUDA events, best of 3 after a warm-up,
     the reference's check on the last one."""
     from gpu_workgroup_managment_gb300.octree import Octree, clustered_particles
-    pts = clustered_particles(3_000_000, seed=1)
+    pts = clustered_particles(n, seed=1)
     with Octree(rt, pts) as oc:
         oc.run()
         runs = [oc.run() for _ in range(3)]
@@ -413,9 +413,23 @@ def main() -> int:
     ap.add_argument("--barrier-sweep", action="store_true",
                     help="ns per barrier for every barrier kind and CTA size")
     ap.add_argument("--served", action="store_true", help="served-form measurement only")
+    ap.add_argument("--only", choices=["octree", "bc", "c1", "c3"],
+                    help="one extra measurement alone (the commands profiled with ncu)")
+    ap.add_argument("--particles", type=int, default=3_000_000, help="octree size for --only")
     args = ap.parse_args()
     if args.barrier_sweep:
         return _barrier_sweep()
+    if args.only:
+        from gpu_workgroup_managment_gb300 import Runtime
+        with Runtime() as rt:
+            if args.only == "octree":
+                r = _octree(rt, args.particles)
+            elif args.only == "bc":
+                r = _bc(rt)
+            else:
+                r = {"c1": _c1, "c3": _c3}[args.only](rt, None)
+        print(json.dumps({"only": args.only, **r}))
+        return 0
     if args.sssp_kernel_only:
         return _sssp_kernel_only(args)
     ws, rank, local = _dist_env()
