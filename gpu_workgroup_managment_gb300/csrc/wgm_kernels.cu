@@ -13,6 +13,15 @@
     return;                                                      \
   }
 
+/* The same for task loops that need no per-warp edge tables. */
+#define WGM_PERSISTENT_PROLOGUE_TASKS                            \
+  __shared__ wgm_cta c;                                          \
+  if (!wgm_discover(L, &c)) return;                              \
+  if (L.handshake && !wgm_standalone_handshake(L, &c)) {         \
+    wgm_standalone_exit(L);                                      \
+    return;                                                      \
+  }
+
 #define WGM_PERSISTENT_EPILOGUE \
   if (L.handshake) wgm_standalone_exit(L);
 
@@ -88,8 +97,7 @@ __global__ void __launch_bounds__(1024) wgm_k_barrier_bench(wgm_launch L,
 /* Standalone octree build (octree.cl:150-320 without a scheduler): init,
  * one barrier, then the task loop; nothing is offered to kill or fork. */
 __global__ void __launch_bounds__(1024) wgm_k_octree(wgm_launch L, wgm_octree_args a) {
-  WGM_PERSISTENT_PROLOGUE
-  (void)sm;
+  WGM_PERSISTENT_PROLOGUE_TASKS
   wgm_octree_init(L, &c, a);
   if (wgm_barrier(L, &c)) wgm_octree_loop(L, &c, a, [](wgm_cta *) { return false; });
   WGM_PERSISTENT_EPILOGUE
@@ -127,8 +135,7 @@ __global__ void __launch_bounds__(1024) wgm_k_bc_cta(wgm_bc_args a, int *queue) 
 /* Standalone connect-four look-ahead (connect_four.cl:350-487 without a
  * scheduler). */
 __global__ void __launch_bounds__(1024) wgm_k_c4(wgm_launch L, wgm_c4_args a) {
-  WGM_PERSISTENT_PROLOGUE
-  (void)sm;
+  WGM_PERSISTENT_PROLOGUE_TASKS
   wgm_c4_init(L, &c, a);
   if (wgm_barrier(L, &c)) wgm_c4_loop(L, &c, a, [](wgm_cta *) { return false; });
   WGM_PERSISTENT_EPILOGUE
