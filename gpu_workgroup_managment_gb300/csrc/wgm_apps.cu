@@ -301,7 +301,8 @@ extern "C" int wgm_app_create(wgm_runtime *rt, int kind, const wgm_graph_desc *g
       if (e == cudaSuccess && kind == WGM_APP_LONESTAR_SSSP)
         e = wgm_dmalloc(&a->d_wl_u, 2 * (size_t)a->wl_cap);
       if (e == cudaSuccess) e = wgm_dmalloc(&a->d_cnt, 3 * WGM_LINE);
-      if (e == cudaSuccess && kind == WGM_APP_LONESTAR_SSSP) e = wgm_dmalloc(&a->d_stamp, V);
+      /* SSSP: 64-bit {level tag, distance} words (wgm_ls_chunk PACK) */
+      if (e == cudaSuccess && kind == WGM_APP_LONESTAR_SSSP) e = wgm_dmalloc(&a->d_stamp, 2 * V);
       break;
     }
     case WGM_APP_PANNOTIA_COLOR:
@@ -525,6 +526,7 @@ int wgm_app_fill_mega(wgm_app *a, wgm_mega_args *A) {
       x.stamp = a->d_stamp;
       x.source = a->source;
       x.levels_out = a->d_rounds;
+      x.packed = a->kind == WGM_APP_LONESTAR_SSSP ? 1 : 0;
       return WGM_OK;
     }
     case WGM_APP_PANNOTIA_COLOR: {

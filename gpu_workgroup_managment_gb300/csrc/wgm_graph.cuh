@@ -139,9 +139,11 @@ struct wgm_lonestar_args {
   int cap;       /* >= V + E/piece, so no level can overflow */
   int piece;     /* edges per piece (>= 32) */
   int *cnt;      /* [3 lines]: pieces queued for each level, by level mod 3 */
-  int *stamp;    /* SSSP: level a vertex was last queued at */
+  int *stamp;    /* SSSP: level a vertex was last queued at, or (packed) [2V] the
+                    64-bit {level tag, distance} words, dist[] written at the end */
   int source;
   int *levels_out; /* number of levels run (written by group 0) */
+  int packed = 0;  /* SSSP relaxes packed words (wgm_ls_chunk PACK) */
 };
 
 /* Degree as the Lonestar kernel sees it: psrc[nn+1]-psrc[nn] (bfs.cl:165);
@@ -479,8 +481,13 @@ __device__ __forceinline__ bool wgm_ls_level(const wgm_launch &Lc, wgm_cta *c,
       deg = __ldcg(&i_cnt[i]);
       if (SSSP) src = __ldcg(&i_u[i]);
     }
-    ok &= wgm_ls_chunk<SSSP>(a.row, a.col, a.wt, a.dist, a.stamp, a.V, a.piece, L, start, deg,
-                             src, o);
+    if (SSSP && a.packed)
+      ok &= wgm_ls_chunk<SSSP, true, SSSP>(a.row, a.col, a.wt,
+                                           reinterpret_cast<unsigned *>(a.stamp), a.stamp, a.V,
+                                           a.piece, L, start, deg, src, o);
+    else
+      ok &= wgm_ls_chunk<SSSP>(a.row, a.col, a.wt, a.dist, a.stamp, a.V, a.piece, L, start, deg,
+                               src, o);
   }
   (void)sm;
   return ok;
@@ -499,8 +506,13 @@ static __device__ int wgm_phase_lonestar(const wgm_launch &Lc, wgm_cta *c,
     const int tid = c->id * blockDim.x + threadIdx.x, nth = c->ngroups * blockDim.x;
     /* Host init of the plugin (bfs.h:250-262) done on the device. */
     for (int i = tid; i < V; i += nth) {
-      a.dist[i] = (i == a.source) ? 0u : WGM_LONESTAR_INF;
-      if (SSSP) a.stamp[i] = 0;
+      if (SSSP && a.packed) {
+        reinterpret_cast<unsigned long long *>(a.stamp)[i] =
+            (i == a.source) ? 0ull : (unsigned long long)WGM_LONESTAR_INF << 32;
+      } else {
+        a.dist[i] = (i == a.source) ? 0u : WGM_LONESTAR_INF;
+        if (SSSP) a.stamp[i] = 0;
+      }
     }
     if (c->id == 0 && threadIdx.x < 32) {
       /* Level 1 processes the source (bfs.cl:235-241 seeds it at iteration 0). */
@@ -517,6 +529,11 @@ static __device__ int wgm_phase_lonestar(const wgm_launch &Lc, wgm_cta *c,
   int n = __ldcg(&a.cnt[(Lv % 3) * WGM_LINE]);
   if (n == 0) {
     if (c->id == 0 && threadIdx.x == 0 && a.levels_out) *a.levels_out = Lv;
+    if (SSSP && a.packed) { /* the distances out of the packed words */
+      const int tid = c->id * blockDim.x + threadIdx.x, nth = c->ngroups * blockDim.x;
+      const unsigned *w = reinterpret_cast<const unsigned *>(a.stamp);
+      for (int i = tid; i < V; i += nth) a.dist[i] = __ldcg(&w[2 * i + 1]);
+    }
     return 0;
   }
   if (n > a.cap) {
