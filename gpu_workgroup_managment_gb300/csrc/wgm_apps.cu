@@ -147,7 +147,7 @@ static void wgm_app_free_buffers(wgm_app *a) {
                   a->d_oct_input, a->d_oct_second, a->d_oct_pools, a->d_oct_tree,
                   a->d_oct_ctr, a->d_oct_locks, a->d_oct_heads,
                   a->d_c4_board, a->d_c4_nodes, a->d_c4_pool, a->d_c4_locks,
-                  a->d_c4_heads, a->d_c4_ctr};
+                  a->d_c4_heads, a->d_c4_ctr, a->d_tcv};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   a->hubs = wgm_dev_hubs();
@@ -322,6 +322,7 @@ extern "C" int wgm_app_create(wgm_runtime *rt, int kind, const wgm_graph_desc *g
         if (e == cudaSuccess) e = wgm_dmalloc(&a->d_wl_u, 2 * (size_t)a->wl_cap);
         if (e == cudaSuccess) e = wgm_dmalloc(&a->d_stamp, V); /* pending */
         if (e == cudaSuccess) e = wgm_dmalloc(&a->d_cnt, 3 * WGM_LINE);
+        if (e == cudaSuccess) e = wgm_dmalloc(&a->d_tcv, E); /* in-edges with values */
       }
       if (e == cudaSuccess && kind == WGM_APP_PANNOTIA_MIS) e = wgm_dmalloc(&a->d_status, V);
       break;
@@ -550,6 +551,7 @@ int wgm_app_fill_mega(wgm_app *a, wgm_mega_args *A) {
       x.cap = a->wl_cap;
       x.piece = a->piece;
       x.cnt = a->d_cnt;
+      x.tcv = a->d_tcv;
       return WGM_OK;
     }
     case WGM_APP_PANNOTIA_MIS: {

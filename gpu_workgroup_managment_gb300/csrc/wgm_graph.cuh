@@ -628,6 +628,7 @@ struct wgm_color_args {
                                     the value bits of the piece's vertex */
   int cap, piece;
   int *cnt;      /* [3 lines] frontier sizes by round mod 3 */
+  int2 *tcv;     /* [in-edges] {in-neighbour, its value bits}, filled at init */
 };
 
 /* Pannotia colour (color.cl:3-97) computed as the frontier recurrence it
@@ -646,12 +647,13 @@ struct wgm_color_args {
  * once per round.
  * Phases: (0) init; (3,0) count larger out-neighbours; (4,0) round-1
  * frontier; (1,r) the vertices coloured r release their in-neighbours. */
-/* pre(w, src, &tag) tests an in-neighbour w without side effects and sets
- * the word its queue entry will carry; commit(w) claims it (true: queue
- * it).  The in-edge row bounds of every w that passes `pre` are loaded
- * beside `commit`'s atomic, not after it. */
+/* tcv[e] = {in-neighbour w, a word about w} (one 8-byte load per edge).
+ * pre(w, word, src, &tag) tests w without side effects and sets the word
+ * its queue entry will carry; commit(w) claims it (true: queue it).  The
+ * in-edge row bounds of every w that passes `pre` are loaded beside
+ * `commit`'s atomic, not after it. */
 template <class Pre, class Commit>
-__device__ __forceinline__ bool wgm_frontier_chunk(const int *trow, const int *tcol, int P,
+__device__ __forceinline__ bool wgm_frontier_chunk(const int *trow, const int2 *tcv, int P,
                                                    int start, int deg, unsigned sv,
                                                    const wgm_ls_out &o, Pre &&pre,
                                                    Commit &&commit) {
@@ -663,7 +665,7 @@ __device__ __forceinline__ bool wgm_frontier_chunk(const int *trow, const int *t
   const int base = start - off;
   bool ok = true;
   for (int w = 0; w < total; w += 32 * K) {
-    int u[K], rs[K], d[K], np[K], tg[K];
+    int u[K], rs[K], d[K], np[K], tg[K], wv[K];
     unsigned src[K];
     bool f[K];
 #pragma unroll
@@ -673,12 +675,14 @@ __device__ __forceinline__ bool wgm_frontier_chunk(const int *trow, const int *t
       const int own = wgm_owner_of(off, min(s, total - 1));
       const int e = __shfl_sync(WGM_FULL, base, own) + s;
       src[k] = __shfl_sync(WGM_FULL, sv, own);
-      u[k] = f[k] ? __ldg(&tcol[e]) : -1;
+      const int2 p = f[k] ? __ldg(&tcv[e]) : make_int2(-1, 0);
+      u[k] = p.x;
+      wv[k] = p.y;
     }
 #pragma unroll
     for (int k = 0; k < K; k++) {
       tg[k] = 0;
-      f[k] = f[k] && pre(u[k], src[k], &tg[k]);
+      f[k] = f[k] && pre(u[k], wv[k], src[k], &tg[k]);
     }
 #pragma unroll
     for (int k = 0; k < K; k++) {
@@ -783,6 +787,12 @@ static __device__ int wgm_phase_color(const wgm_launch &Lc, wgm_cta *c, const wg
     for (int i = s.tid; i < V; i += s.nth) {
       a.color[i] = -1; /* color.h:50 */
       a.pending[i] = 0;
+    }
+    /* every in-edge beside its neighbour's value: a release reads both at once */
+    const int ET = __ldg(&a.trow[V]);
+    for (int e = s.tid; e < ET; e += s.nth) {
+      const int w = __ldg(&a.tcol[e]);
+      a.tcv[e] = make_int2(w, __float_as_int(__ldg(&a.node_value[w])));
     }
     if (c->id == 0 && threadIdx.x < 3) a.cnt[threadIdx.x * WGM_LINE] = 0;
     *nxt = {3, 0};
@@ -889,12 +899,12 @@ static __device__ int wgm_phase_color(const wgm_launch &Lc, wgm_cta *c, const wg
       sv = (unsigned)__ldcg(&a.wl_u[io + i]); /* the coloured vertex's value bits */
     }
     ok &= wgm_frontier_chunk(
-        a.trow, a.tcol, a.piece, start, deg, sv, o,
-        [&](int w, unsigned src, int *tag) {
+        a.trow, a.tcv, a.piece, start, deg, sv, o,
+        [&](int w, int wbits, unsigned src, int *tag) {
           /* w has the coloured vertex as a larger out-neighbour */
-          const float vw = __ldg(&a.node_value[w]);
-          *tag = __float_as_int(vw);
-          return vw < __uint_as_float(src);
+          (void)w;
+          *tag = wbits;
+          return __int_as_float(wbits) < __uint_as_float(src);
         },
         [&](int w) {
           if (atomicSub(&a.pending[w], 1) != 1) return false;

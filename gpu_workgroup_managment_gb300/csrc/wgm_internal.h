@@ -57,6 +57,7 @@ struct wgm_app {
   int *d_rounds = nullptr;
   /* colour: in-edge CSR when the graph is not symmetric (else the graph) */
   int *d_trow = nullptr, *d_tcol = nullptr;
+  int2 *d_tcv = nullptr; /* colour: in-edges beside their neighbour's value */
   int source = 0;
   float damping = 0.85f;
   float dang0 = 0.f;
