@@ -91,8 +91,11 @@ class Clocks:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.Q}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "20"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            # the sampler is live (its first line printed, and dropped: it
+            # precedes the timed region) before the timed region starts
+            self.proc.stdout.readline()
         except Exception:
             self.proc = None
         return self
@@ -399,7 +402,7 @@ def _served(rt, rates=(1000, 5000, 20000), reps: int = 20, reserve: int = 96) ->
 def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="wgm", choices=["wgm", "reference"])
     ap.add_argument("--no-extra", action="store_true", help="skip the extra measurements")
