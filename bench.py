@@ -314,11 +314,12 @@ def _c2(rt, _barrier_ns) -> dict:
     return out
 
 
-def _c3(rt, _barrier_ns) -> dict:
+def _c3(rt, _barrier_ns, scale: int = 22) -> dict:
     """C3: PageRank on RMAT-22 (edge factor 16, seed 1), 20 iterations, best
-    of 3; Bytes_alg per iteration = 8 E + 16 V."""
+    of 3; Bytes_alg per iteration = 8 E + 16 V.  `scale` < 22 gives the
+    smaller profiling case."""
     from gpu_workgroup_managment_gb300 import PersistentApp, graphs
-    g = graphs.rmat(22, 16, seed=1)
+    g = graphs.rmat(scale, 16, seed=1)
     with PersistentApp(rt, "pagerank", g, iterations=20) as a:
         st = _best(a, 3)
     s = st.kernel_ms * 1e-3
@@ -419,6 +420,7 @@ def main() -> int:
     ap.add_argument("--only", choices=["octree", "bc", "c1", "c3"],
                     help="one extra measurement alone (the commands profiled with ncu)")
     ap.add_argument("--particles", type=int, default=3_000_000, help="octree size for --only")
+    ap.add_argument("--pr-scale", type=int, default=22, help="RMAT scale of --only c3")
     args = ap.parse_args()
     if args.barrier_sweep:
         return _barrier_sweep()
@@ -429,8 +431,10 @@ def main() -> int:
                 r = _octree(rt, args.particles)
             elif args.only == "bc":
                 r = _bc(rt)
+            elif args.only == "c3":
+                r = _c3(rt, None, args.pr_scale)
             else:
-                r = {"c1": _c1, "c3": _c3}[args.only](rt, None)
+                r = _c1(rt, None)
         print(json.dumps({"only": args.only, **r}))
         return 0
     if args.sssp_kernel_only:

@@ -1239,6 +1239,37 @@ struct wgm_pr_args {
   float dang0;     /* initial dangling mass: (zero-degree vertices)/V */
 };
 
+/* Hub sums of four windows of PageRank hub edges (values v, hub hh per
+ * lane), in groups of M consecutive windows.  A group's 32*M slots span at
+ * most two hubs when every hub has at least 32*M edges (hub threshold >=
+ * 32*M - 1): the group's first hub h0 and h0 + 1.  Each lane sums its M
+ * values into those two, then one two-sum warp reduction and at most two
+ * atomics serve the group.  Windows past the end hold zeros. */
+template <int M>
+__device__ __forceinline__ void wgm_pr_hub_sums(const int4 *w, const int *hh, const float *v,
+                                                int k0, int nwin, int H, float *hub_sum) {
+#pragma unroll
+  for (int g = 0; g < 4; g += M) {
+    if (k0 + g >= nwin) break; /* warp-uniform */
+    const int h0 = w[g].x;
+    float f0 = 0.f, f1 = 0.f;
+#pragma unroll
+    for (int q = g; q < g + M; q++) {
+      if (hh[q] == h0) f0 += v[q];
+      else f1 += v[q];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      f0 += __shfl_xor_sync(WGM_FULL, f0, o);
+      f1 += __shfl_xor_sync(WGM_FULL, f1, o);
+    }
+    if (wgm_lane() == 0) {
+      atomicAdd(&hub_sum[h0], f0);
+      if (h0 + 1 < H && f1 != 0.f) atomicAdd(&hub_sum[h0 + 1], f1);
+    }
+  }
+}
+
 /* pr' = (1-d)/V + d*(sum_{u in N(v)} pr[u]/deg(u) + dangling/V).  Phases:
  * (0) init; (1,t) iteration t for non-hub vertices, hub sums accumulated over
  * the grid; (2,t) hub finalisation.  Per-vertex sums run in a fixed order (a
@@ -1340,7 +1371,7 @@ static __device__ int wgm_phase_pagerank(const wgm_launch &Lc, wgm_cta *c, const
     }
   }
   /* hub edges: four windows per warp step, their records, col loads and
-   * gathers in flight together */
+   * gathers in flight together, summed in groups of M windows */
   const int nwin = (a.hubs.total + 31) >> 5;
   const int4 *wrec = reinterpret_cast<const int4 *>(a.hubs.wmap);
   for (int k0 = s.gw * 4; k0 < nwin; k0 += s.NW * 4) {
@@ -1362,18 +1393,12 @@ static __device__ int wgm_phase_pagerank(const wgm_launch &Lc, wgm_cta *c, const
     }
 #pragma unroll
     for (int q = 0; q < 4; q++) v[q] = val[q] ? __ldcg(&cin[u[q]]) : 0.f;
-#pragma unroll
-    for (int q = 0; q < 4; q++) {
-      if (k0 + q >= nwin) break; /* warp-uniform */
-      const int h0 = w[q].x;
-      int m0, m1;
-      float f0, f1;
-      wgm_two_seg_reduce(hh[q] == h0, 0, v[q], 2, &m0, &m1, &f0, &f1);
-      if (lane == 0) {
-        atomicAdd(&a.hub_sum[h0], f0);
-        if (h0 + 1 < a.hubs.H && f1 != 0.f) atomicAdd(&a.hub_sum[h0 + 1], f1);
-      }
-    }
+    if (a.hub_threshold >= 127)
+      wgm_pr_hub_sums<4>(w, hh, v, k0, nwin, a.hubs.H, a.hub_sum);
+    else if (a.hub_threshold >= 63)
+      wgm_pr_hub_sums<2>(w, hh, v, k0, nwin, a.hubs.H, a.hub_sum);
+    else
+      wgm_pr_hub_sums<1>(w, hh, v, k0, nwin, a.hubs.H, a.hub_sum);
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) dl += __shfl_xor_sync(WGM_FULL, dl, o);

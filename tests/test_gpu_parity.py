@@ -92,7 +92,8 @@ def test_few_groups(rt, num_wgs):
     dict(barrier_kind=4), dict(barrier_kind=4, threads_per_wg=1024),
     dict(discovery_mode=1, discovery_extra_rounds=2), dict(threads_per_wg=128),
     dict(threads_per_wg=512), dict(threads_per_wg=1024), dict(hub_threshold=32),
-    dict(hub_threshold=100000), dict(host_handshake=1),
+    dict(hub_threshold=63),
+    dict(hub_threshold=127), dict(hub_threshold=100000), dict(host_handshake=1),
 ])
 def test_runtime_variants(cfg):
     g = graphs.rmat(13, 16, seed=9)
