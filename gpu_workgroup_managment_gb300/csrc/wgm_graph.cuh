@@ -1239,19 +1239,37 @@ struct wgm_pr_args {
   float dang0;     /* initial dangling mass: (zero-degree vertices)/V */
 };
 
+/* First stage of a PageRank hub step: the records of windows k0..k0+3
+ * (first hub of each in hx), this lane's hub in each (hh) and the col
+ * value of its slot (u; -1 past the end). */
+__device__ __forceinline__ void wgm_pr_hub_stage(const int4 *wrec, const int *col, int total,
+                                                 int nwin, int k0, int lane, int *hx, int *hh,
+                                                 int *u) {
+  int4 w[4];
+#pragma unroll
+  for (int q = 0; q < 4; q++) w[q] = __ldg(wrec + min(k0 + q, nwin - 1));
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    int e;
+    wgm_hub_slot(w[q], lane, &hh[q], &e);
+    hx[q] = w[q].x;
+    u[q] = (k0 + q < nwin && (k0 + q) * 32 + lane < total) ? __ldg(&col[e]) : -1;
+  }
+}
+
 /* Hub sums of four windows of PageRank hub edges (values v, hub hh per
- * lane), in groups of M consecutive windows.  A group's 32*M slots span at
+ * lane, first hub of each window hx), in groups of M consecutive windows.  A group's 32*M slots span at
  * most two hubs when every hub has at least 32*M edges (hub threshold >=
  * 32*M - 1): the group's first hub h0 and h0 + 1.  Each lane sums its M
  * values into those two, then one two-sum warp reduction and at most two
  * atomics serve the group.  Windows past the end hold zeros. */
 template <int M>
-__device__ __forceinline__ void wgm_pr_hub_sums(const int4 *w, const int *hh, const float *v,
+__device__ __forceinline__ void wgm_pr_hub_sums(const int *hx, const int *hh, const float *v,
                                                 int k0, int nwin, int H, float *hub_sum) {
 #pragma unroll
   for (int g = 0; g < 4; g += M) {
     if (k0 + g >= nwin) break; /* warp-uniform */
-    const int h0 = w[g].x;
+    const int h0 = hx[g];
     float f0 = 0.f, f1 = 0.f;
 #pragma unroll
     for (int q = g; q < g + M; q++) {
@@ -1370,35 +1388,34 @@ static __device__ int wgm_phase_pagerank(const wgm_launch &Lc, wgm_cta *c, const
       if (dfull == 0) dl += p;
     }
   }
-  /* hub edges: four windows per warp step, their records, col loads and
-   * gathers in flight together, summed in groups of M windows */
+  /* hub edges: four windows per warp step, summed in groups of M windows,
+   * in a two-stage pipeline: the next step's window records and col loads
+   * (two dependent round trips) are issued before this step's gathers are
+   * summed, so each step waits for about one round trip instead of three */
   const int nwin = (a.hubs.total + 31) >> 5;
   const int4 *wrec = reinterpret_cast<const int4 *>(a.hubs.wmap);
-  for (int k0 = s.gw * 4; k0 < nwin; k0 += s.NW * 4) {
-    int4 w[4];
-    int hh[4], u[4];
-    bool val[4];
+  const int kstep = s.NW * 4;
+  int k0 = s.gw * 4;
+  int hx[4], hh[4], u[4];
+  if (k0 < nwin) wgm_pr_hub_stage(wrec, a.col, a.hubs.total, nwin, k0, lane, hx, hh, u);
+  for (; k0 < nwin; k0 += kstep) {
     float v[4];
 #pragma unroll
-    for (int q = 0; q < 4; q++) {
-      const int k = min(k0 + q, nwin - 1);
-      w[q] = __ldg(wrec + k);
-      val[q] = k0 + q < nwin && (k0 + q) * 32 + lane < a.hubs.total;
-    }
+    for (int q = 0; q < 4; q++) v[q] = u[q] >= 0 ? __ldcg(&cin[u[q]]) : 0.f;
+    int cx[4], ch[4];
 #pragma unroll
     for (int q = 0; q < 4; q++) {
-      int e;
-      wgm_hub_slot(w[q], lane, &hh[q], &e);
-      u[q] = val[q] ? __ldg(&a.col[e]) : 0;
+      cx[q] = hx[q];
+      ch[q] = hh[q];
     }
-#pragma unroll
-    for (int q = 0; q < 4; q++) v[q] = val[q] ? __ldcg(&cin[u[q]]) : 0.f;
+    if (k0 + kstep < nwin)
+      wgm_pr_hub_stage(wrec, a.col, a.hubs.total, nwin, k0 + kstep, lane, hx, hh, u);
     if (a.hub_threshold >= 127)
-      wgm_pr_hub_sums<4>(w, hh, v, k0, nwin, a.hubs.H, a.hub_sum);
+      wgm_pr_hub_sums<4>(cx, ch, v, k0, nwin, a.hubs.H, a.hub_sum);
     else if (a.hub_threshold >= 63)
-      wgm_pr_hub_sums<2>(w, hh, v, k0, nwin, a.hubs.H, a.hub_sum);
+      wgm_pr_hub_sums<2>(cx, ch, v, k0, nwin, a.hubs.H, a.hub_sum);
     else
-      wgm_pr_hub_sums<1>(w, hh, v, k0, nwin, a.hubs.H, a.hub_sum);
+      wgm_pr_hub_sums<1>(cx, ch, v, k0, nwin, a.hubs.H, a.hub_sum);
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) dl += __shfl_xor_sync(WGM_FULL, dl, o);
