@@ -68,7 +68,9 @@ __global__ void __launch_bounds__(1024) wgm_k_psssp(wgm_launch L, wgm_psssp_args
   WGM_PERSISTENT_EPILOGUE
 }
 
-__global__ void __launch_bounds__(1024) wgm_k_pagerank(wgm_launch L, wgm_pr_args a) {
+/* 48 registers (no spills): five 256-thread CTAs per SM instead of four,
+ * more gathers in flight for a kernel bound by their latency */
+__global__ void __maxnreg__(48) wgm_k_pagerank(wgm_launch L, wgm_pr_args a) {
   WGM_PERSISTENT_PROLOGUE
   WGM_DRIVE(wgm_phase_pagerank(L, &c, a, &sm, cur, nxt));
   WGM_PERSISTENT_EPILOGUE
