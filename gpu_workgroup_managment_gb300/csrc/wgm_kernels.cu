@@ -62,7 +62,8 @@ __global__ void __launch_bounds__(1024) wgm_k_mis(wgm_launch L, wgm_mis_args a) 
   WGM_PERSISTENT_EPILOGUE
 }
 
-__global__ void __launch_bounds__(1024) wgm_k_psssp(wgm_launch L, wgm_psssp_args a) {
+/* 40 registers (no spills): six 256-thread CTAs per SM instead of four */
+__global__ void __maxnreg__(40) wgm_k_psssp(wgm_launch L, wgm_psssp_args a) {
   WGM_PERSISTENT_PROLOGUE
   WGM_DRIVE(wgm_phase_pannotia_sssp(L, &c, a, &sm, cur, nxt));
   WGM_PERSISTENT_EPILOGUE
