@@ -115,6 +115,25 @@ def test_star_and_edge_cases(rt):
     _all_apps_vs_oracle(rt, g, 17, 3)     # leaf source
 
 
+def test_color_default_groups():
+    """Colour on the default group count takes 512 threads per SM (two
+    256-thread CTAs); an explicit count is honoured; the colours are the
+    oracle's either way."""
+    import torch
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    g = graphs.rmat(12, 16, seed=3)
+    nv = graphs.seeded_node_values(g.num_nodes, 3)
+    want = oracle.color(g, nv)
+    for tpw, groups in ((256, 2 * sms), (128, 4 * sms), (1024, sms)):
+        with Runtime(threads_per_wg=tpw) as r, PersistentApp(r, "color", g, node_values=nv) as a:
+            st = a.run()
+            assert st.groups == groups, (tpw, st.groups)
+            assert np.array_equal(a.result(), want)
+            st = a.run(7)
+            assert st.groups == 7
+            assert np.array_equal(a.result(), want)
+
+
 def test_single_vertex(rt):
     g = graphs.Graph(np.array([0, 0], np.int32), np.zeros(0, np.int32), np.zeros(0, np.uint32))
     for app in ("lonestar_bfs", "lonestar_sssp", "color", "mis", "sssp", "pagerank"):
