@@ -645,6 +645,18 @@ static int wgm_pick_grid(wgm_app *a, int num_wgs, int block, int *grid) {
     const int sms = a->rt->prop.multiProcessorCount;
     *grid = std::min(hw, std::max(sms, sms * 512 / std::max(block, 1)));
   }
+  /* Lonestar BFS/SSSP by default: one group per 8192 edges, rounded up to
+   * a multiple of the SM count.  A level costs a grid barrier plus a chain
+   * of dependent round trips whatever its size, so a small graph runs its
+   * levels faster on fewer groups: the 256x256 grid's 512 BFS levels took
+   * 4.1 us each on 152 CTAs against 6.4 us on all 608.  At 256 threads a
+   * graph of 5M edges or more keeps every co-resident CTA. */
+  if (num_wgs <= 0 &&
+      (a->kind == WGM_APP_LONESTAR_BFS || a->kind == WGM_APP_LONESTAR_SSSP)) {
+    const long long sms = a->rt->prop.multiProcessorCount;
+    const long long want = ((long long)a->E / 8192 + sms - 1) / sms * sms;
+    *grid = (int)std::min<long long>(hw, std::max(sms, want));
+  }
   return WGM_OK;
 }
 

@@ -167,10 +167,11 @@ int wgm_app_set_bc_sources(wgm_app *app, int32_t num_sources);
  * 10240 vertices; the default there).  Same arithmetic, same tolerance. */
 int wgm_app_set_bc_mode(wgm_app *app, int32_t mode);
 /* One iteration of run_persistent (skel.cpp:316-355): launch the persistent
- * kernel on up to num_wgs groups (<=0: all co-resident, except Pannotia
- * colour, which then takes 512 threads per SM - two 256-thread CTAs, at
- * least one CTA - because its ~1600 short rounds run faster on fewer
- * groups; an explicit num_wgs is always honoured) and wait. */
+ * kernel on up to num_wgs groups and wait.  num_wgs <= 0: all co-resident,
+ * except where fewer groups run the many short rounds faster - Pannotia
+ * colour takes 512 threads per SM (two 256-thread CTAs, at least one CTA),
+ * Lonestar BFS/SSSP one group per 8192 edges rounded up to a multiple of
+ * the SM count, at most all.  An explicit num_wgs is always honoured. */
 int wgm_run_persistent(wgm_runtime *rt, wgm_app *app, int num_wgs, wgm_run_stats *stats);
 /* Asynchronous launch on a caller stream (cudaStream_t; NULL = the runtime's
  * stream).  With cfg.host_handshake set the kernel waits for

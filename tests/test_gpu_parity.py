@@ -134,6 +134,30 @@ def test_color_default_groups():
             assert np.array_equal(a.result(), want)
 
 
+def test_lonestar_default_groups():
+    """Lonestar BFS/SSSP on the default group count: one group per 8192
+    edges rounded up to the SM count (the 256x256 grid: one CTA per SM),
+    every co-resident CTA on large graphs; same distances as on all CTAs."""
+    import torch
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    gg, gr = graphs.grid(256, 256), graphs.rmat(18, 16, seed=2)  # 262K / 7.5M edges
+    gg.weights = graphs.uniform_weights(gg, 1)
+    gr.weights = graphs.uniform_weights(gr, 2)
+    grid, big = graphs.lonestar_view(gg), graphs.lonestar_view(gr)
+    with Runtime() as r:
+        for g, small in ((grid, True), (big, False)):
+            for app, ref in (("lonestar_bfs", oracle.lonestar_bfs),
+                             ("lonestar_sssp", oracle.lonestar_sssp)):
+                src = graphs.max_degree_vertex(g)
+                want = ref(g, src)
+                with PersistentApp(r, app, g, source=src) as a:
+                    st = a.run()
+                    assert np.array_equal(a.result(), want), app
+                    full = a.run(1 << 20).groups
+                    assert np.array_equal(a.result(), want), app
+                    assert st.groups == (sms if small else full), (app, st.groups, full)
+
+
 def test_single_vertex(rt):
     g = graphs.Graph(np.array([0, 0], np.int32), np.zeros(0, np.int32), np.zeros(0, np.uint32))
     for app in ("lonestar_bfs", "lonestar_sssp", "color", "mis", "sssp", "pagerank"):
