@@ -657,6 +657,16 @@ static int wgm_pick_grid(wgm_app *a, int num_wgs, int block, int *grid) {
     const long long want = ((long long)a->E / 8192 + sms - 1) / sms * sms;
     *grid = (int)std::min<long long>(hw, std::max(sms, want));
   }
+  /* Pannotia SSSP by default: 1024 threads per SM (four 256-thread CTAs of
+   * the six that fit), more only for graphs of more than one 256-thread CTA
+   * per 32768 edges: on grids and RMAT graphs up to 7.6M edges four CTAs
+   * per SM ran 10-15 % faster than six, on RMAT-20 (33M edges) six won. */
+  if (num_wgs <= 0 && a->kind == WGM_APP_PANNOTIA_SSSP) {
+    const long long sms = a->rt->prop.multiProcessorCount, b = std::max(block, 1);
+    const long long base = sms * std::max(1LL, 1024 / b);
+    const long long byE = ((long long)a->E / 128 / b + sms - 1) / sms * sms;
+    *grid = (int)std::min<long long>(hw, std::max(base, byE));
+  }
   return WGM_OK;
 }
 

@@ -171,7 +171,9 @@ int wgm_app_set_bc_mode(wgm_app *app, int32_t mode);
  * except where fewer groups run the many short rounds faster - Pannotia
  * colour takes 512 threads per SM (two 256-thread CTAs, at least one CTA),
  * Lonestar BFS/SSSP one group per 8192 edges rounded up to a multiple of
- * the SM count, at most all.  An explicit num_wgs is always honoured. */
+ * the SM count, Pannotia SSSP 1024 threads per SM or one thread per 128
+ * edges, whichever is more; never more than all.  An explicit num_wgs is
+ * always honoured. */
 int wgm_run_persistent(wgm_runtime *rt, wgm_app *app, int num_wgs, wgm_run_stats *stats);
 /* Asynchronous launch on a caller stream (cudaStream_t; NULL = the runtime's
  * stream).  With cfg.host_handshake set the kernel waits for

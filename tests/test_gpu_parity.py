@@ -156,6 +156,11 @@ def test_lonestar_default_groups():
                     full = a.run(1 << 20).groups
                     assert np.array_equal(a.result(), want), app
                     assert st.groups == (sms if small else full), (app, st.groups, full)
+        # Pannotia SSSP: 1024 threads per SM on the grid
+        with PersistentApp(r, "sssp", gg, source=0) as a:
+            st = a.run()
+            assert st.groups == min(4 * sms, a.run(1 << 20).groups)
+            assert np.array_equal(a.result(), oracle.pannotia_sssp(gg, 0))
 
 
 def test_single_vertex(rt):
