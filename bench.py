@@ -417,7 +417,7 @@ def main() -> int:
     ap.add_argument("--barrier-sweep", action="store_true",
                     help="ns per barrier for every barrier kind and CTA size")
     ap.add_argument("--served", action="store_true", help="served-form measurement only")
-    ap.add_argument("--only", choices=["octree", "bc", "c1", "c3"],
+    ap.add_argument("--only", choices=["octree", "bc", "c1", "c2", "c3"],
                     help="one extra measurement alone (the commands profiled with ncu)")
     ap.add_argument("--particles", type=int, default=3_000_000, help="octree size for --only")
     ap.add_argument("--pr-scale", type=int, default=22, help="RMAT scale of --only c3")
@@ -433,6 +433,8 @@ def main() -> int:
                 r = _bc(rt)
             elif args.only == "c3":
                 r = _c3(rt, None, args.pr_scale)
+            elif args.only == "c2":
+                r = _c2(rt, None)
             else:
                 r = _c1(rt, None)
         print(json.dumps({"only": args.only, **r}))
