@@ -28,9 +28,11 @@
 
 #include "wgm_graph.cuh"
 
-/* Whether batch jobs read dist[dst] before the atomic (one more dependent
- * load, fewer atomics).  The batch's graphs are small and its critical path
- * is latency: go straight to the atomic. */
+/* Whether batch BFS jobs read dist[dst] before the atomic (one more
+ * dependent load, fewer atomics): no, a BFS claim mostly succeeds.  SSSP
+ * jobs always pre-check: on the RMAT graphs most relaxations fail, and the
+ * 64-bit atomics they skip cost more than the load (the batch's RMAT SSSP
+ * CTA time fell 12 %, the launch 3.5 %). */
 #ifndef WGM_BATCH_PRECHECK
 #define WGM_BATCH_PRECHECK false
 #endif
@@ -475,7 +477,7 @@ __device__ void wgm_cta_lonestar(const wgm_batch_args &B, const wgm_batch_job &j
         wgm_ls_chunk_async<SSSP>(row, col, wt, dist, stamp, V, j.piece, L, start, deg, src, o,
                                  q, 0);
       else
-        wgm_ls_chunk<SSSP, WGM_BATCH_PRECHECK, PACK>(row, col, wt, dw, stamp, V, j.piece, L,
+        wgm_ls_chunk<SSSP, WGM_BATCH_PRECHECK || SSSP, PACK>(row, col, wt, dw, stamp, V, j.piece, L,
                                                      start, deg, src, o);
     }
     if (ASYNC) wgm_ls_local_rounds<SSSP>(row, col, wt, dist, stamp, V, j.piece, L, o, q,
@@ -692,7 +694,7 @@ __device__ int wgm_team_ls_run(const wgm_ls_job &J, wgm_warp_smem *sm, int *err,
         wgm_ls_chunk_async<SSSP>(J.row, J.col, J.wt, J.dist, J.stamp, V, J.piece, L, start, deg,
                                  src, o, q, 0);
       else
-        wgm_ls_chunk<SSSP, WGM_BATCH_PRECHECK, PACK>(J.row, J.col, J.wt, dw, J.stamp, V,
+        wgm_ls_chunk<SSSP, WGM_BATCH_PRECHECK || SSSP, PACK>(J.row, J.col, J.wt, dw, J.stamp, V,
                                                      J.piece, L, start, deg, src, o);
     }
     if (ASYNC)
