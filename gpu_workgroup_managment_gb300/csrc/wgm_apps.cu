@@ -660,7 +660,7 @@ static int wgm_pick_grid(wgm_app *a, int num_wgs, int block, int *grid) {
   /* Pannotia SSSP by default: 1024 threads per SM (four 256-thread CTAs of
    * the six that fit), more only for graphs of more than one 256-thread CTA
    * per 32768 edges: on grids and RMAT graphs up to 7.6M edges four CTAs
-   * per SM ran 10-15 % faster than six, on RMAT-20 (33M edges) six won. */
+   * per SM ran 9-15 % faster than six, on RMAT-20 (33M edges) six won. */
   if (num_wgs <= 0 && a->kind == WGM_APP_PANNOTIA_SSSP) {
     const long long sms = a->rt->prop.multiProcessorCount, b = std::max(block, 1);
     const long long base = sms * std::max(1LL, 1024 / b);
