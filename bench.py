@@ -178,20 +178,35 @@ def _batch_inputs():
     return batch_workload()
 
 
+def _cpu_best(fn, budget_s: float = 10.0, max_runs: int = 3) -> float:
+    """Best wall time (s) of up to max_runs calls of fn, stopping once the
+    calls have taken budget_s."""
+    best, total, runs = float("inf"), 0.0, 0
+    while runs < max_runs and (runs == 0 or total < budget_s):
+        t0 = time.perf_counter()
+        fn()
+        dt = time.perf_counter() - t0
+        best, total, runs = min(best, dt), total + dt, runs + 1
+    return best
+
+
 def _reference_arm(args, ws, rank) -> int:
     """The reference's algorithm on the host cores: the oracle's job-parallel
     batched restatement of lonestar bfs.cl / sssp.cl over the same 1024 jobs,
-    every host thread busy.  One step = the whole batch."""
+    every host thread busy.  One step = the whole batch.  The graphs come from
+    oracle/workload.py (the same arrays as the GPU arm's), so this arm loads
+    no product library."""
     if rank != 0:
         return 0
     from oracle import oracle
-    gs, jobs, meta = _batch_inputs()
+    from oracle.workload import batch_workload
+    gs, jobs, meta = batch_workload()
     arena = oracle.BatchArena(gs, jobs)
     d = arena.run()
     offsets = np.concatenate([[0], np.cumsum(arena.V.astype(np.int64))])
     et, _ = _job_edges(gs, jobs, d, offsets)
     E = int(et.sum())
-    warm = max(1, min(args.warmup, 3))
+    warm = max(args.warmup, 3)
     for _ in range(warm - 1):
         arena.run()
     times = []
@@ -277,8 +292,11 @@ def _best(app, k: int = 5):
 def _c1(rt, barrier_ns) -> dict:
     """C1: plain persistent BFS on the 256x256 4-neighbour grid from vertex 0
     (Lonestar view), one launch per run, CUDA events, best of 5.  Bytes_alg
-    = 8 E_t + 20 V_r; ns per level and the barrier's share of it."""
+    = 8 E_t + 20 V_r; ns per level and the barrier's share of it.  CPU
+    baseline: the oracle's level-synchronous restatement of bfs.cl on every
+    host core and on one."""
     from gpu_workgroup_managment_gb300 import PersistentApp, graphs
+    from oracle import oracle
     g = graphs.lonestar_view(graphs.grid(256, 256))
     with PersistentApp(rt, "lonestar_bfs", g) as a:
         st = _best(a)
@@ -287,11 +305,18 @@ def _c1(rt, barrier_ns) -> dict:
     et, vr = int(np.diff(g.row_ptr)[reached].clip(min=0).sum()), int(reached.sum())
     peak, kind = _peak_hbm()
     s = st.kernel_ms * 1e-3
+    if not np.array_equal(d, oracle.lonestar_bfs(g, 0)):
+        raise SystemExit("C1 BFS differs from the oracle")
+    t_omp = _cpu_best(lambda: oracle.lonestar_bfs(g, 0, omp=True))
+    t_one = _cpu_best(lambda: oracle.lonestar_bfs(g, 0))
     out = {"ms": st.kernel_ms, "levels": st.rounds, "groups": st.groups,
            "gteps": et / s / 1e9, "gteps_undirected": et / 2 / s / 1e9,
            "ns_per_level": st.kernel_ms * 1e6 / max(st.rounds, 1),
            "gbs_alg": (8 * et + 20 * vr) / s / 1e9,
-           "frac_of_" + kind: (8 * et + 20 * vr) / s / 1e9 / peak}
+           "frac_of_" + kind: (8 * et + 20 * vr) / s / 1e9 / peak,
+           "cpu_baseline": {"ms": t_omp * 1e3, "gteps": et / t_omp / 1e9,
+                            "cores": oracle.threads(), "ms_1core": t_one * 1e3,
+                            "kind": "port", "sample": "the whole BFS, best of 3"}}
     if barrier_ns:
         out["barrier_share"] = barrier_ns * st.rounds / (st.kernel_ms * 1e6)
     return out
@@ -300,33 +325,90 @@ def _c1(rt, barrier_ns) -> dict:
 def _c2(rt, _barrier_ns) -> dict:
     """C2: RMAT-20 (edge factor 16, seed 1) persistent Lonestar SSSP from
     the max-degree vertex, Pannotia colour and MIS with seeded priorities;
-    best of 5 launches each."""
+    best of 5 launches each, results checked against the oracle.
+    Algorithmic bytes: SSSP 12 E_t + 36 V_r + 8 V (the packed-word kernel);
+    colour 16 E + 24 V (each edge read twice as a (neighbour, value) pair:
+    once to count a vertex's larger neighbours, once to release them; per
+    vertex two row-pair reads, the colour write and the pending count); MIS
+    12 B per edge scanned and 16 B per active vertex, summed over rounds
+    (the oracle counts both).  CPU baselines: the oracle's OpenMP
+    restatements of sssp.cl, color.cl and mis.cl on every host core, on the
+    whole graph (colour: one run - the reference's rounds rescan every
+    uncoloured vertex's edges)."""
     from gpu_workgroup_managment_gb300 import PersistentApp, graphs
+    from oracle import oracle
     g = graphs.rmat(20, 16, seed=1)
     nv = graphs.seeded_node_values(g.num_nodes, 1)
     src = graphs.max_degree_vertex(g)
-    out = {}
-    for app, kw in (("lonestar_sssp", {"source": src}), ("color", {"node_values": nv}),
-                    ("mis", {"node_values": nv})):
-        with PersistentApp(rt, app, g, **kw) as a:
-            st = _best(a)
-        out[app] = {"ms": st.kernel_ms, "rounds": st.rounds, "groups": st.groups}
+    peak, kind = _peak_hbm()
+    V, E = g.num_nodes, g.num_edges
+    out = {"vertices": V, "edges": E, "cores": oracle.threads()}
+    with PersistentApp(rt, "lonestar_sssp", g, source=src) as a:
+        st = _best(a)
+        d = a.result()
+    want = oracle.lonestar_sssp(g, src, omp=True)
+    if not np.array_equal(d, want):
+        raise SystemExit("C2 SSSP differs from the oracle")
+    reached = d != INF
+    et, vr = int(g.degrees()[reached].sum()), int(reached.sum())
+    s = st.kernel_ms * 1e-3
+    gbs = (12 * et + 36 * vr + 8 * V) / s / 1e9
+    t = _cpu_best(lambda: oracle.lonestar_sssp(g, src, omp=True))
+    out["lonestar_sssp"] = {"ms": st.kernel_ms, "rounds": st.rounds, "groups": st.groups,
+                            "gteps": et / s / 1e9, "gbs_alg": gbs, "frac_of_" + kind: gbs / peak,
+                            "cpu_ms": t * 1e3, "cpu_gteps": et / t / 1e9}
+    with PersistentApp(rt, "color", g, node_values=nv) as a:
+        st = _best(a)
+        col = a.result()
+    t0 = time.perf_counter()
+    want = oracle.color(g, nv, omp=True)
+    t = time.perf_counter() - t0
+    if not np.array_equal(col, want):
+        raise SystemExit("C2 colour differs from the oracle")
+    s = st.kernel_ms * 1e-3
+    gbs = (16 * E + 24 * V) / s / 1e9
+    out["color"] = {"ms": st.kernel_ms, "rounds": st.rounds, "groups": st.groups,
+                    "gbs_alg": gbs, "frac_of_" + kind: gbs / peak, "cpu_ms": t * 1e3,
+                    "cpu_sample": "one run of the OpenMP restatement of color.cl"}
+    with PersistentApp(rt, "mis", g, node_values=nv) as a:
+        st = _best(a)
+        m = a.result()
+    want, e_scan, v_act = oracle.mis_work(g, nv)
+    if not np.array_equal(m, want):
+        raise SystemExit("C2 MIS differs from the oracle")
+    s = st.kernel_ms * 1e-3
+    gbs = (12 * e_scan + 16 * v_act) / s / 1e9
+    t = _cpu_best(lambda: oracle.mis(g, nv, omp=True))
+    out["mis"] = {"ms": st.kernel_ms, "rounds": st.rounds, "groups": st.groups,
+                  "edges_scanned": e_scan, "gbs_alg": gbs, "frac_of_" + kind: gbs / peak,
+                  "cpu_ms": t * 1e3}
     return out
 
 
 def _c3(rt, _barrier_ns, scale: int = 22) -> dict:
     """C3: PageRank on RMAT-22 (edge factor 16, seed 1), 20 iterations, best
     of 3; Bytes_alg per iteration = 8 E + 16 V.  `scale` < 22 gives the
-    smaller profiling case."""
+    smaller profiling case.  CPU baseline: the oracle's OpenMP FP32 pull
+    PageRank (same definition) on every host core; error against the FP64
+    oracle."""
     from gpu_workgroup_managment_gb300 import PersistentApp, graphs
+    from oracle import oracle
     g = graphs.rmat(scale, 16, seed=1)
     with PersistentApp(rt, "pagerank", g, iterations=20) as a:
         st = _best(a, 3)
+        pr = a.result()
     s = st.kernel_ms * 1e-3
     peak, kind = _peak_hbm()
     gbs = 20 * (8 * g.num_edges + 16 * g.num_nodes) / s / 1e9
+    ref = oracle.pagerank_f64(g)
+    err = float(np.max(np.abs(pr.astype(np.float64) - ref)) / np.max(np.abs(ref)))
+    if not err <= 1e-5:
+        raise SystemExit(f"C3 PageRank error {err} above 1e-5")
+    t = _cpu_best(lambda: oracle.pagerank_f32_omp(g), budget_s=8.0)
     return {"ms": st.kernel_ms, "iterations": 20, "groups": st.groups, "gbs_alg": gbs,
-            "frac_of_" + kind: gbs / peak}
+            "frac_of_" + kind: gbs / peak, "rel_linf_vs_f64": err,
+            "cpu_ms": t * 1e3, "cpu_cores": oracle.threads(),
+            "cpu_gbs_alg": 20 * (8 * g.num_edges + 16 * g.num_nodes) / t / 1e9}
 
 
 def _bc(rt) -> dict:
@@ -374,9 +456,17 @@ def _served(rt, rates=(1000, 5000, 20000), reps: int = 20, reserve: int = 96) ->
     with PersistentApp(rt, "color", g, node_values=nv) as ca, \
             PersistentApp(rt, "lonestar_bfs", g, source=src) as ba, \
             Serve(rt, ca, ba, graphs=qg, vecs=vecs, mats=mats, arena_bytes=1 << 30) as sv:
+        # the same job as two standalone persistent launches per repetition
+        # (each app on its default group count), the reference's
+        # "standalone" run of the persistent app (run_test.py:345-360)
+        sc, sb = _best(ca, 3).kernel_ms, _best(ba, 3).kernel_ms
+        standalone = reps * (sc + sb)
+        out["persist_ms_standalone"] = standalone
+        out["standalone_rep_ms"] = {"color": sc, "bfs": sb}
         sv.run(reps=1)
         alone = sv.run(reps=reps)
         out["persist_ms_alone"] = alone["persist_ms"]
+        out["alone_kept_vs_standalone"] = standalone / alone["persist_ms"]
         runs = []
         for rate in rates:
             st = sv.run(rate=rate, duration_s=60.0, reps=reps, seed=11, reserve=reserve,
@@ -389,6 +479,7 @@ def _served(rt, rates=(1000, 5000, 20000), reps: int = 20, reserve: int = 96) ->
                          "exec_p99_us": st["exec_p99_us"], "wait_p50_us": st["wait_p50_us"],
                          "wait_p99_us": st["wait_p99_us"], "persist_ms": st["persist_ms"],
                          "persist_kept": alone["persist_ms"] / st["persist_ms"],
+                         "kept_vs_standalone": standalone / st["persist_ms"],
                          "kills": st["kills"], "forks": st["forks"],
                          "waited_for_memory": st["waited_for_memory"]})
         out["runs"] = runs
@@ -397,6 +488,40 @@ def _served(rt, rates=(1000, 5000, 20000), reps: int = 20, reserve: int = 96) ->
                     bfs_edges_per_group=1 << 16, reduce_groups=4, matmul_groups=4)
         out["requests_only"] = {"rate_offered": rates[0], "p50_us": st["lat_p50_us"],
                                 "p99_us": st["lat_p99_us"], "completed": st["completed"]}
+    return out
+
+
+def _r(x, n=3):
+    """Round for the summary (None and strings pass through)."""
+    if isinstance(x, float):
+        return float(f"{x:.{n}g}")
+    return x
+
+
+def _summary(ex: dict) -> dict:
+    """The figures each configuration is judged on, rounded, in one short
+    object printed at the end of the JSON line."""
+    out = {}
+    out["per_graph"] = {"all_ctas_ms": _r(ex.get("per_graph_ms")),
+                        "x_all": _r(ex.get("speedup_vs_per_graph")),
+                        "default_groups_ms": _r(ex.get("per_graph_default_groups_ms")),
+                        "x_default": _r(ex.get("speedup_vs_per_graph_default_groups"))}
+    out["barrier_ns"] = {"256t": _r(ex.get("barrier_ns")), "ctas": ex.get("barrier_ctas"),
+                         "1024t": _r(ex.get("barrier_ns_1024_threads")),
+                         "ctas_1024t": ex.get("barrier_ctas_1024_threads")}
+    c1 = ex.get("c1_bfs_grid256", {})
+    out["c1"] = {"ms": _r(c1.get("ms")), "ns_per_level": _r(c1.get("ns_per_level")),
+                 "cpu_ms": _r(c1.get("cpu_baseline", {}).get("ms"))}
+    c2 = ex.get("c2_rmat20", {})
+    out["c2"] = {k: {"ms": _r(c2.get(k, {}).get("ms")), "cpu_ms": _r(c2.get(k, {}).get("cpu_ms"))}
+                 for k in ("lonestar_sssp", "color", "mis")}
+    c3 = ex.get("c3_pagerank_rmat22", {})
+    out["c3"] = {"ms": _r(c3.get("ms")), "frac": _r(c3.get("frac_of_measured")),
+                 "cpu_ms": _r(c3.get("cpu_ms"))}
+    sv = ex.get("served", {})
+    out["c5"] = [{"rate": r.get("rate_offered"), "p99_us": _r(r.get("p99_us")),
+                  "kept_sa": _r(r.get("kept_vs_standalone")), "kills": r.get("kills")}
+                 for r in sv.get("runs", [])]
     return out
 
 
@@ -575,10 +700,19 @@ def main() -> int:
         extra["per_graph_ms"] = pg
         extra["per_graph_gteps"] = E / (pg * 1e-3) / 1e9
         extra["speedup_vs_per_graph"] = pg / ms_step
+        pgd = b.run_per_graph(default_groups=True)
+        pgd = min(pgd, b.run_per_graph(default_groups=True))
+        if not np.array_equal(b.results(), res):
+            raise SystemExit("per-graph (default groups) results differ from the batched ones")
+        extra["per_graph_default_groups_ms"] = pgd
+        extra["per_graph_default_groups_gteps"] = E / (pgd * 1e-3) / 1e9
+        extra["speedup_vs_per_graph_default_groups"] = pgd / ms_step
         st = b.job_stats()
         extra["makespan_ms"] = float(st["end_ns"].max()) / 1e6
         extra["max_team"] = int(st["team"].max())
         # the default barrier (automatic kind: counting up to 384 CTAs, sense above)
+        # os_freq's default block (256 threads, os_freq.cpp:38) on every
+        # co-resident CTA, then 1024-thread CTAs
         bb = rt.barrier_bench(iterations=100000, threads_per_wg=256)
         extra["barrier_ns"] = bb["ns_per_barrier"]
         extra["barrier_ctas"] = bb["groups"]
@@ -608,6 +742,8 @@ def main() -> int:
             extra["served"] = {"error": repr(exc)}
         line["extra"] = extra
     b.close()
+    if rank == 0 and "extra" in line:
+        line["summary"] = _summary(line["extra"])
     if rank == 0:
         from oracle import oracle
         arena = oracle.BatchArena(gs, jobs)
@@ -626,6 +762,8 @@ def main() -> int:
             "kind": "port",
             "sample": f"{runs} runs of all {len(jobs)} jobs, jobs spread over the host "
                       "threads, each the serial restatement of lonestar bfs.cl/sssp.cl"}
+        if "summary" in line:  # keep the compact figures at the end of the line
+            line["summary"] = line.pop("summary")
         print(json.dumps(line))
     rt.close()
     if dist:

@@ -160,6 +160,8 @@ _PROTOS = {
     "wgm_batch_run": (_I, [_P, _I, C.POINTER(C.c_double)]),
     "wgm_batch_launch_per_graph": (_I, [_P]),
     "wgm_batch_run_per_graph": (_I, [_P, C.POINTER(C.c_double)]),
+    "wgm_batch_launch_per_graph_sized": (_I, [_P, _I]),
+    "wgm_batch_run_per_graph_sized": (_I, [_P, _I, C.POINTER(C.c_double)]),
     "wgm_batch_read": (_I, [_P, _I, _P, C.c_int64]),
     "wgm_batch_read_all": (_I, [_P, _P, C.c_int64]),
     "wgm_batch_info": (_I, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(_I),

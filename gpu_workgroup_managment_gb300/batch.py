@@ -119,9 +119,12 @@ class Batch:
         check(lib.wgm_batch_run(self._h, int(use_cuda_graph), C.byref(ms)), "wgm_batch_run")
         return ms.value
 
-    def run_per_graph(self) -> float:
+    def run_per_graph(self, default_groups: bool = False) -> float:
+        """One standalone persistent launch per job on every co-resident CTA,
+        or (default_groups) on the group count wgm_run_persistent picks."""
         ms = C.c_double()
-        check(lib.wgm_batch_run_per_graph(self._h, C.byref(ms)), "wgm_batch_run_per_graph")
+        check(lib.wgm_batch_run_per_graph_sized(self._h, int(default_groups), C.byref(ms)),
+              "wgm_batch_run_per_graph_sized")
         return ms.value
 
     def result(self, job: int) -> np.ndarray:

@@ -3,12 +3,16 @@
 Every translation unit is compiled by nvcc in parallel with
 `-gencode arch=compute_103a,code=sm_103a`; the shared library is linked with
 the static CUDA runtime so it loads on a machine without a GPU (calls then
-return WGM_ERR_NO_DEVICE).  The library is written next to this file.
+return WGM_ERR_NO_DEVICE).  The library is written next to this file; a
+SHA-256 of its sources, flags and host architecture (in _build/) decides
+whether an existing library is current.
 """
 from __future__ import annotations
 
 import concurrent.futures as cf
+import hashlib
 import os
+import platform
 import shutil
 import subprocess
 
@@ -32,15 +36,34 @@ def _nvcc() -> str:
 
 def _inputs() -> list[str]:
     files = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
-    files.append(os.path.join(ROOT, "include", "wgm.h"))
+    inc = os.path.join(ROOT, "include")
+    files += [os.path.join(inc, f) for f in os.listdir(inc)]
+    files.append(os.path.abspath(__file__))
     return files
 
 
+STAMP = os.path.join(OBJ, "libwgm.sha256")
+
+
+def _digest() -> str:
+    """Hash of every input file, the compile flags and this machine's
+    architecture: a library built elsewhere (another checkout, another
+    host architecture) or from other sources never counts as current."""
+    h = hashlib.sha256()
+    h.update(" ".join(ARCH + SOURCES).encode())
+    h.update(platform.machine().encode())
+    for f in sorted(_inputs()):
+        h.update(os.path.basename(f).encode())
+        with open(f, "rb") as fh:
+            h.update(fh.read())
+    return h.hexdigest()
+
+
 def needs_build() -> bool:
-    if not os.path.exists(LIB):
+    if not os.path.exists(LIB) or not os.path.exists(STAMP):
         return True
-    t = os.path.getmtime(LIB)
-    return any(os.path.getmtime(f) > t for f in _inputs())
+    with open(STAMP) as f:
+        return f.read().strip() != _digest()
 
 
 def _compile(src: str) -> str:
@@ -64,6 +87,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
     subprocess.run([_nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-Xcompiler", "-fopenmp",
                     "-lgomp"], check=True)
     os.replace(tmp, LIB)
+    with open(STAMP, "w") as f:
+        f.write(_digest())
     if verbose:
         print(LIB)
     return LIB

@@ -710,9 +710,13 @@ extern "C" int wgm_batch_run(wgm_batch *b, int use_cuda_graph, double *device_ms
 }
 
 /* The plain form: one standalone persistent launch (discovery, barrier per
- * level) per job, each on the whole GPU. */
-extern "C" int wgm_batch_launch_per_graph(wgm_batch *b) {
-  if (!b) return WGM_ERR_INVALID;
+ * level) per job, on every co-resident CTA (policy WGM_PER_GRAPH_ALL) or on
+ * the group count wgm_run_persistent picks by default for a Lonestar app
+ * (WGM_PER_GRAPH_DEFAULT: one group per 8192 edges, rounded up to a
+ * multiple of the SM count, at least one per SM). */
+extern "C" int wgm_batch_launch_per_graph_sized(wgm_batch *b, int policy) {
+  if (!b || (policy != WGM_PER_GRAPH_ALL && policy != WGM_PER_GRAPH_DEFAULT))
+    return WGM_ERR_INVALID;
   wgm_runtime *rt = b->rt;
   cudaSetDevice(rt->device);
   int block = rt->cfg.threads_per_wg;
@@ -740,6 +744,11 @@ extern "C" int wgm_batch_launch_per_graph(wgm_batch *b) {
     a.source = j.source;
     a.levels_out = b->d_levels + q;
     int grid = hw[j.algo];
+    if (policy == WGM_PER_GRAPH_DEFAULT) {
+      const long long sms = rt->prop.multiProcessorCount;
+      const long long want = (b->gE[j.graph] / 8192 + sms - 1) / sms * sms;
+      grid = (int)std::min<long long>(grid, std::max(sms, want));
+    }
     wgm_launch L = wgm_make_launch(rt, grid, 0, 0);
     cudaError_t e = wgm_launch_lonestar(j.algo == 1, L, a, grid, block, rt->stream);
     if (e != cudaSuccess) return wgm_cuda_fail(rt, e);
@@ -747,15 +756,23 @@ extern "C" int wgm_batch_launch_per_graph(wgm_batch *b) {
   return WGM_OK;
 }
 
-extern "C" int wgm_batch_run_per_graph(wgm_batch *b, double *device_ms) {
+extern "C" int wgm_batch_launch_per_graph(wgm_batch *b) {
+  return wgm_batch_launch_per_graph_sized(b, WGM_PER_GRAPH_ALL);
+}
+
+extern "C" int wgm_batch_run_per_graph_sized(wgm_batch *b, int policy, double *device_ms) {
   if (!b) return WGM_ERR_INVALID;
   int s = wgm_timer_start(b->rt);
-  if (!s) s = wgm_batch_launch_per_graph(b);
+  if (!s) s = wgm_batch_launch_per_graph_sized(b, policy);
   double ms = 0;
   int t = wgm_timer_stop(b->rt, &ms);
   if (!s) s = t;
   if (device_ms) *device_ms = ms;
   return s;
+}
+
+extern "C" int wgm_batch_run_per_graph(wgm_batch *b, double *device_ms) {
+  return wgm_batch_run_per_graph_sized(b, WGM_PER_GRAPH_ALL, device_ms);
 }
 
 extern "C" int wgm_batch_read(wgm_batch *b, int job, uint32_t *out, int64_t n) {

@@ -22,6 +22,7 @@
 #include "wgm_graph.cuh"
 #include "wgm_octree.cuh"
 #include "wgm_c4.cuh"
+#include "wgm_protocol.h"
 
 /* Non-persistent task kinds. */
 #define WGM_NP_MATMULT_I32 1 /* matmult.cl: int32 C = A*B, djb2 hash of the diagonal */
@@ -151,17 +152,25 @@ static __device__ void wgm_np_reduce(const wgm_np_args &a, int kid, int kn) {
 /* offer_kill / offer_fork and the resizing barrier                           */
 /* ------------------------------------------------------------------------ */
 
+/* The protocol steps of wgm_protocol.h on the GPU: gpu-scope acquire loads
+ * and acq_rel read-modify-writes. */
+struct wgm_gpu_ops {
+  static __device__ __forceinline__ int ld_acquire(int *p) { return wgm_ld_acquire_gpu(p); }
+  static __device__ __forceinline__ int cas(int *p, int cmp, int v) {
+    return wgm_atom_cas_acqrel_gpu(p, cmp, v);
+  }
+  static __device__ __forceinline__ int add(int *p, int v) { return wgm_atom_add_acqrel_gpu(p, v); }
+  static __device__ __forceinline__ void between() {}
+};
+
 /* __offer_kill (scheduler_1.cl:59-81), thread 0 only: the group with the
  * highest persistent id leaves when the scheduler wants groups; being the
- * highest id is the lock, and the decrement of num_groups releases it. */
+ * highest id is the lock, and the decrement of num_groups releases it.  The
+ * decrement of groups_to_kill is a compare-and-swap, because the scheduler
+ * may clear the word at any time (wgm_proto_offer_kill). */
 __device__ __forceinline__ bool wgm_offer_kill(const wgm_launch &L, int kid) {
-  int *kng = &L.st->k_num_groups[1][0];
-  if (kid != wgm_ld_acquire_gpu(kng) - 1) return false;
-  int tk = wgm_ld_acquire_gpu(&L.st->groups_to_kill);
-  if (tk <= 0) return false;
-  wgm_st_relaxed_gpu(&L.st->groups_to_kill, tk - 1);
-  wgm_atom_add_acqrel_gpu(kng, -1);
-  return true;
+  return wgm_proto_offer_kill<wgm_gpu_ops>(&L.st->k_num_groups[1][0], &L.st->groups_to_kill,
+                                           kid);
 }
 
 /* offer_fork (scheduler_1.cl:10-57), master thread 0 only, after every live
@@ -255,11 +264,11 @@ static __device__ int wgm_resize_barrier(const wgm_launch &L, wgm_cta *c, wgm_st
       if (res == 1) {
         wgm_st_relaxed_gpu(&st->bar_count, 0);
         int n = wgm_ld_acquire_gpu(kng);
-        int tk = query ? wgm_ld_acquire_gpu(&st->groups_to_kill) : 0;
+        const int tk = query ? wgm_ld_acquire_gpu(&st->groups_to_kill) : 0;
         if (tk > 0) {
-          /* query barrier: shrink by min(to_kill, n-1) from the top */
-          int k = min(tk, n - 1);
-          wgm_st_relaxed_gpu(&st->groups_to_kill, tk - k);
+          /* query barrier: shrink by min(to_kill, n-1) from the top; no fork
+           * while the scheduler wants groups */
+          const int k = wgm_proto_take_kills<wgm_gpu_ops>(&st->groups_to_kill, n - 1);
           wgm_atom_add_acqrel_gpu(kng, -k);
           n -= k;
         } else {

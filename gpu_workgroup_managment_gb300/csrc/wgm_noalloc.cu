@@ -18,10 +18,15 @@
  * The first call on a device (with that device current) looks the array's
  * device address up with cudaGetSymbolAddress; in host code the array's name
  * is only a host-side stand-in, never a device address.  Make that first call
- * before any stream capture.  All calls share the one array and it keeps the
- * last call's contents: each call clears the words that must start at zero,
- * and two calls whose kernels overlap on the GPU race on the array, so the
- * caller must keep calls on one device ordered (one stream, or synchronised).
+ * before any stream capture.  Every call waits for its BFS to finish (it
+ * reads the status word back and synchronises `stream`), which a stream
+ * under capture cannot do: on a capturing stream the call returns
+ * WGM_ERR_STATE at once and leaves the capture as it was.  All calls share
+ * the one array and it keeps the last call's contents: each call clears the
+ * words that must start at zero, and two calls whose kernels overlap on the
+ * GPU race on the array, so the caller must keep calls on one device ordered
+ * (one stream, or synchronised).  Calls from several host threads are
+ * serialised per device.
  */
 #include <cuda_runtime.h>
 
@@ -50,13 +55,13 @@ struct wgm_noalloc_scratch {
 constexpr int kMaxDevices = 64;
 
 struct wgm_noalloc_device {
+  std::mutex mu;                      /* orders the calls on this device */
   bool ready = false;
   wgm_noalloc_scratch *ptr = nullptr; /* device address of the array */
   int gen = 0;                        /* launch generation of this device */
   int grid = 0;
 };
 
-std::mutex g_mu;
 wgm_noalloc_device g_dev[kMaxDevices];
 
 }  // namespace
@@ -97,9 +102,14 @@ extern "C" int wgm_bfs_noalloc(const int32_t *d_row_ptr, const int32_t *d_col,
   if (cudaGetDevice(&dev) != cudaSuccess) return WGM_ERR_NO_DEVICE;
   if (dev < 0 || dev >= kMaxDevices) return WGM_ERR_INVALID;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  /* The status read-back and the stream synchronisation below would fail on
+   * a capturing stream and invalidate the caller's capture. */
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone)
+    return WGM_ERR_STATE;
 
-  std::lock_guard<std::mutex> lock(g_mu);
   wgm_noalloc_device *d = &g_dev[dev];
+  std::lock_guard<std::mutex> lock(d->mu);
   if (!d->ready) {
     int st = wgm_noalloc_setup(dev, d);
     if (st) return st;
@@ -118,6 +128,10 @@ extern "C" int wgm_bfs_noalloc(const int32_t *d_row_ptr, const int32_t *d_col,
   L.spin_ns = 2000000000ull;
   L.window_ns = 200000ull;
   L.gen = ++d->gen;
+  /* Wrap by an even amount, as the runtime's launches do: the discovery
+   * slot parity keeps alternating and no stale `published` value matches a
+   * new generation. */
+  if (d->gen >= (1 << 29)) d->gen -= (1 << 28);
   L.expected = d->grid;
   L.disc_mode = WGM_DISCOVERY_TICKET;
   L.barrier_kind = WGM_BARRIER_SENSE;

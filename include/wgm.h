@@ -311,9 +311,19 @@ int wgm_batch_kernel_info(wgm_batch *b, int *max_regs);
  * captured CUDA graph of the queue reset and the launch). */
 int wgm_batch_launch(wgm_batch *b, int use_cuda_graph);
 int wgm_batch_run(wgm_batch *b, int use_cuda_graph, double *device_ms);
-/* The plain form for comparison: one standalone persistent launch per job. */
+/* The plain form for comparison: one standalone persistent launch per job,
+ * each on every co-resident CTA (the reference's standalone run,
+ * src/host_skeleton/skel.cpp:316-355, uses the discovered group count). */
 int wgm_batch_launch_per_graph(wgm_batch *b);
 int wgm_batch_run_per_graph(wgm_batch *b, double *device_ms);
+/* The same with a group-count policy: WGM_PER_GRAPH_ALL (every co-resident
+ * CTA, as above) or WGM_PER_GRAPH_DEFAULT (the count wgm_run_persistent
+ * picks with num_wgs <= 0 for a Lonestar app: one group per 8192 edges,
+ * rounded up to a multiple of the SM count). */
+#define WGM_PER_GRAPH_ALL 0
+#define WGM_PER_GRAPH_DEFAULT 1
+int wgm_batch_launch_per_graph_sized(wgm_batch *b, int policy);
+int wgm_batch_run_per_graph_sized(wgm_batch *b, int policy, double *device_ms);
 /* Pipelined batches (no reference counterpart): upload_packed + launch +
  * read_all of one step, queued without waiting.  Steps alternate between two
  * device copies of the graphs and distances, so the upload of step k+1 and
@@ -441,8 +451,10 @@ int wgm_timer_stop(wgm_runtime *rt, double *elapsed_ms);
  * before any stream capture.  Calls share the array: calls whose kernels
  * overlap on the GPU race, so keep them ordered on one device.  `stream` is a
  * cudaStream_t (NULL: the default stream); the call returns when the BFS has
- * finished.  d_row_ptr must be a valid CSR (row_ptr[V] may be one short of
- * num_edges, as the Lonestar loader produces). */
+ * finished, so it cannot run on a stream under capture: there it returns
+ * WGM_ERR_STATE without touching the capture.  d_row_ptr must be a valid CSR
+ * (row_ptr[V] may be one short of num_edges, as the Lonestar loader
+ * produces). */
 #define WGM_NOALLOC_MAX_NODES (1 << 18)
 int wgm_bfs_noalloc(const int32_t *d_row_ptr, const int32_t *d_col, int32_t num_nodes,
                     int64_t num_edges, int32_t source, uint32_t *d_dist, void *stream);

@@ -18,11 +18,15 @@ LIB = os.path.join(HERE, "liboracle.so")
 REF_DIR = os.path.join(HERE, "_ref")
 
 
+SOURCES = ("wgm_oracle.c", "oracle_inputs.c")
+
+
 def build(force: bool = False) -> str:
-    src = os.path.join(HERE, "wgm_oracle.c")
-    if force or not os.path.exists(LIB) or os.path.getmtime(src) > os.path.getmtime(LIB):
+    srcs = [os.path.join(HERE, s) for s in SOURCES]
+    newest = max(os.path.getmtime(s) for s in srcs + [os.path.join(HERE, "wgm_oracle.h")])
+    if force or not os.path.exists(LIB) or newest > os.path.getmtime(LIB):
         tmp = LIB + ".tmp"
-        subprocess.run(["gcc", "-O2", "-fPIC", "-fopenmp", "-shared", "-o", tmp, src],
+        subprocess.run(["gcc", "-O2", "-fPIC", "-fopenmp", "-shared", "-o", tmp, *srcs],
                        check=True)
         os.replace(tmp, LIB)
     return LIB
@@ -42,6 +46,7 @@ def lib() -> C.CDLL:
             "oracle_lonestar_sssp": [I, P, P, P, I, P],
             "oracle_pannotia_color": [I, P, P, P, P],
             "oracle_pannotia_mis": [I, P, P, P, P],
+            "oracle_pannotia_mis_work": [I, P, P, P, P, P],
             "oracle_pannotia_sssp": [I, P, P, P, I, P],
             "oracle_lonestar_bfs_omp": [I, P, P, I, P, P],
             "oracle_lonestar_sssp_omp": [I, P, P, P, I, P, P],
@@ -69,6 +74,15 @@ def lib() -> C.CDLL:
         _lib.oracle_pagerank_f32_omp.argtypes = [C.c_int32, C.c_void_p, C.c_void_p, C.c_float,
                                                  C.c_int, C.c_void_p, C.c_void_p]
         _lib.oracle_reduce_min_i32.argtypes = [C.c_void_p, C.c_int64]
+        _lib.oracle_grid_edges.argtypes = [I, I]
+        _lib.oracle_grid_edges.restype = C.c_int64
+        _lib.oracle_gen_grid.argtypes = [I, I, P, P]
+        _lib.oracle_gen_grid.restype = C.c_int
+        _lib.oracle_gen_rmat.argtypes = [I, I, C.c_double, C.c_double, C.c_double, C.c_uint64,
+                                         I, C.c_uint32, C.c_uint32, P, P, P, P]
+        _lib.oracle_gen_rmat.restype = C.c_int
+        _lib.oracle_free.argtypes = [P]
+        _lib.oracle_free.restype = None
         _lib.oracle_reduce_min_f32.argtypes = [C.c_void_p, C.c_int64]
     return _lib
 
@@ -188,6 +202,17 @@ def mis(g, node_value: np.ndarray, omp: bool = False) -> np.ndarray:
     else:
         lib().oracle_pannotia_mis(V, _p(g.row_ptr), _p(g.col), _p(nv), _p(out))
     return out
+
+
+def mis_work(g, node_value: np.ndarray) -> tuple[np.ndarray, int, int]:
+    """MIS membership plus its work: edges scanned by the minimum phase and
+    active vertices, each summed over rounds."""
+    V = g.num_nodes
+    out = np.empty(V, np.int32)
+    work = np.zeros(2, np.int64)
+    nv = np.ascontiguousarray(node_value, np.float32)
+    lib().oracle_pannotia_mis_work(V, _p(g.row_ptr), _p(g.col), _p(nv), _p(out), _p(work))
+    return out, int(work[0]), int(work[1])
 
 
 def pannotia_sssp(g, source: int = 0) -> np.ndarray:

@@ -201,8 +201,11 @@ int oracle_pannotia_color(int32_t V, const int32_t *row_ptr,
 
 #define MIS_BIGNUM 99999999 /* mis.cl:1 */
 
-int oracle_pannotia_mis(int32_t V, const int32_t *row_ptr, const int32_t *col,
-                        const float *node_value, int32_t *s_array) {
+/* work[0] += edges scanned by mis1 (the active vertices' degrees, summed
+ * over rounds), work[1] += active vertices summed over rounds: the work
+ * units of the MIS bytes/s figure.  NULL: no counting. */
+static int mis_impl(int32_t V, const int32_t *row_ptr, const int32_t *col,
+                    const float *node_value, int32_t *s_array, int64_t *work) {
   int32_t num_edges = row_ptr[V];
   size_t n = (size_t)(V > 0 ? V : 1);
   int32_t *c = (int32_t *)malloc(sizeof(int32_t) * n);
@@ -225,6 +228,10 @@ int oracle_pannotia_mis(int32_t V, const int32_t *row_ptr, const int32_t *col,
       stop = 1;
       int32_t start = row_ptr[t];
       int32_t end = (t + 1 < V) ? row_ptr[t + 1] : num_edges;
+      if (work) {
+        work[0] += end - start;
+        work[1] += 1;
+      }
       float mn = (float)MIS_BIGNUM;
       for (int32_t e = start; e < end; e++)
         if (c[col[e]] == -1 && node_value[col[e]] < mn) mn = node_value[col[e]];
@@ -256,6 +263,17 @@ int oracle_pannotia_mis(int32_t V, const int32_t *row_ptr, const int32_t *col,
   free(cu);
   free(min_array);
   return rounds;
+}
+
+int oracle_pannotia_mis(int32_t V, const int32_t *row_ptr, const int32_t *col,
+                        const float *node_value, int32_t *s_array) {
+  return mis_impl(V, row_ptr, col, node_value, s_array, NULL);
+}
+
+int oracle_pannotia_mis_work(int32_t V, const int32_t *row_ptr, const int32_t *col,
+                             const float *node_value, int32_t *s_array, int64_t *work) {
+  work[0] = work[1] = 0;
+  return mis_impl(V, row_ptr, col, node_value, s_array, work);
 }
 
 /* ------------------------------------------------------------------------ */

@@ -85,6 +85,11 @@ int oracle_lonestar_sssp_omp(int32_t V, const int32_t *row_ptr,
 int oracle_pannotia_color_omp(int32_t V, const int32_t *row_ptr,
                               const int32_t *col, const float *node_value,
                               int32_t *color, float *max_d);
+/* oracle_pannotia_mis plus its work: work[0] = edges scanned by the
+ * minimum phase summed over rounds, work[1] = active vertices summed over
+ * rounds. */
+int oracle_pannotia_mis_work(int32_t V, const int32_t *row_ptr, const int32_t *col,
+                             const float *node_value, int32_t *s_array, int64_t *work);
 int oracle_pannotia_mis_omp(int32_t V, const int32_t *row_ptr,
                             const int32_t *col, const float *node_value,
                             int32_t *s_array, int32_t *scratch /* 2*V */,
@@ -127,6 +132,17 @@ int oracle_connect_four(const uint8_t *board, int32_t maxlevel, int32_t *next_mo
  * 0 .. num_sources-1.  Returns 0, or -1 when memory runs out. */
 int oracle_pannotia_bc_f64(int32_t V, const int32_t *row, const int32_t *col,
                            int32_t num_sources, double *bc);
+
+/* Seeded synthetic graphs (oracle_inputs.c): a rows x cols grid (row_ptr
+ * V+1, col oracle_grid_edges(rows, cols)), and an RMAT graph whose arrays are
+ * allocated here and released with oracle_free. */
+int64_t oracle_grid_edges(int32_t rows, int32_t cols);
+int oracle_gen_grid(int32_t rows, int32_t cols, int32_t *row_ptr, int32_t *col);
+int oracle_gen_rmat(int32_t scale, int32_t edge_factor, double a, double b, double c,
+                    uint64_t seed, int32_t permute, uint32_t wmin, uint32_t wmax,
+                    int32_t **row_ptr_out, int32_t **col_out, uint32_t **w_out,
+                    int64_t *num_edges);
+void oracle_free(void *p);
 
 #ifdef __cplusplus
 }

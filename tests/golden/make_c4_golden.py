@@ -13,12 +13,19 @@ from __future__ import annotations
 import json
 import os
 import re
+import sys
 
-REF = "/root/reference/src/test_suite/connect_four"
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "connect_four.json")
 
 
 def main() -> None:
+    sys.path.insert(0, ROOT)
+    from oracle.build_ref import reference_root
+    root = reference_root()
+    if root is None:
+        raise SystemExit("reference checkout not found (set WGM_REFERENCE_ROOT)")
+    REF = os.path.join(root, "src", "test_suite", "connect_four")
     cells = []
     with open(os.path.join(REF, "board.txt")) as f:
         for ch in f.read():

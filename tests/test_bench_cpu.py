@@ -37,3 +37,50 @@ def test_batched_oracle_matches_per_job_oracle():
         want = oracle.lonestar_bfs(gs[gi], src) if algo == "bfs" else \
             oracle.lonestar_sssp(gs[gi], src)
         assert np.array_equal(d[a.dist_off[k]:a.dist_off[k] + a.V[k]], want), k
+
+
+def test_oracle_workload_equals_product_workload():
+    """The reference arm's inputs (oracle/workload.py) are the GPU arm's,
+    array for array."""
+    sys.path.insert(0, ROOT)
+    from gpu_workgroup_managment_gb300 import graphs as G
+    from gpu_workgroup_managment_gb300.batch import batch_workload
+    from oracle import workload as W
+    for scale, ef, seed in ((8, 5, 3), (13, 11, 2024007)):
+        a, b = W.rmat(scale, ef, seed=seed), G.rmat(scale, ef, seed=seed)
+        assert np.array_equal(a.row_ptr, b.row_ptr) and np.array_equal(a.col, b.col)
+        assert np.array_equal(a.weights, b.weights)
+    a, b = W.grid(17, 29), G.grid(17, 29)
+    assert np.array_equal(a.row_ptr, b.row_ptr) and np.array_equal(a.col, b.col)
+    kw = dict(n_graphs=40, seed=5, mu=10.0, sigma=2.0, lo=8, hi=13)
+    ga, ja, ma = W.batch_workload(**kw)
+    gb, jb, mb = batch_workload(**kw)
+    assert ja == jb and ma == mb
+    for x, y in zip(ga, gb):
+        assert np.array_equal(x.row_ptr, y.row_ptr) and np.array_equal(x.col, y.col)
+        assert (x.weights is None) == (y.weights is None)
+        if x.weights is not None:
+            assert np.array_equal(x.weights, y.weights)
+
+
+def test_reference_arm_loads_no_product_library():
+    """--impl reference maps only oracle/ libraries: it never imports the
+    package and never loads libwgm.so."""
+    code = (
+        "import runpy, sys\n"
+        f"sys.argv = ['bench.py', '--impl', 'reference', '--steps', '1', '--warmup', '3']\n"
+        "try:\n"
+        f"    runpy.run_path({os.path.join(ROOT, 'bench.py')!r}, run_name='__main__')\n"
+        "except SystemExit as e:\n"
+        "    assert not e.code, e.code\n"
+        "assert not any(m.startswith('gpu_workgroup_managment_gb300') for m in sys.modules)\n"
+        "maps = open('/proc/self/maps').read()\n"
+        "assert 'libwgm.so' not in maps\n"
+        "print('CLEAN')\n")
+    out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True,
+                         timeout=600, cwd=ROOT)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = out.stdout.strip().splitlines()
+    assert lines[-1] == "CLEAN"
+    ref = json.loads(lines[-2])
+    assert ref["warmup"] == 3 and ref["steps"] == 1

@@ -57,3 +57,48 @@ def test_noalloc_rejects_graph_beyond_limit():
     st = lib.wgm_bfs_noalloc(C.c_void_p(16), C.c_void_p(16), MAX_NODES + 1, 10, 0,
                              C.c_void_p(16), None)
     assert st == STATUS_CODE["WGM_ERR_INVALID"]
+
+
+def test_noalloc_rejects_bad_arguments_then_still_matches():
+    """Arguments the entry point refuses before it launches anything: a
+    source below 0 or at num_nodes, and no column array for a graph with
+    edges.  A valid call afterwards still equals the regular entry point."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device visible to torch")
+    g = graphs.lonestar_view(graphs.rmat(12, 8, seed=5))
+    bad = STATUS_CODE["WGM_ERR_INVALID"]
+    p = C.c_void_p(16)  # never dereferenced: every case is refused first
+    for source, col in ((-1, p), (g.num_nodes, p), (0, None)):
+        st = lib.wgm_bfs_noalloc(p, col, g.num_nodes, g.num_edges, source, p, None)
+        assert st == bad, (source, col, st)
+    src = graphs.max_degree_vertex(g)
+    assert np.array_equal(_noalloc_bfs(torch, g, src), _regular_bfs(g, src))
+
+
+def test_noalloc_refuses_a_capturing_stream():
+    """The call waits for its BFS, which a stream under capture cannot do: it
+    returns WGM_ERR_STATE and the caller's capture still completes and
+    replays."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device visible to torch")
+    g = graphs.lonestar_view(graphs.grid(16, 16))
+    dev = torch.device("cuda:0")
+    rp = torch.from_numpy(g.row_ptr).to(dev)
+    col = torch.from_numpy(g.col).to(dev)
+    dist = torch.zeros(g.num_nodes, dtype=torch.int32, device=dev)
+    x = torch.zeros(4, device=dev)
+    s = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=s):
+        x.add_(1.0)
+        st = lib.wgm_bfs_noalloc(C.c_void_p(rp.data_ptr()), C.c_void_p(col.data_ptr()),
+                                 g.num_nodes, g.num_edges, 0, C.c_void_p(dist.data_ptr()),
+                                 C.c_void_p(s.cuda_stream))
+    assert st == STATUS_CODE["WGM_ERR_STATE"]
+    graph.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(x.cpu(), torch.full((4,), 1.0))  # captured once, replayed once
+    assert np.array_equal(_noalloc_bfs(torch, g, 0), _regular_bfs(g, 0))
