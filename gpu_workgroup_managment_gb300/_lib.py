@@ -76,9 +76,25 @@ class WgmGraphDesc(C.Structure):
                 ("row_ptr", C.c_void_p), ("col", C.c_void_p), ("weights", C.c_void_p)]
 
 
+class WgmAppVtable(C.Structure):
+    """wgm_app_vtable (include/wgm.h): a registered app's table; the entry
+    points are filled by the app's own library, so they stay plain
+    pointers here."""
+    _fields_ = [("version", C.c_int), ("user", C.c_void_p), ("app_name", C.c_char_p),
+                ("kernel_name", C.c_char_p), ("init", C.c_void_p), ("reset", C.c_void_p),
+                ("check", C.c_void_p), ("read_result", C.c_void_p), ("rounds", C.c_void_p),
+                ("clean", C.c_void_p), ("occupancy", C.c_void_p), ("launch", C.c_void_p),
+                ("launch_mega", C.c_void_p)]
+
+
+APP_PLUGIN = 100
+APP_VTABLE_VERSION = 1
+
 _P = C.c_void_p
 _I = C.c_int
 _PROTOS = {
+    "wgm_app_register": (_I, [_P, C.POINTER(WgmAppVtable), C.POINTER(_P)]),
+    "wgm_app_check": (_I, [_P, C.POINTER(_I)]),
     "wgm_config_default": (None, [C.POINTER(WgmConfig)]),
     "wgm_status_string": (C.c_char_p, [_I]),
     "wgm_runtime_create": (_I, [C.POINTER(WgmConfig), C.POINTER(_P)]),

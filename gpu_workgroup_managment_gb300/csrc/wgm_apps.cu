@@ -234,7 +234,9 @@ static int wgm_upload_transpose(wgm_app *a, const wgm_graph_desc *g) {
 }
 
 extern "C" int wgm_app_upload(wgm_app *a, const wgm_graph_desc *g) {
-  if (!a || a->kind == WGM_APP_OCTREE || a->kind == WGM_APP_CONNECT_FOUR) return WGM_ERR_INVALID;
+  if (!a || a->kind == WGM_APP_OCTREE || a->kind == WGM_APP_CONNECT_FOUR ||
+      a->kind == WGM_APP_PLUGIN)
+    return WGM_ERR_INVALID;
   int s = wgm_validate_graph(a->kind, g);
   if (s) return s;
   if (g->num_nodes != a->V || g->num_edges != a->E) return WGM_ERR_INVALID;
@@ -375,8 +377,8 @@ extern "C" int wgm_app_create(wgm_runtime *rt, int kind, const wgm_graph_desc *g
 }
 
 extern "C" int wgm_app_set_source(wgm_app *a, int32_t source) {
-  if (!a || a->kind == WGM_APP_OCTREE || a->kind == WGM_APP_CONNECT_FOUR || source < 0 ||
-      source >= a->V)
+  if (!a || a->kind == WGM_APP_OCTREE || a->kind == WGM_APP_CONNECT_FOUR ||
+      a->kind == WGM_APP_PLUGIN || source < 0 || source >= a->V)
     return WGM_ERR_INVALID;
   a->source = source;
   return WGM_OK;
@@ -452,6 +454,7 @@ static wgm_hubs wgm_hubs_view(const wgm_app *a) {
 
 /* Fill the kernel arguments of the app (also used by the megakernel). */
 int wgm_app_fill_mega(wgm_app *a, wgm_mega_args *A) {
+  if (a->kind == WGM_APP_PLUGIN) return WGM_ERR_INVALID; /* its own megakernel */
   A->app = wgm_kind_to_kernel(a->kind);
   switch (a->kind) {
     case WGM_APP_OCTREE: {
@@ -606,6 +609,11 @@ int wgm_app_fill_mega(wgm_app *a, wgm_mega_args *A) {
 /* Enqueue the app's standalone persistent kernel on `stream`. */
 static cudaError_t wgm_app_enqueue(wgm_app *a, const wgm_launch &L, int grid, int block,
                                    cudaStream_t stream) {
+  if (a->kind == WGM_APP_PLUGIN) {
+    if (a->vt.reset && a->vt.reset(a->vt.user, stream) != WGM_OK) return cudaErrorInvalidValue;
+    return a->vt.launch(a->vt.user, &L, grid, block, stream) == WGM_OK ? cudaSuccess
+                                                                        : cudaErrorLaunchFailure;
+  }
   wgm_mega_args A;
   std::memset(&A, 0, sizeof(A));
   if (wgm_app_fill_mega(a, &A) != WGM_OK) return cudaErrorInvalidValue;
@@ -631,9 +639,20 @@ static cudaError_t wgm_app_enqueue(wgm_app *a, const wgm_launch &L, int grid, in
   return cudaErrorInvalidValue;
 }
 
+/* Co-resident CTAs of a registered app's kernel (mega = 1: its megakernel). */
+int wgm_plugin_hw_bound(wgm_app *a, int mega, int block, int *groups) {
+  int per_sm = 0;
+  int s = a->vt.occupancy(a->vt.user, mega, block, &per_sm);
+  if (s) return s;
+  const long g = (long)per_sm * a->rt->prop.multiProcessorCount;
+  *groups = (int)std::min<long>(g, WGM_MAX_GROUPS);
+  return WGM_OK;
+}
+
 static int wgm_pick_grid(wgm_app *a, int num_wgs, int block, int *grid) {
   int hw = 0;
-  int s = wgm_hw_bound_for(a->rt, wgm_kind_to_kernel(a->kind), block, &hw);
+  int s = a->kind == WGM_APP_PLUGIN ? wgm_plugin_hw_bound(a, 0, block, &hw)
+                                    : wgm_hw_bound_for(a->rt, wgm_kind_to_kernel(a->kind), block, &hw);
   if (s) return s;
   if (hw < 1) return WGM_ERR_INVALID;
   *grid = (num_wgs > 0) ? std::min(num_wgs, hw) : hw;
@@ -767,8 +786,7 @@ extern "C" int wgm_run_persistent(wgm_runtime *rt, wgm_app *a, int num_wgs,
     stats->kernel_ms = ms;
     stats->host_ms = host_ms;
     int rounds = 0;
-    if (s == WGM_OK && cudaMemcpy(&rounds, a->d_rounds, 4, cudaMemcpyDeviceToHost) == cudaSuccess)
-      stats->rounds = rounds;
+    if (s == WGM_OK && wgm_app_rounds(a, &rounds) == WGM_OK) stats->rounds = rounds;
   }
   if (s == WGM_OK && hs_status != WGM_OK) s = hs_status;
   if (s == WGM_OK && ws != WGM_OK) s = ws;
@@ -929,6 +947,11 @@ extern "C" int wgm_octree_check(wgm_app *a, int32_t *ok) {
 }
 
 extern "C" int wgm_app_read_result(wgm_app *a, void *host_out, size_t bytes) {
+  if (a && a->kind == WGM_APP_PLUGIN) {
+    if (!host_out || !a->vt.read_result) return WGM_ERR_INVALID;
+    cudaSetDevice(a->rt->device);
+    return a->vt.read_result(a->vt.user, host_out, bytes);
+  }
   if (!a || !host_out || bytes < a->out_bytes) return WGM_ERR_INVALID;
   cudaSetDevice(a->rt->device);
   cudaError_t e =
@@ -939,7 +962,7 @@ extern "C" int wgm_app_read_result(wgm_app *a, void *host_out, size_t bytes) {
 }
 
 extern "C" int wgm_app_result_device_ptr(wgm_app *a, void **p, size_t *bytes) {
-  if (!a || !p) return WGM_ERR_INVALID;
+  if (!a || !p || a->kind == WGM_APP_PLUGIN) return WGM_ERR_INVALID;
   *p = a->d_out;
   if (bytes) *bytes = a->out_bytes;
   return WGM_OK;
@@ -948,6 +971,10 @@ extern "C" int wgm_app_result_device_ptr(wgm_app *a, void **p, size_t *bytes) {
 extern "C" int wgm_app_rounds(wgm_app *a, int *rounds) {
   if (!a || !rounds) return WGM_ERR_INVALID;
   cudaSetDevice(a->rt->device);
+  if (a->kind == WGM_APP_PLUGIN) {
+    *rounds = 0;
+    return a->vt.rounds ? a->vt.rounds(a->vt.user, rounds) : WGM_OK;
+  }
   int h = 0;
   cudaError_t e = cudaMemcpyAsync(&h, a->d_rounds, 4, cudaMemcpyDeviceToHost, a->rt->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(a->rt->stream);
@@ -960,9 +987,44 @@ extern "C" int wgm_app_destroy(wgm_app *a) {
   if (!a) return WGM_ERR_INVALID;
   cudaSetDevice(a->rt->device);
   cudaStreamSynchronize(a->rt->stream);
-  wgm_app_free_buffers(a);
+  if (a->kind == WGM_APP_PLUGIN) {
+    if (a->vt.clean) a->vt.clean(a->vt.user);
+  } else {
+    wgm_app_free_buffers(a);
+  }
   delete a;
   return WGM_OK;
+}
+
+extern "C" int wgm_app_register(wgm_runtime *rt, const wgm_app_vtable *vt, wgm_app **out) {
+  if (!rt || !vt || !out || vt->version != WGM_APP_VTABLE_VERSION || !vt->occupancy ||
+      !vt->launch)
+    return WGM_ERR_INVALID;
+  *out = nullptr;
+  cudaSetDevice(rt->device);
+  wgm_app *a = new (std::nothrow) wgm_app();
+  if (!a) return WGM_ERR_OOM;
+  a->rt = rt;
+  a->kind = WGM_APP_PLUGIN;
+  a->vt = *vt;
+  if (vt->init) {
+    int s = vt->init(vt->user, rt->device);
+    if (s) {
+      if (vt->clean) vt->clean(vt->user);
+      delete a;
+      return s;
+    }
+  }
+  *out = a;
+  return WGM_OK;
+}
+
+extern "C" int wgm_app_check(wgm_app *a, int *ok) {
+  if (!a || !ok) return WGM_ERR_INVALID;
+  cudaSetDevice(a->rt->device);
+  if (a->kind == WGM_APP_OCTREE) return wgm_octree_check(a, ok);
+  if (a->kind != WGM_APP_PLUGIN || !a->vt.check) return WGM_ERR_INVALID;
+  return a->vt.check(a->vt.user, ok);
 }
 
 extern "C" void *wgm_host_alloc(size_t bytes) {

@@ -552,61 +552,6 @@ static __device__ int wgm_phase_lonestar(const wgm_launch &Lc, wgm_cta *c,
 }
 
 /* ------------------------------------------------------------------------ */
-/* Resumable phases                                                          */
-/* ------------------------------------------------------------------------ */
-
-/* Every app runs as a sequence of phases separated by inter-CTA barriers.
- * A phase is named by (target, round); target 0 is the device-side init.
- * A phase function does its work, names the next phase and returns
- * WGM_PHASE_NEXT (a barrier follows) or WGM_PHASE_DONE.  Everything a phase
- * needs is in global memory or derivable from (target, round), so a group
- * forked in at a resizing barrier starts at the next phase with nothing but
- * that pair: the role of the reference's generated Restoration_ctx and its
- * `switch (target)` resume points (lonestar/graph_apps/bfs/device/
- * merged.cl:310-397, kernel_merge/src/ProcessPersistentKernelVisitor.cpp:
- * 110-137,401-431). */
-struct wgm_step {
-  int target;
-  int round;
-};
-#define WGM_PHASE_DONE 0
-#define WGM_PHASE_NEXT 1
-
-/* Work split of the current phase: group id and group count can change at
- * every resizing barrier, so each phase reads them afresh. */
-struct wgm_split {
-  int lane, warp, gw, NW, tid, nth;
-  __device__ __forceinline__ explicit wgm_split(const wgm_cta *c) {
-    lane = wgm_lane();
-    warp = threadIdx.x >> 5;
-    const int nw = blockDim.x >> 5;
-    gw = c->id * nw + warp;
-    NW = c->ngroups * nw;
-    tid = c->id * blockDim.x + threadIdx.x;
-    nth = c->ngroups * blockDim.x;
-  }
-};
-
-/* Run phases from `cur` until done, with `sync` between phases. */
-template <class Sync, class Phase>
-__device__ __forceinline__ void wgm_drive(const wgm_launch &L, wgm_cta *c, wgm_step cur,
-                                          Sync &&sync, Phase &&phase) {
-  for (;;) {
-    wgm_step nxt = cur;
-    if (phase(cur, &nxt) != WGM_PHASE_NEXT) return;
-    if (!sync(L, c, nxt)) return;
-    cur = nxt;
-  }
-}
-
-/* Plain barrier between phases (standalone persistent kernels). */
-struct wgm_plain_sync {
-  __device__ __forceinline__ bool operator()(const wgm_launch &L, wgm_cta *c, wgm_step) const {
-    return wgm_barrier(L, c);
-  }
-};
-
-/* ------------------------------------------------------------------------ */
 /* Pannotia colour                                                           */
 /* ------------------------------------------------------------------------ */
 

@@ -38,6 +38,7 @@ struct wgm_dev_hubs {
 struct wgm_app {
   wgm_runtime *rt = nullptr;
   int kind = 0;
+  wgm_app_vtable vt{}; /* kind == WGM_APP_PLUGIN: the registered app's table */
   int V = 0;
   int64_t E = 0;
   int hub_threshold = 256;
@@ -89,5 +90,6 @@ int wgm_kind_to_kernel(int app_kind);
 int wgm_stream_wait(wgm_runtime *rt, cudaStream_t stream);
 struct wgm_mega_args;
 int wgm_app_fill_mega(wgm_app *a, wgm_mega_args *A);
+int wgm_plugin_hw_bound(wgm_app *a, int mega, int block, int *groups);
 
 #endif

@@ -121,73 +121,13 @@ __device__ __forceinline__ void wgm_mega_run_app(const wgm_launch &L, const wgm_
   }
 }
 
-/* main_device_body.cl:1-93: group 0 schedules, every other group loops
- * "TASK_WAIT, available++ -> get_task -> run". */
+/* The built-in megakernel: the worker loop of wgm_device.cuh around the
+ * built-in apps' phase functions. */
 __global__ void __launch_bounds__(1024) wgm_k_mega(wgm_launch L, wgm_mega_args A) {
-  __shared__ wgm_cta c;  /* discovered view */
-  __shared__ wgm_cta pc; /* persistent-task view: k-ids, resizing */
   __shared__ wgm_warp_smem sm;
-  __shared__ int s_task;
-  __shared__ wgm_rctx s_rc;
-  if (!wgm_discover(L, &c)) return;
-  wgm_dev_state *st = L.st;
-  if (c.id == 0) {
-    if (threadIdx.x == 0) wgm_scheduler(L, A, c.ngroups - 1);
-    __syncthreads();
-    return;
-  }
-  for (;;) {
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      wgm_st_relaxed_gpu(&st->task_array[c.id], WGM_TASK_WAIT);
-      wgm_atom_add_acqrel_gpu(&st->available_workgroups, 1);
-      /* get_task (cl_scheduler.cl:168-187) */
-      wgm_spin s = wgm_idle_start(L, A.idle_ns);
-      int t;
-      for (;;) {
-        t = wgm_ld_acquire_gpu(&st->task_array[c.id]);
-        if (t != WGM_TASK_WAIT) break;
-        if (wgm_spin_giveup(L, s, WGM_SITE_GET_TASK)) {
-          t = WGM_TASK_QUIT;
-          break;
-        }
-      }
-      s_task = t;
-      if (t == WGM_TASK_PERSIST) s_rc = st->r_ctx_arr[c.id];
-      if (t == WGM_TASK_PERSIST) {
-        pc.id = __ldcg(&st->k_group_ids[1][c.id]);
-        pc.ngroups = s_rc.w[WGM_RC_NGROUPS];
-        pc.gen = s_rc.w[WGM_RC_GEN];
-        pc.ok = 1;
-        pc.tmp[0] = 0;
-      }
-    }
-    __syncthreads();
-    const int t = s_task;
-    if (t == WGM_TASK_QUIT) break;
-    if (t == WGM_TASK_MULT) {
-      int kid = __ldcg(&st->k_group_ids[0][c.id]);
-      int kn = __ldcg(&st->k_num_groups[0][0]);
-      if (A.np.kind == WGM_NP_MATMULT_I32 || A.np.kind == WGM_NP_MATMULT_F32)
-        wgm_np_matmult(L, A.np, kid, kn);
-      else
-        wgm_np_reduce(A.np, kid, kn);
-      __syncthreads();
-      if (threadIdx.x == 0) wgm_atom_add_acqrel_gpu(&st->k_executing[0][0], -1);
-    } else if (t == WGM_TASK_PERSIST) {
-      wgm_step start = {s_rc.w[WGM_RC_TARGET], s_rc.w[WGM_RC_ROUND]};
-      const bool query = A.use_query_barrier != 0;
-      wgm_mega_run_app(L, A, &pc, &sm, start,
-                       [&](const wgm_launch &Lx, wgm_cta *cx, wgm_step nx) {
-                         return wgm_resize_barrier(Lx, cx, nx, query) == 1;
-                       });
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        wgm_atom_add_acqrel_gpu(&st->k_executing[1][0], -1);
-        wgm_atom_add_acqrel_sys(&L.hf->persistent_flag, -1);
-      }
-    }
-  }
+  wgm_mega_body(L, A.ctl, [&](wgm_cta *pc, wgm_step start, auto &sync) {
+    wgm_mega_run_app(L, A, pc, &sm, start, sync);
+  });
 }
 
 /* ------------------------------------------------------------------------ */
@@ -393,41 +333,59 @@ extern "C" int wgm_comm_launch_mega_kernel(wgm_comm *c, int num_wgs) {
   wgm_comm_join(c);
   int block = rt->cfg.threads_per_wg;
   if (block < 32 || block > 1024 || block % 32) block = 256;
-  int per_sm = 0;
-  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wgm_k_mega, block, 0);
-  if (e != cudaSuccess) return wgm_comm_fail(c, e);
-  int hw = std::min(per_sm * rt->prop.multiProcessorCount, WGM_MAX_GROUPS);
+  /* a registered app brings its own megakernel (wgm_app_mega_kernel) */
+  const bool plugin = c->papp && c->papp->kind == WGM_APP_PLUGIN;
+  if (plugin && !c->papp->vt.launch_mega) return WGM_ERR_INVALID;
+  int per_sm = 0, hw = 0;
+  cudaError_t e = cudaSuccess;
+  if (plugin) {
+    int s = wgm_plugin_hw_bound(c->papp, 1, block, &hw);
+    if (s) return s;
+  } else {
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wgm_k_mega, block, 0);
+    if (e != cudaSuccess) return wgm_comm_fail(c, e);
+    hw = std::min(per_sm * rt->prop.multiProcessorCount, WGM_MAX_GROUPS);
+  }
   int grid = num_wgs > 0 ? std::min(num_wgs, hw) : hw;
   if (grid < 2) return WGM_ERR_INVALID;
   wgm_mega_args A;
   std::memset(&A, 0, sizeof(A));
   A.app = -1;
-  if (c->papp) {
+  if (c->papp && !plugin) {
     int s = wgm_app_fill_mega(c->papp, &A);
     if (s) return s;
   }
-  A.np.kind = c->np_kind;
-  A.np.n = c->np_size;
-  A.np.A = c->dA;
-  A.np.B = c->dB;
-  A.np.C = c->dC;
-  A.np.Af = c->dAf;
-  A.np.Bf = c->dBf;
-  A.np.Cf = c->dCf;
-  A.np.buf = c->dbuf;
-  A.np.buff = c->dbuff;
-  A.np.len = c->np_size;
-  A.np.hash = &c->np_dev->hash;
-  A.np.result = &c->np_dev->result;
-  A.idle_ns = wgm_idle_budget(c);
-  A.use_query_barrier = rt->cfg.use_query_barrier;
+  A.ctl.np.kind = c->np_kind;
+  A.ctl.np.n = c->np_size;
+  A.ctl.np.A = c->dA;
+  A.ctl.np.B = c->dB;
+  A.ctl.np.C = c->dC;
+  A.ctl.np.Af = c->dAf;
+  A.ctl.np.Bf = c->dBf;
+  A.ctl.np.Cf = c->dCf;
+  A.ctl.np.buf = c->dbuf;
+  A.ctl.np.buff = c->dbuff;
+  A.ctl.np.len = c->np_size;
+  A.ctl.np.hash = &c->np_dev->hash;
+  A.ctl.np.result = &c->np_dev->result;
+  A.ctl.idle_ns = wgm_idle_budget(c);
+  A.ctl.use_query_barrier = rt->cfg.use_query_barrier;
   /* restart_scheduler (rt_host/cl_scheduler.h:35-50) for the host words */
   __atomic_store_n(&rt->hf->persistent_flag, -1, __ATOMIC_RELEASE);
   __atomic_store_n(&rt->hf->participating_groups, 0, __ATOMIC_RELEASE);
   wgm_store_flag(c, WGM_DEVICE_SCHEDULER_INIT);
   wgm_launch L = wgm_make_launch(rt, grid, 0, 0);
-  wgm_k_mega<<<grid, block, 0, rt->stream>>>(L, A);
-  if ((e = cudaGetLastError()) != cudaSuccess) return wgm_comm_fail(c, e);
+  if (plugin) {
+    if (c->papp->vt.reset) {
+      int s = c->papp->vt.reset(c->papp->vt.user, rt->stream);
+      if (s) return s;
+    }
+    int s = c->papp->vt.launch_mega(c->papp->vt.user, &L, &A.ctl, grid, block, rt->stream);
+    if (s) return s == WGM_ERR_CUDA ? wgm_comm_fail(c, cudaErrorLaunchFailure) : s;
+  } else {
+    wgm_k_mega<<<grid, block, 0, rt->stream>>>(L, A);
+    if ((e = cudaGetLastError()) != cudaSuccess) return wgm_comm_fail(c, e);
+  }
   c->launched = true;
   uint64_t budget = rt->cfg.spin_timeout_ns ? rt->cfg.spin_timeout_ns * 4 : 8000000000ull;
   if (!wgm_host_wait(&rt->hf->scheduler_flag, WGM_DEVICE_WAITING, true, budget)) {

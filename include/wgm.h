@@ -39,6 +39,9 @@ extern "C" {
 #define WGM_ERR_NO_DEVICE (-7)
 #define WGM_ERR_ABORTED (-8)
 #define WGM_ERR_STATE (-9)
+/* Device-side result of the kernel API (wgm_device.cuh), not an error: this
+ * group left the persistent task at a resizing barrier or offer_kill. */
+#define WGM_KILLED 1
 
 /* ---- discovery / barrier flavours */
 #define WGM_DISCOVERY_TICKET 0
@@ -191,6 +194,63 @@ int wgm_app_result_device_ptr(wgm_app *app, void **device_ptr, size_t *bytes);
 int wgm_app_rounds(wgm_app *app, int *rounds);
 /* clean_persistent_task (bfs.h:330-334). */
 int wgm_app_destroy(wgm_app *app);
+
+/* An app built outside the library (no reference counterpart for the
+ * mechanism; the reference selects its app at compile time, skel.cpp:50-77,
+ * and binds it through the plugin functions of e.g. bfs.h:192-370):
+ * the app compiles its phase function against include/wgm_device.cuh into
+ * its own standalone kernel and megakernel (wgm_app_kernel /
+ * wgm_app_mega_kernel) and hands the runtime this table.  Each entry gets
+ * `user` first; entries marked optional may be NULL.  The runtime then
+ * runs it like a built-in app: wgm_run_persistent / wgm_launch_persistent
+ * (standalone, on discovered groups), the communicator (wgm_comm_*,
+ * resizable inside the megakernel next to non-persistent tasks),
+ * wgm_app_read_result, wgm_app_rounds, wgm_app_check, wgm_app_destroy. */
+#define WGM_APP_PLUGIN 100
+#define WGM_APP_VTABLE_VERSION 1
+typedef struct wgm_app_vtable {
+  int version;             /* WGM_APP_VTABLE_VERSION */
+  void *user;              /* the app's own state */
+  const char *app_name;    /* persistent_app_name (bfs.h:192-194) */
+  const char *kernel_name; /* persistent_kernel_name (bfs.h:196-198) */
+  /* init_persistent_app_for_occupancy / _for_real (bfs.h:209-282): device
+   * buffers and inputs, on `device`; called once by wgm_app_register.
+   * Optional. */
+  int (*init)(void *user, int device);
+  /* reset_persistent_task (bfs.h:284-313): inputs back to their initial
+   * state, queued on `stream` (cudaStream_t) before every standalone run.
+   * Optional. */
+  int (*reset)(void *user, void *stream);
+  /* check_persistent_task (bfs.h:336-370): *ok = 1 if the last run's output
+   * is right.  Optional. */
+  int (*check)(void *user, int *ok);
+  /* output_persistent_solution (color.h:180-195): the output, copied to
+   * host memory.  Optional. */
+  int (*read_result)(void *user, void *host_out, size_t bytes);
+  /* Rounds (levels, iterations) of the last run.  Optional. */
+  int (*rounds)(void *user, int *rounds);
+  /* clean_persistent_task (bfs.h:330-334).  Optional. */
+  void (*clean)(void *user);
+  /* CTAs per SM of the standalone kernel (mega = 0) or of the megakernel
+   * (mega = 1) at threads_per_wg threads: wgm_app_kernels<App>::occupancy. */
+  int (*occupancy)(void *user, int mega, int threads_per_wg, int *ctas_per_sm);
+  /* Queue the standalone kernel on `stream` with the runtime's launch record
+   * `launch` (a wgm_launch of wgm_device.cuh): wgm_app_kernels<App>::launch. */
+  int (*launch)(void *user, const void *launch, int grid, int threads_per_wg, void *stream);
+  /* Queue the megakernel with `launch` and the control block `mega` (a
+   * wgm_mega_ctl): wgm_app_kernels<App>::launch_mega.  Optional: without it
+   * the app cannot be the communicator's persistent app. */
+  int (*launch_mega)(void *user, const void *launch, const void *mega, int grid,
+                     int threads_per_wg, void *stream);
+} wgm_app_vtable;
+/* Register an app table (copied) and call its init; the app runs on this
+ * runtime's device.  If init fails, the table's clean is called and its
+ * status returned; once registered, wgm_app_destroy calls clean. */
+int wgm_app_register(wgm_runtime *rt, const wgm_app_vtable *vt, wgm_app **out);
+/* check_persistent_task of a registered app (the table's check), or of the
+ * octree (wgm_octree_check); WGM_ERR_INVALID for other built-in apps, whose
+ * outputs the caller compares itself. */
+int wgm_app_check(wgm_app *app, int *ok);
 
 /* Octree app (test_suite/final_octree/octree.h:98-132 init_persistent_app_for_real,
  * octree.cl:150-320): num_particles float4 positions (xyzw, host), boxes of

@@ -14,7 +14,7 @@
 #include <thread>
 #include <vector>
 
-#include "../../gpu_workgroup_managment_gb300/csrc/wgm_protocol.h"
+#include "../../include/wgm_protocol.h"
 
 namespace {
 
