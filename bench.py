@@ -610,11 +610,15 @@ def main() -> int:
     rt.synchronize()
     if dist:
         dist.barrier()
+    if args.kernel_only:
+        lib.wgm_profiler_start(rt.handle)  # ncu --profile-from-start off sees these
     with Clocks(local) as clk:
         rt.timer_start()
         for _ in range(args.steps):
             b.launch(True)
         ms_total = rt.timer_stop()
+    if args.kernel_only:
+        lib.wgm_profiler_stop(rt.handle)
     ms_step = _max_over_ranks(dist, ms_total / args.steps)
     value = E * ws / (ms_step * 1e-3) / 1e9
     if not np.array_equal(b.results(), res):

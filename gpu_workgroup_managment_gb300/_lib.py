@@ -94,6 +94,8 @@ _P = C.c_void_p
 _I = C.c_int
 _PROTOS = {
     "wgm_app_register": (_I, [_P, C.POINTER(WgmAppVtable), C.POINTER(_P)]),
+    "wgm_profiler_start": (_I, [_P]),
+    "wgm_profiler_stop": (_I, [_P]),
     "wgm_app_check": (_I, [_P, C.POINTER(_I)]),
     "wgm_config_default": (None, [C.POINTER(WgmConfig)]),
     "wgm_status_string": (C.c_char_p, [_I]),

@@ -6,6 +6,7 @@
  * device state in HBM, host-polled words in mapped pinned memory, one CUDA
  * stream per runtime, CUDA events for kernel time.
  */
+#include <cuda_profiler_api.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -402,4 +403,18 @@ extern "C" int wgm_timer_stop(wgm_runtime *rt, double *elapsed_ms) {
   if (e != cudaSuccess) return wgm_cuda_fail(rt, e);
   *elapsed_ms = ms;
   return WGM_OK;
+}
+
+extern "C" int wgm_profiler_start(wgm_runtime *rt) {
+  if (!rt) return WGM_ERR_INVALID;
+  cudaSetDevice(rt->device);
+  cudaError_t e = cudaProfilerStart();
+  return e == cudaSuccess ? WGM_OK : wgm_cuda_fail(rt, e);
+}
+
+extern "C" int wgm_profiler_stop(wgm_runtime *rt) {
+  if (!rt) return WGM_ERR_INVALID;
+  cudaSetDevice(rt->device);
+  cudaError_t e = cudaProfilerStop();
+  return e == cudaSuccess ? WGM_OK : wgm_cuda_fail(rt, e);
 }

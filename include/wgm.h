@@ -519,6 +519,13 @@ int wgm_timer_stop(wgm_runtime *rt, double *elapsed_ms);
 int wgm_bfs_noalloc(const int32_t *d_row_ptr, const int32_t *d_col, int32_t num_nodes,
                     int64_t num_edges, int32_t source, uint32_t *d_dist, void *stream);
 
+/* ---- profiler range (no reference counterpart) -------------------------- */
+/* cudaProfilerStart / cudaProfilerStop on the runtime's device: a profiler
+ * started with its capture off (ncu --profile-from-start off) sees only the
+ * launches in between. */
+int wgm_profiler_start(wgm_runtime *rt);
+int wgm_profiler_stop(wgm_runtime *rt);
+
 /* ---- host memory helpers (pinned, for H2D/D2H at full bandwidth) ------- */
 void *wgm_host_alloc(size_t bytes);
 void wgm_host_free(void *p);
