@@ -108,6 +108,12 @@ class Batch:
         check(lib.wgm_batch_configure_sssp(self._h, float(delta_mult), int(far_cap)),
               "configure_sssp")
 
+    def configure_sssp_dense(self, light_mult: float = 0.2) -> None:
+        """SSSP jobs on graphs of average degree >= 6: buckets of light_mult x
+        the mean weight, heavy edges relaxed once per bucket (0: off)."""
+        check(lib.wgm_batch_configure_sssp_dense(self._h, float(light_mult)),
+              "configure_sssp_dense")
+
     def launch(self, use_cuda_graph: bool = True) -> None:
         check(lib.wgm_batch_launch(self._h, int(use_cuda_graph)), "wgm_batch_launch")
 
@@ -169,9 +175,11 @@ class Batch:
         dm, fc, rg = C.c_double(), C.c_int(), C.c_int()
         check(lib.wgm_batch_sssp_info(self._h, C.byref(dm), C.byref(fc)))
         check(lib.wgm_batch_kernel_info(self._h, C.byref(rg)))
+        lm = C.c_double()
+        check(lib.wgm_batch_sssp_dense_info(self._h, C.byref(lm)))
         return {"threads": t.value, "ctas_per_sm": c.value, "piece": p.value, "ms": ms.value,
                 "team_edges": te.value, "max_team": mt.value, "sssp_delta_mult": dm.value,
-                "max_regs": rg.value}
+                "sssp_dense_mult": lm.value, "max_regs": rg.value}
 
     def close(self):
         if self._h:

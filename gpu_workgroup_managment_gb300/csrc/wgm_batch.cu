@@ -29,7 +29,7 @@ __global__ void __launch_bounds__(MAXT) wgm_k_batch(wgm_batch_args B) {
   __shared__ wgm_warp_smem sm;
   extern __shared__ wgm_lq wgm_lqs[]; /* one local queue per warp */
   wgm_lq *q = &wgm_lqs[threadIdx.x >> 5];
-  __shared__ int s_cnt[8];
+  __shared__ int s_cnt[10];
   __shared__ int s_slot;
   for (;;) {
     if (threadIdx.x == 0) s_slot = atomicAdd(&B.ctl[0], 1);
@@ -113,6 +113,10 @@ struct wgm_batch {
    * (0: 2V + 64) */
   double nf_mult = 20.0;
   int far_cap_cfg = 0;
+  /* SSSP jobs on dense graphs (average degree >= WGM_BATCH_DENSE_DEGREE):
+   * buckets of light_mult x the mean weight with heavy edges deferred
+   * (wgm_batch_job.light); 0: the schedule of the other SSSP jobs */
+  double light_mult = 0.2;
   std::vector<double> gmeanw; /* mean weight per graph (1 without weights) */
   int teams_grid = 0; /* grid the team sizes were computed for (0 = stale) */
   cudaGraph_t graph = nullptr;
@@ -168,6 +172,15 @@ extern "C" int wgm_batch_destroy(wgm_batch *b) {
   return WGM_OK;
 }
 
+/* Graphs whose SSSP jobs take the dense schedule: average degree at least
+ * this (the batch's RMAT graphs have 8-32, its grids under 4). */
+#define WGM_BATCH_DENSE_DEGREE 6
+
+static bool wgm_batch_deferred(const wgm_batch *b, const wgm_batch_job &j) {
+  return j.algo == 1 && b->nf_mult > 0 && b->light_mult > 0 &&
+         b->gE[j.graph] >= (long long)WGM_BATCH_DENSE_DEGREE * b->gV[j.graph];
+}
+
 /* Piece size of a job: the configured one, else max(32, ceil(E/V)); the
  * worklist capacity V + E/piece + 64 then bounds every level. */
 static void wgm_batch_layout(wgm_batch *b) {
@@ -182,6 +195,8 @@ static void wgm_batch_layout(wgm_batch *b) {
     j.far_cap = j.algo ? (int)(b->far_cap_cfg > 0 ? std::min<long long>(b->far_cap_cfg, fc) : fc) : 0;
     j.wl_off = wl;
     wl += 3LL * 2 * j.cap + 2LL * j.far_cap;
+    /* deferred heavy edges: two heavy lists and a settle stamp per vertex */
+    if (wgm_batch_deferred(b, j)) wl += 6LL * j.cap + V;
   }
   b->scratch_total = wl;
 }
@@ -189,12 +204,18 @@ static void wgm_batch_layout(wgm_batch *b) {
 /* Near-far bucket width of every SSSP job from its graph's mean weight. */
 static void wgm_batch_set_deltas(wgm_batch *b) {
   for (auto &j : b->jobs) {
+    j.light = 0;
     if (!j.algo || b->nf_mult <= 0) {
       j.delta = 0;
       continue;
     }
     const double w = b->gmeanw.empty() ? 1.0 : b->gmeanw[j.graph];
-    j.delta = (unsigned)std::min(1e9, std::max(1.0, std::round(b->nf_mult * w)));
+    const bool dense = wgm_batch_deferred(b, j);
+    const double mult = dense ? b->light_mult : b->nf_mult;
+    j.delta = (unsigned)std::min(1e9, std::max(1.0, std::round(mult * w)));
+    /* heavy = at least one bucket width: a heavy edge from the bucket lands
+     * at or above its end */
+    if (dense) j.light = j.delta;
   }
 }
 
@@ -533,6 +554,24 @@ extern "C" int wgm_batch_configure_sssp(wgm_batch *b, double delta_mult, int far
   int st = wgm_batch_relayout(b);
   if (st) return st;
   wgm_batch_free_graph(b);
+  return WGM_OK;
+}
+
+extern "C" int wgm_batch_configure_sssp_dense(wgm_batch *b, double light_mult) {
+  if (!b || !(light_mult >= 0) || light_mult > 1e6) return WGM_ERR_INVALID;
+  cudaSetDevice(b->rt->device);
+  cudaStreamSynchronize(b->rt->stream);
+  b->light_mult = light_mult;
+  wgm_batch_set_deltas(b);
+  int st = wgm_batch_relayout(b);
+  if (st) return st;
+  wgm_batch_free_graph(b);
+  return WGM_OK;
+}
+
+extern "C" int wgm_batch_sssp_dense_info(wgm_batch *b, double *light_mult) {
+  if (!b || !light_mult) return WGM_ERR_INVALID;
+  *light_mult = b->light_mult;
   return WGM_OK;
 }
 
@@ -941,6 +980,23 @@ extern "C" int wgm_batch_autotune(wgm_batch *b, int reps, int *best_threads,
       }
     }
     s = wgm_batch_configure_sssp(b, bm, b->far_cap_cfg);
+    if (s) return s;
+    /* 4c. bucket width of the dense graphs' SSSP jobs (heavy edges
+     * deferred), 0 = their schedule is the others' */
+    const double l0 = b->light_mult;
+    double bl = l0;
+    for (double lm : {0.0, 0.1, 0.4}) {
+      if (lm == l0) continue;
+      s = wgm_batch_configure_sssp_dense(b, lm);
+      double ms = 0;
+      if (!s) s = point(bt, bc, bp, bte, &ms);
+      if (s) return s;
+      if (ms < best) {
+        best = ms;
+        bl = lm;
+      }
+    }
+    s = wgm_batch_configure_sssp_dense(b, bl);
     if (s) return s;
   }
   /* 5. critical path: the jobs that run longest double their team, while

@@ -51,6 +51,10 @@ struct wgm_batch_job {
   int cap;
   unsigned delta; /* SSSP near-far bucket width (0: Bellman-Ford worklist) */
   int far_cap;    /* entries per far list */
+  unsigned light; /* near-far SSSP: edges of weight >= light are heavy, relaxed
+                     once per bucket (0: every edge at every visit); the
+                     scratch then also holds two heavy lists (3 x cap ints
+                     each) and a settle stamp per vertex after the far lists */
   int graph; /* graph index (host bookkeeping) */
   int team;  /* CTAs working on the job */
   int boost; /* host: team multiplier from the critical-path pass */
@@ -371,10 +375,57 @@ struct wgm_nf_state {
   int fb;   /* far list receiving parked vertices */
   int pend; /* far list drained by the last split: cleared at the next step */
   bool split_last;
+  /* heavy-edge deferral: the bucket's heavy list (parity ph), how much of it
+   * the heavy steps have relaxed, and the bucket's settle stamp */
+  int ph = 0, hdone = 0, phid = 1;
 };
 
+/* Heavy-edge deferral (delta-stepping's light/heavy split on the near-far
+ * buckets).  In a bucket's levels only light edges (weight < light, light =
+ * the bucket width) are relaxed; the first time a vertex is visited in a
+ * bucket (its first piece, a settle stamp exchanged to the bucket's id) its
+ * pieces are also appended to the bucket's heavy list.  When the near list
+ * runs dry, a heavy step relaxes the heavy edges of the listed vertices
+ * with their distances as they now stand: every vertex visited in the
+ * bucket had its distance in [bucket start, T), so a heavy edge lands at or
+ * above T and parks in the far list, and no later light relaxation of the
+ * bucket can lower a listed vertex again.  Each vertex is thus relaxed
+ * through its light edges once per improvement and through its heavy edges
+ * once per bucket it was visited in; every improvement is still followed by
+ * the relaxation of all its edges, so the fixpoint is the same.  On RMAT
+ * graphs with weights U[1,1000] the Bellman-Ford bucket reads every edge ~4
+ * times; with buckets of 0.2 x the mean weight and deferral, ~2 times
+ * (relaxations ~1 per edge). */
+struct wgm_heavy_lists {
+  int *buf;    /* 2 x 3 x cap: (start, count, vertex) by bucket parity */
+  int *settle; /* [V] id of the last bucket that visited the vertex */
+  int cap;
+  __device__ __forceinline__ int *start(int p) const { return buf + (size_t)p * 3 * cap; }
+  __device__ __forceinline__ int *cnt(int p) const { return start(p) + cap; }
+  __device__ __forceinline__ int *vtx(int p) const { return start(p) + 2 * (size_t)cap; }
+};
+
+/* A warp's pieces of one light level: lanes holding a vertex's first piece
+ * whose settle stamp was not yet this bucket's append the vertex's pieces to
+ * the bucket's heavy list (counter hc). */
+__device__ __forceinline__ void wgm_heavy_note(const int *row, int P, bool valid, int start,
+                                               int src, const wgm_heavy_lists &H, int ph,
+                                               int phid, int *hc) {
+  bool first = false;
+  if (valid && start == __ldg(&row[src]))
+    first = atomicExch(&H.settle[src], phid) != phid;
+  wgm_ls_out h;
+  h.counter = hc;
+  h.o_start = H.start(ph);
+  h.o_cnt = H.cnt(ph);
+  h.o_u = H.vtx(ph);
+  h.cap = H.cap;
+  wgm_out_push_vertices(row, P, first, src, h);
+}
+
 /* One job on one CTA.  s_cnt: 3 shared level counters, then (s_cnt[4..7])
- * the two far-list counts and least parked distances. */
+ * the two far-list counts and least parked distances, then (s_cnt[8..9])
+ * the two heavy-list counts. */
 template <bool SSSP, bool ASYNC>
 __device__ void wgm_cta_lonestar(const wgm_batch_args &B, const wgm_batch_job &j, int job,
                                  int *s_cnt, wgm_warp_smem *sm, wgm_lq *q) {
@@ -393,36 +444,48 @@ __device__ void wgm_cta_lonestar(const wgm_batch_args &B, const wgm_batch_job &j
    * the stamp scratch and copies the distances out at the end */
   constexpr bool PACK = SSSP && !ASYNC;
   unsigned *dw = PACK ? reinterpret_cast<unsigned *>(stamp) : dist;
+  const bool nf = PACK && j.delta > 0;
+  const bool defer = nf && j.light > 0;
+  int *far = wl_u + 2 * (size_t)cap;
+  wgm_heavy_lists H;
+  H.buf = far + 2 * (size_t)j.far_cap;
+  H.settle = H.buf + 6 * (size_t)cap;
+  H.cap = cap;
   for (int i = threadIdx.x; i < V; i += blockDim.x) {
     if (PACK) {
       reinterpret_cast<unsigned long long *>(stamp)[i] =
           (i == j.source) ? 0ull : (unsigned long long)WGM_LONESTAR_INF << 32;
+      if (defer) H.settle[i] = 0;
     } else {
       dist[i] = (i == j.source) ? 0u : WGM_LONESTAR_INF;
       stamp[i] = 0;
     }
   }
-  if (threadIdx.x < 8) s_cnt[threadIdx.x] = threadIdx.x >= 6 ? (int)0xffffffffu : 0;
+  if (threadIdx.x < 10) s_cnt[threadIdx.x] = (threadIdx.x == 6 || threadIdx.x == 7) ? (int)0xffffffffu : 0;
   if (lane == 0) q->n[0] = q->n[1] = 0;
   __syncthreads();
   if (threadIdx.x < 32)
     wgm_cta_push(row, j.piece, threadIdx.x == 0, j.source, &s_cnt[1], wl_start + cap,
                  wl_cnt + cap, wl_u ? wl_u + cap : nullptr, sm->acc[0]);
   __syncthreads();
-  const bool nf = PACK && j.delta > 0;
-  int *far = wl_u + 2 * (size_t)cap;
   int *fctl = s_cnt + 4;
+  int *hcnt = s_cnt + 8;
   wgm_nf_state ns{nf ? j.delta : 0xffffffffu, 0, -1, false};
-  const int Lmax = nf ? 4 * V + 16 : V + 2;
+  const int Lmax = nf ? (defer ? 8 : 4) * V + 16 : V + 2;
   int L = 1;
   for (;;) {
     const int n = s_cnt[L % 3];
-    int step = 0, nfar = 0; /* 0: level, 1: split, 2: clear only */
+    int step = 0, nfar = 0; /* 0: level, 1: split, 2: clear only, 3: heavy */
+    const int hn = defer ? hcnt[ns.ph] : 0;
     if (n == 0) {
       if (!nf) break;
-      nfar = fctl[ns.fb];
-      if (nfar == 0) break;
-      step = ns.split_last ? 2 : 1;
+      if (hn > ns.hdone) {
+        step = 3;
+      } else {
+        nfar = fctl[ns.fb];
+        if (nfar == 0) break;
+        step = ns.split_last ? 2 : 1;
+      }
     }
     if (L > Lmax) break;
     /* the counter of level L-1, read before the previous barrier */
@@ -432,6 +495,8 @@ __device__ void wgm_cta_lonestar(const wgm_batch_args &B, const wgm_batch_job &j
         fctl[ns.pend] = 0;
         fctl[2 + ns.pend] = (int)0xffffffffu;
       }
+      /* the next bucket's heavy list, last read two buckets ago */
+      if (defer && step == 1) hcnt[ns.ph ^ 1] = 0;
     }
     ns.pend = -1;
     wgm_ls_out o;
@@ -448,6 +513,10 @@ __device__ void wgm_cta_lonestar(const wgm_batch_args &B, const wgm_batch_job &j
       o.far_cap = j.far_cap;
       o.T = ns.T;
     }
+    if (defer) {
+      o.wlo = step == 3 ? j.light : 0u;
+      o.whi = step == 3 ? 0xffffffffu : j.light;
+    }
     if (step == 1) {
       const unsigned fmin = (unsigned)fctl[2 + ns.fb];
       const unsigned Tn =
@@ -461,18 +530,39 @@ __device__ void wgm_cta_lonestar(const wgm_batch_args &B, const wgm_batch_job &j
       ns.T = Tn;
       ns.pend = ns.fb;
       ns.fb = nb;
+      if (defer) {
+        ns.ph ^= 1;
+        ns.hdone = 0;
+        ns.phid++;
+      }
     }
     ns.split_last = step == 1;
+    /* the list this level walks: the near list, or a heavy step's part of
+     * the bucket's heavy list */
+    const int *ls = wl_start + io, *lc = wl_cnt + io, *lu = wl_u ? wl_u + io : nullptr;
+    int lb = 0, le = n;
+    if (step == 3) {
+      ls = H.start(ns.ph);
+      lc = H.cnt(ns.ph);
+      lu = H.vtx(ns.ph);
+      lb = ns.hdone;
+      le = hn;
+      ns.hdone = hn;
+    }
+    const int m = le - lb;
     /* pieces per warp: 32, or fewer when the list is short, so a small
      * frontier spreads over every warp instead of queueing on a few */
-    const int per = max(1, min(32, (n + nw - 1) / nw));
-    for (int b = warp * per; b < n; b += nw * per) {
+    const int per = max(1, min(32, (m + nw - 1) / nw));
+    for (int b = warp * per; b < m; b += nw * per) {
       int i = b + lane, deg = 0, start = 0, src = 0;
-      if (lane < per && i < n) {
-        start = wl_start[io + i];
-        deg = wl_cnt[io + i];
-        src = wl_u[io + i];
+      const bool valid = lane < per && i < m;
+      if (valid) {
+        start = ls[lb + i];
+        deg = lc[lb + i];
+        src = lu[lb + i];
       }
+      if (defer && step == 0)
+        wgm_heavy_note(row, j.piece, valid, start, src, H, ns.ph, ns.phid, &hcnt[ns.ph]);
       if (ASYNC)
         wgm_ls_chunk_async<SSSP>(row, col, wt, dist, stamp, V, j.piece, L, start, deg, src, o,
                                  q, 0);
@@ -587,6 +677,7 @@ struct wgm_ls_job {
   int lq_rounds;                 /* warp-local continuation rounds (async runs) */
   unsigned delta = 0;            /* packed SSSP: near-far bucket width (0: worklist) */
   int far_cap = 0;               /* entries per far list (after wl_u's 2 x cap) */
+  unsigned light = 0;            /* near-far: heavy edges deferred (wgm_batch_job.light) */
 };
 
 /* Run a job on a team of G > 1 CTAs.  The level loop is the persistent
@@ -603,17 +694,23 @@ __device__ int wgm_team_ls_run(const wgm_ls_job &J, wgm_warp_smem *sm, int *err,
   const int tid = rank * blockDim.x + threadIdx.x, nth = G * blockDim.x;
   constexpr bool PACK = SSSP && !ASYNC; /* as in wgm_cta_lonestar */
   unsigned *dw = PACK ? reinterpret_cast<unsigned *>(J.stamp) : J.dist;
+  const bool nf = PACK && J.delta > 0;
+  const bool defer = nf && J.light > 0;
+  wgm_heavy_lists H;
+  H.buf = J.wl_u + 2 * (size_t)cap + 2 * (size_t)J.far_cap;
+  H.settle = H.buf + 6 * (size_t)cap;
+  H.cap = cap;
   for (int i = tid; i < V; i += nth) {
     if (PACK) {
       reinterpret_cast<unsigned long long *>(J.stamp)[i] =
           (i == J.source) ? 0ull : (unsigned long long)WGM_LONESTAR_INF << 32;
+      if (defer) H.settle[i] = 0;
     } else {
       J.dist[i] = (i == J.source) ? 0u : WGM_LONESTAR_INF;
       if (SSSP || ASYNC) J.stamp[i] = 0;
     }
   }
   if (ASYNC && lane == 0) q->n[0] = q->n[1] = 0;
-  const bool nf = PACK && J.delta > 0;
   /* far-list counts [0..1] and least parked distances [2..3], on the
    * arrival line after its counter */
   int *fctl = J.arr + 8;
@@ -629,16 +726,24 @@ __device__ int wgm_team_ls_run(const wgm_ls_job &J, wgm_warp_smem *sm, int *err,
   unsigned long long *lw = reinterpret_cast<unsigned long long *>(J.cnt);
   int n = __ldcg(&J.cnt[1 * WGM_LINE]);
   int *far = nf ? J.wl_u + 2 * (size_t)cap : nullptr;
+  /* heavy-list counts [16..17] of the same line (zeroed with the control
+   * block before the launch) */
+  int *hcnt = J.arr + 16;
   wgm_nf_state ns{nf ? J.delta : 0xffffffffu, 0, -1, false};
-  const int Lmax = nf ? 4 * V + 16 : V + 2;
+  const int Lmax = nf ? (defer ? 8 : 4) * V + 16 : V + 2;
   int L = 1;
   for (;;) {
-    int step = 0, nfar = 0; /* 0: level, 1: split, 2: clear only */
+    int step = 0, nfar = 0; /* 0: level, 1: split, 2: clear only, 3: heavy */
+    const int hn = defer ? __ldcg(&hcnt[ns.ph]) : 0;
     if (n == 0) {
       if (!nf) break;
-      nfar = __ldcg(&fctl[ns.fb]);
-      if (nfar == 0) break;
-      step = ns.split_last ? 2 : 1;
+      if (hn > ns.hdone) {
+        step = 3;
+      } else {
+        nfar = __ldcg(&fctl[ns.fb]);
+        if (nfar == 0) break;
+        step = ns.split_last ? 2 : 1;
+      }
     }
     if (L > Lmax) break;
     if (rank == 0 && threadIdx.x == 0) {
@@ -648,6 +753,9 @@ __device__ int wgm_team_ls_run(const wgm_ls_job &J, wgm_warp_smem *sm, int *err,
         fctl[ns.pend] = 0;
         fctl[2 + ns.pend] = (int)0xffffffffu;
       }
+      /* the next bucket's heavy list: appended to only after this level's
+       * barrier, last read two buckets ago */
+      if (defer && step == 1) hcnt[ns.ph ^ 1] = 0;
     }
     ns.pend = -1;
     wgm_ls_out o;
@@ -665,6 +773,10 @@ __device__ int wgm_team_ls_run(const wgm_ls_job &J, wgm_warp_smem *sm, int *err,
       o.far_cap = J.far_cap;
       o.T = ns.T;
     }
+    if (defer) {
+      o.wlo = step == 3 ? J.light : 0u;
+      o.whi = step == 3 ? 0xffffffffu : J.light;
+    }
     if (step == 1) {
       const unsigned fmin = (unsigned)__ldcg(&fctl[2 + ns.fb]);
       const unsigned Tn =
@@ -678,18 +790,40 @@ __device__ int wgm_team_ls_run(const wgm_ls_job &J, wgm_warp_smem *sm, int *err,
       ns.T = Tn;
       ns.pend = ns.fb;
       ns.fb = nb2;
+      if (defer) {
+        ns.ph ^= 1;
+        ns.hdone = 0;
+        ns.phid++;
+      }
     }
     ns.split_last = step == 1;
+    /* the list this level walks: the near list, or a heavy step's part of
+     * the bucket's heavy list */
+    const int *ls = J.wl_start + io, *lc = J.wl_cnt + io;
+    const int *lu = J.wl_u ? J.wl_u + io : nullptr;
+    int lb = 0, le = n;
+    if (step == 3) {
+      ls = H.start(ns.ph);
+      lc = H.cnt(ns.ph);
+      lu = H.vtx(ns.ph);
+      lb = ns.hdone;
+      le = hn;
+      ns.hdone = hn;
+    }
+    const int m = le - lb;
     /* pieces per warp: 32, or fewer when the list is short, so a small
      * frontier spreads over every warp instead of queueing on a few */
-    const int per = max(1, min(32, (n + NW - 1) / NW));
-    for (int b = gw * per; b < n; b += NW * per) {
+    const int per = max(1, min(32, (m + NW - 1) / NW));
+    for (int b = gw * per; b < m; b += NW * per) {
       int i = b + lane, deg = 0, start = 0, src = 0;
-      if (lane < per && i < n) {
-        start = __ldcg(&J.wl_start[io + i]);
-        deg = __ldcg(&J.wl_cnt[io + i]);
-        if (SSSP || ASYNC) src = __ldcg(&J.wl_u[io + i]);
+      const bool valid = lane < per && i < m;
+      if (valid) {
+        start = __ldcg(&ls[lb + i]);
+        deg = __ldcg(&lc[lb + i]);
+        if (SSSP || ASYNC) src = __ldcg(&lu[lb + i]);
       }
+      if (defer && step == 0)
+        wgm_heavy_note(J.row, J.piece, valid, start, src, H, ns.ph, ns.phid, &hcnt[ns.ph]);
       if (ASYNC)
         wgm_ls_chunk_async<SSSP>(J.row, J.col, J.wt, J.dist, J.stamp, V, J.piece, L, start, deg,
                                  src, o, q, 0);
@@ -718,6 +852,7 @@ __device__ void wgm_team_lonestar(const wgm_batch_args &B, const wgm_batch_job &
   wgm_ls_job J;
   J.delta = j.delta;
   J.far_cap = j.far_cap;
+  J.light = j.light;
   J.V = j.V;
   J.source = j.source;
   J.piece = j.piece;

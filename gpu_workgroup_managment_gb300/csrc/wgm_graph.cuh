@@ -233,6 +233,9 @@ struct wgm_ls_out {
   int *far_list = nullptr;
   int far_cap = 0;
   unsigned T = 0xffffffffu;
+  /* SSSP: relax only edges of weight in [wlo, whi) (batched near-far with
+   * heavy edges deferred; the defaults relax every edge) */
+  unsigned wlo = 0, whi = 0xffffffffu;
 };
 
 /* Reserve n slots of the output list; returns the first. */
@@ -326,7 +329,7 @@ __device__ __forceinline__ bool wgm_ls_chunk(const int *row, const int *col, con
       if (SSSP) {
         unsigned wk = f[k] ? __ldg(&wt[e[k]]) : WGM_LONESTAR_INF;
         unsigned dvk = f[k] ? __ldcg(&dist[DS * sv[k] + DH]) : 0u;
-        f[k] = f[k] && wk < WGM_LONESTAR_INF; /* sssp.cl:120 */
+        f[k] = f[k] && wk < WGM_LONESTAR_INF /* sssp.cl:120 */ && wk >= o.wlo && wk < o.whi;
         alt[k] = dvk + wk;
       }
     }

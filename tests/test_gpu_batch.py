@@ -102,6 +102,67 @@ def test_batch_sssp_schedules(small_batch, mult, far_cap, team_edges):
             assert b.job_stats()["team"].max() > 1
 
 
+@pytest.mark.parametrize("light,far_cap,team_edges", [(0.05, 0, 0), (0.2, 0, 0), (0.2, 2, 1500),
+                                                      (1.0, 0, 800), (3.0, 1, 0), (0.2, 0, 400)])
+def test_batch_sssp_heavy_deferral(small_batch, light, far_cap, team_edges):
+    """SSSP on the dense (RMAT) graphs with heavy edges deferred to once per
+    bucket (buckets of `light` x the mean weight), on single CTAs and teams,
+    with far lists so small that parked vertices take the full-list path:
+    every distance equals the oracle's, across CUDA-graph replays, and the
+    sparse (grid) jobs keep their own schedule."""
+    gs, jobs = small_batch
+    want = _oracle(gs, jobs)
+    with Runtime() as rt, Batch(rt, gs, jobs) as b:
+        b.configure(256, 0, 0)
+        b.configure_local(0)
+        b.configure_teams(team_edges, 0)
+        b.configure_sssp(20.0, far_cap)
+        b.configure_sssp_dense(light)
+        for rep in range(3):
+            b.run(use_cuda_graph=rep > 0)
+            allres = b.results()
+            for k in range(len(jobs)):
+                assert np.array_equal(allres[b.offsets[k]:b.offsets[k + 1]], want[k]), (rep, k)
+        if team_edges:
+            assert b.job_stats()["team"].max() > 1
+
+
+def test_batch_heavy_deferral_dense_edge_cases():
+    """A dense graph whose weights span [1, 10^6] (most edges heavy at every
+    bucket width tried) and a clique, from several sources, on single CTAs
+    and teams."""
+    rng = np.random.default_rng(5)
+    V = 600
+    rows = [sorted(set(rng.integers(0, V, 24).tolist()) - {v}) for v in range(V)]
+    adj = {v: set(r) for v, r in enumerate(rows)}
+    for v, r in enumerate(rows):
+        for u in r:
+            adj[u].add(v)
+    rp = np.zeros(V + 1, np.int32)
+    rp[1:] = np.cumsum([len(adj[v]) for v in range(V)])
+    col = np.array([u for v in range(V) for u in sorted(adj[v])], np.int32)
+    g = graphs.Graph(rp, col)
+    lo = np.minimum(np.repeat(np.arange(V), np.diff(rp)), col)
+    hi = np.maximum(np.repeat(np.arange(V), np.diff(rp)), col)
+    g.weights = (1 + (lo * 7919 + hi * 104729) % 1000000).astype(np.uint32)
+    K = 40
+    kr = np.arange(0, K * (K - 1) + 1, K - 1, dtype=np.int32)
+    kc = np.array([u for v in range(K) for u in range(K) if u != v], np.int32)
+    clique = graphs.Graph(kr, kc)
+    clique.weights = graphs.uniform_weights(clique, 9)
+    gs = [g, clique]
+    jobs = [(0, "sssp", 0), (0, "sssp", 599), (1, "sssp", 3), (0, "bfs", 5)]
+    want = _oracle(gs, jobs)
+    with Runtime() as rt, Batch(rt, gs, jobs) as b:
+        for light, cap, te in ((0.2, 0, 0), (0.01, 3, 0), (0.001, 0, 2000), (0.5, 1, 500)):
+            b.configure_teams(te, 0)
+            b.configure_sssp(20.0, cap)
+            b.configure_sssp_dense(light)
+            b.run()
+            for k in range(len(jobs)):
+                assert np.array_equal(b.result(k), want[k]), (light, cap, te, k)
+
+
 @pytest.mark.parametrize("regs,threads", [(64, 1024), (80, 768), (96, 640), (96, 128)])
 def test_batch_register_budgets(small_batch, regs, threads):
     """The kernel built for 64, 80 and 96 registers per thread, at the
