@@ -375,30 +375,32 @@ struct wgm_nf_state {
   int fb;   /* far list receiving parked vertices */
   int pend; /* far list drained by the last split: cleared at the next step */
   bool split_last;
-  /* heavy-edge deferral: the bucket's heavy list (parity ph), how much of it
-   * the heavy steps have relaxed, and the bucket's settle stamp */
-  int ph = 0, hdone = 0, phid = 1;
+  /* heavy-edge deferral: the heavy epoch (heavy steps so far + 1); its
+   * parity selects the heavy list being filled */
+  int ep = 1;
 };
 
 /* Heavy-edge deferral (delta-stepping's light/heavy split on the near-far
- * buckets).  In a bucket's levels only light edges (weight < light, light =
- * the bucket width) are relaxed; the first time a vertex is visited in a
- * bucket (its first piece, a settle stamp exchanged to the bucket's id) its
- * pieces are also appended to the bucket's heavy list.  When the near list
- * runs dry, a heavy step relaxes the heavy edges of the listed vertices
- * with their distances as they now stand: every vertex visited in the
- * bucket had its distance in [bucket start, T), so a heavy edge lands at or
- * above T and parks in the far list, and no later light relaxation of the
- * bucket can lower a listed vertex again.  Each vertex is thus relaxed
- * through its light edges once per improvement and through its heavy edges
- * once per bucket it was visited in; every improvement is still followed by
- * the relaxation of all its edges, so the fixpoint is the same.  On RMAT
- * graphs with weights U[1,1000] the Bellman-Ford bucket reads every edge ~4
- * times; with buckets of 0.2 x the mean weight and deferral, ~2 times
- * (relaxations ~1 per edge). */
+ * buckets).  The levels of a bucket relax only light edges (weight < light,
+ * light = the bucket width).  A vertex whose first piece a level visits is
+ * also appended to the heavy list of the current epoch, unless its settle
+ * stamp already names that epoch (it is listed and not yet relaxed).  When
+ * the near list runs dry and the heavy list is not empty, a heavy step
+ * relaxes the heavy edges of the listed vertices, with their distances as
+ * they stand then, and the next epoch begins with the other list.  Any
+ * improvement of a vertex is followed by a visit (the near-far schedule
+ * visits every improved vertex), which lists it for a heavy step that runs
+ * later and reads its distance then; so every improvement is still followed
+ * by the relaxation of all its edges and the fixpoint is the same.  With
+ * exact buckets a heavy edge from bucket [lo, T) lands at or above T and
+ * waits in the far list, so there is one heavy step per bucket and each
+ * vertex is relaxed through its heavy edges once; a list holds a vertex at
+ * most once, so it fits in cap entries.  On RMAT graphs with weights
+ * U[1,1000] the Bellman-Ford bucket reads every edge ~4 times; buckets of
+ * 0.2 x the mean weight with deferral read it ~2 times and relax ~1 time. */
 struct wgm_heavy_lists {
-  int *buf;    /* 2 x 3 x cap: (start, count, vertex) by bucket parity */
-  int *settle; /* [V] id of the last bucket that visited the vertex */
+  int *buf;    /* 2 x 3 x cap: (start, count, vertex) by epoch parity */
+  int *settle; /* [V] the epoch whose heavy list holds the vertex */
   int cap;
   __device__ __forceinline__ int *start(int p) const { return buf + (size_t)p * 3 * cap; }
   __device__ __forceinline__ int *cnt(int p) const { return start(p) + cap; }
@@ -406,14 +408,14 @@ struct wgm_heavy_lists {
 };
 
 /* A warp's pieces of one light level: lanes holding a vertex's first piece
- * whose settle stamp was not yet this bucket's append the vertex's pieces to
- * the bucket's heavy list (counter hc). */
+ * whose settle stamp was not yet this epoch's append the vertex's pieces to
+ * the epoch's heavy list (counter hc). */
 __device__ __forceinline__ void wgm_heavy_note(const int *row, int P, bool valid, int start,
                                                int src, const wgm_heavy_lists &H, int ph,
-                                               int phid, int *hc) {
+                                               int ep, int *hc) {
   bool first = false;
   if (valid && start == __ldg(&row[src]))
-    first = atomicExch(&H.settle[src], phid) != phid;
+    first = atomicExch(&H.settle[src], ep) != ep;
   wgm_ls_out h;
   h.counter = hc;
   h.o_start = H.start(ph);
@@ -476,10 +478,10 @@ __device__ void wgm_cta_lonestar(const wgm_batch_args &B, const wgm_batch_job &j
   for (;;) {
     const int n = s_cnt[L % 3];
     int step = 0, nfar = 0; /* 0: level, 1: split, 2: clear only, 3: heavy */
-    const int hn = defer ? hcnt[ns.ph] : 0;
+    const int hn = defer ? hcnt[ns.ep & 1] : 0;
     if (n == 0) {
       if (!nf) break;
-      if (hn > ns.hdone) {
+      if (hn > 0) {
         step = 3;
       } else {
         nfar = fctl[ns.fb];
@@ -495,8 +497,8 @@ __device__ void wgm_cta_lonestar(const wgm_batch_args &B, const wgm_batch_job &j
         fctl[ns.pend] = 0;
         fctl[2 + ns.pend] = (int)0xffffffffu;
       }
-      /* the next bucket's heavy list, last read two buckets ago */
-      if (defer && step == 1) hcnt[ns.ph ^ 1] = 0;
+      /* the next epoch's heavy list, last read at the heavy step before */
+      if (step == 3) hcnt[(ns.ep + 1) & 1] = 0;
     }
     ns.pend = -1;
     wgm_ls_out o;
@@ -530,26 +532,18 @@ __device__ void wgm_cta_lonestar(const wgm_batch_args &B, const wgm_batch_job &j
       ns.T = Tn;
       ns.pend = ns.fb;
       ns.fb = nb;
-      if (defer) {
-        ns.ph ^= 1;
-        ns.hdone = 0;
-        ns.phid++;
-      }
     }
     ns.split_last = step == 1;
-    /* the list this level walks: the near list, or a heavy step's part of
-     * the bucket's heavy list */
+    /* the list this level walks: the near list, or the epoch's heavy list */
     const int *ls = wl_start + io, *lc = wl_cnt + io, *lu = wl_u ? wl_u + io : nullptr;
-    int lb = 0, le = n;
+    int m = n;
     if (step == 3) {
-      ls = H.start(ns.ph);
-      lc = H.cnt(ns.ph);
-      lu = H.vtx(ns.ph);
-      lb = ns.hdone;
-      le = hn;
-      ns.hdone = hn;
+      ls = H.start(ns.ep & 1);
+      lc = H.cnt(ns.ep & 1);
+      lu = H.vtx(ns.ep & 1);
+      m = min(hn, cap); /* a list holds a vertex once per epoch: never more */
     }
-    const int m = le - lb;
+    const int lb = 0;
     /* pieces per warp: 32, or fewer when the list is short, so a small
      * frontier spreads over every warp instead of queueing on a few */
     const int per = max(1, min(32, (m + nw - 1) / nw));
@@ -562,7 +556,7 @@ __device__ void wgm_cta_lonestar(const wgm_batch_args &B, const wgm_batch_job &j
         src = lu[lb + i];
       }
       if (defer && step == 0)
-        wgm_heavy_note(row, j.piece, valid, start, src, H, ns.ph, ns.phid, &hcnt[ns.ph]);
+        wgm_heavy_note(row, j.piece, valid, start, src, H, ns.ep & 1, ns.ep, &hcnt[ns.ep & 1]);
       if (ASYNC)
         wgm_ls_chunk_async<SSSP>(row, col, wt, dist, stamp, V, j.piece, L, start, deg, src, o,
                                  q, 0);
@@ -572,6 +566,7 @@ __device__ void wgm_cta_lonestar(const wgm_batch_args &B, const wgm_batch_job &j
     }
     if (ASYNC) wgm_ls_local_rounds<SSSP>(row, col, wt, dist, stamp, V, j.piece, L, o, q,
                                          B.lq_rounds);
+    if (step == 3) ns.ep++;
     __syncthreads();
     L++;
   }
@@ -734,10 +729,10 @@ __device__ int wgm_team_ls_run(const wgm_ls_job &J, wgm_warp_smem *sm, int *err,
   int L = 1;
   for (;;) {
     int step = 0, nfar = 0; /* 0: level, 1: split, 2: clear only, 3: heavy */
-    const int hn = defer ? __ldcg(&hcnt[ns.ph]) : 0;
+    const int hn = defer ? __ldcg(&hcnt[ns.ep & 1]) : 0;
     if (n == 0) {
       if (!nf) break;
-      if (hn > ns.hdone) {
+      if (hn > 0) {
         step = 3;
       } else {
         nfar = __ldcg(&fctl[ns.fb]);
@@ -753,9 +748,9 @@ __device__ int wgm_team_ls_run(const wgm_ls_job &J, wgm_warp_smem *sm, int *err,
         fctl[ns.pend] = 0;
         fctl[2 + ns.pend] = (int)0xffffffffu;
       }
-      /* the next bucket's heavy list: appended to only after this level's
-       * barrier, last read two buckets ago */
-      if (defer && step == 1) hcnt[ns.ph ^ 1] = 0;
+      /* the next epoch's heavy list: appended to only after this level's
+       * barrier, last read at the heavy step before */
+      if (step == 3) hcnt[(ns.ep + 1) & 1] = 0;
     }
     ns.pend = -1;
     wgm_ls_out o;
@@ -790,27 +785,19 @@ __device__ int wgm_team_ls_run(const wgm_ls_job &J, wgm_warp_smem *sm, int *err,
       ns.T = Tn;
       ns.pend = ns.fb;
       ns.fb = nb2;
-      if (defer) {
-        ns.ph ^= 1;
-        ns.hdone = 0;
-        ns.phid++;
-      }
     }
     ns.split_last = step == 1;
-    /* the list this level walks: the near list, or a heavy step's part of
-     * the bucket's heavy list */
+    /* the list this level walks: the near list, or the epoch's heavy list */
     const int *ls = J.wl_start + io, *lc = J.wl_cnt + io;
     const int *lu = J.wl_u ? J.wl_u + io : nullptr;
-    int lb = 0, le = n;
+    int m = n;
     if (step == 3) {
-      ls = H.start(ns.ph);
-      lc = H.cnt(ns.ph);
-      lu = H.vtx(ns.ph);
-      lb = ns.hdone;
-      le = hn;
-      ns.hdone = hn;
+      ls = H.start(ns.ep & 1);
+      lc = H.cnt(ns.ep & 1);
+      lu = H.vtx(ns.ep & 1);
+      m = min(hn, cap); /* a list holds a vertex once per epoch: never more */
     }
-    const int m = le - lb;
+    const int lb = 0;
     /* pieces per warp: 32, or fewer when the list is short, so a small
      * frontier spreads over every warp instead of queueing on a few */
     const int per = max(1, min(32, (m + NW - 1) / NW));
@@ -823,7 +810,8 @@ __device__ int wgm_team_ls_run(const wgm_ls_job &J, wgm_warp_smem *sm, int *err,
         if (SSSP || ASYNC) src = __ldcg(&lu[lb + i]);
       }
       if (defer && step == 0)
-        wgm_heavy_note(J.row, J.piece, valid, start, src, H, ns.ph, ns.phid, &hcnt[ns.ph]);
+        wgm_heavy_note(J.row, J.piece, valid, start, src, H, ns.ep & 1, ns.ep,
+                       &hcnt[ns.ep & 1]);
       if (ASYNC)
         wgm_ls_chunk_async<SSSP>(J.row, J.col, J.wt, J.dist, J.stamp, V, J.piece, L, start, deg,
                                  src, o, q, 0);
@@ -834,6 +822,7 @@ __device__ int wgm_team_ls_run(const wgm_ls_job &J, wgm_warp_smem *sm, int *err,
     if (ASYNC)
       wgm_ls_local_rounds<SSSP>(J.row, J.col, J.wt, J.dist, J.stamp, V, J.piece, L, o, q,
                                 J.lq_rounds);
+    if (step == 3) ns.ep++;
     n = wgm_team_level_barrier(err, spin_ns, o.counter64, G);
     if (n < 0) return -1;
     L++;

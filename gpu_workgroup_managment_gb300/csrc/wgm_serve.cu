@@ -69,6 +69,7 @@ __global__ void __launch_bounds__(1024) wgm_k_serve(wgm_launch L, wgm_serve_args
         pc.gen = s_rc.w[WGM_RC_GEN];
         pc.ok = 1;
         pc.tmp[0] = 0;
+        pc.tmp[3] = s_rc.w[WGM_RC_SERVE_SLOW];
       } else if (t == WGM_TASK_REQ) {
         s_req = __ldcg(&A.sd->slot_req[c.id]);
         s_rank = __ldcg(&A.sd->slot_rank[c.id]);

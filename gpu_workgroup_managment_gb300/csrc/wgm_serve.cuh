@@ -74,7 +74,22 @@ struct wgm_serve_dev {
   int pad3[WGM_LINE - 2];
   int completed;                      /* requests finished */
   int pad4[WGM_LINE - 1];
+  /* the persistent job's barrier (wgm_serve_barrier): the released
+   * generation in the low half, 1 in the high half when the next barrier
+   * resizes; and the arrivals of the current barrier, plus
+   * WGM_SERVE_RESIZE_FLAG for every request of a resizing barrier */
+  unsigned long long gate;
+  int pad5[WGM_LINE - 2];
+  int arrive;
+  int pad6[WGM_LINE - 1];
 };
+
+#define WGM_SERVE_RESIZE_FLAG (1 << 16)
+#define WGM_SERVE_ARRIVALS 0xffff
+/* restoration record word: the group's next barrier resizes */
+#define WGM_RC_SERVE_SLOW 4
+/* free groups beyond the reserve that make the scheduler ask for a fork */
+#define WGM_SERVE_FORK_MIN 16
 
 /* Host-visible words of the serving loop (mapped pinned memory). */
 struct wgm_serve_host {
@@ -392,37 +407,87 @@ __device__ int wgm_phase_combo(const wgm_launch &L, wgm_cta *c, const wgm_serve_
   return rep + 1 < A.reps ? WGM_PHASE_NEXT : WGM_PHASE_DONE;
 }
 
-/* Resizing barrier of the served form: global_barrier_resize
- * (iw_barrier.cl:165-227) as in the megakernel - a slave first offers to
- * die, the master waits for every live slave - with a fork that takes free
- * groups from the bitmap (any slots) and only when no request is waiting,
- * leaving `reserve` groups free for the next requests.  Warp 0 of the master
- * scans the bitmap.  Returns 1 to continue, 0 if this group was killed, -1
- * on a failed wait. */
+__device__ __forceinline__ unsigned long long wgm_ld_acquire_gpu_u64(const unsigned long long *p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void wgm_st_release_gpu_u64(unsigned long long *p,
+                                                       unsigned long long v) {
+  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ int wgm_atom_exch_acqrel_gpu_s(int *p, int v) {
+  int old;
+  asm volatile("atom.acq_rel.gpu.global.exch.b32 %0, [%1], %2;"
+               : "=r"(old) : "l"(p), "r"(v) : "memory");
+  return old;
+}
+
+/* Wait until the job's gate releases generation g + 1; returns its resize
+ * bit, or -1 when the wait gave up. */
+__device__ __forceinline__ int wgm_serve_gate_wait(const wgm_launch &L, wgm_serve_dev *sd, int g) {
+  wgm_spin s = wgm_spin_start(L);
+  for (;;) {
+    const unsigned long long v = wgm_ld_acquire_gpu_u64(&sd->gate);
+    if ((int)((unsigned)v - (unsigned)(g + 1)) >= 0) return (int)(v >> 32);
+    if (wgm_spin_giveup(L, s, WGM_SITE_RESIZE_BARRIER)) return -1;
+  }
+}
+
+/* Barrier of the served form's persistent job.  Most barriers are plain:
+ * every group adds one arrival, the last one releases the next generation
+ * (a sense barrier, two dependent L2 round trips).  A barrier resizes only
+ * when the one before it said so, in the high half of the generation word
+ * it released: the scheduler asks for that by adding WGM_SERVE_RESIZE_FLAG
+ * to the arrival word when a request waits for groups (or free groups could
+ * be taken back), and the last arriver, resetting the word, sees the flag.
+ * Every group reads the bit with the generation it waits for, so all agree
+ * on the next barrier's kind without another round trip.
+ *
+ * A resizing barrier is global_barrier_resize (iw_barrier.cl:165-227) as in
+ * the megakernel - a slave first offers to die, the master waits for every
+ * live slave - with a fork that takes free groups from the bitmap (any
+ * slots) and only when no request is waiting, leaving `reserve` groups free
+ * for the next requests.  Warp 0 of the master scans the bitmap.  The master
+ * keeps the next barrier resizing while a request still wants groups.  So
+ * the reference's kill on arrival happens within two barriers of the
+ * request, and the plain barriers the job runs otherwise cost what its
+ * standalone barrier costs.  Returns 1 to continue, 0 if this group was
+ * killed, -1 on a failed wait. */
 #define WGM_SERVE_FORK_MAX 256
 static __device__ int wgm_serve_barrier(const wgm_launch &L, wgm_cta *c, wgm_step nxt,
                                         const wgm_serve_args &A, int nslots, int *s_claim) {
   __shared__ int s_want;
   wgm_dev_state *st = L.st;
+  wgm_serve_dev *sd = A.sd;
   int *kng = &st->k_num_groups[1][0];
   __syncthreads();
   if (threadIdx.x < 32) {
     const int g = c->gen;
-    int res = 1;
-    if (c->id != 0) {
+    int res = 1, slow = 0;
+    const bool resize = c->tmp[3] != 0;
+    if (!resize) {
+      if (threadIdx.x == 0) {
+        const int r = wgm_atom_add_acqrel_gpu(&sd->arrive, 1);
+        if ((r & WGM_SERVE_ARRIVALS) + 1 == c->ngroups) {
+          const unsigned old = (unsigned)wgm_atom_exch_acqrel_gpu_s(&sd->arrive, 0);
+          slow = (old >> 16) != 0 ? 1 : 0;
+          wgm_st_release_gpu_u64(&sd->gate,
+                                 (unsigned)(g + 1) | ((unsigned long long)slow << 32));
+        } else {
+          slow = wgm_serve_gate_wait(L, sd, g);
+          if (slow < 0) res = -1;
+        }
+      }
+    } else if (c->id != 0) {
       if (threadIdx.x == 0) {
         if (wgm_offer_kill(L, c->id)) {
           res = 0;
-          atomicAdd(&A.sd->kills, 1);
+          atomicAdd(&sd->kills, 1);
         } else {
-          wgm_atom_add_acqrel_gpu(&st->bar_count, 1);
-          wgm_spin s = wgm_spin_start(L);
-          while ((int)((unsigned)wgm_ld_acquire_gpu(&st->bar_gen) - (unsigned)(g + 1)) < 0) {
-            if (wgm_spin_giveup(L, s, WGM_SITE_RESIZE_BARRIER)) {
-              res = -1;
-              break;
-            }
-          }
+          wgm_atom_add_acqrel_gpu(&sd->arrive, 1);
+          slow = wgm_serve_gate_wait(L, sd, g);
+          if (slow < 0) res = -1;
         }
       }
     } else {
@@ -430,7 +495,7 @@ static __device__ int wgm_serve_barrier(const wgm_launch &L, wgm_cta *c, wgm_ste
       if (threadIdx.x == 0) {
         wgm_spin s = wgm_spin_start(L);
         for (;;) {
-          int arrived = wgm_ld_acquire_gpu(&st->bar_count);
+          int arrived = wgm_ld_acquire_gpu(&sd->arrive) & WGM_SERVE_ARRIVALS;
           n = wgm_ld_acquire_gpu(kng);
           if (arrived == n - 1) break;
           if (wgm_spin_giveup(L, s, WGM_SITE_RESIZE_BARRIER)) {
@@ -440,9 +505,10 @@ static __device__ int wgm_serve_barrier(const wgm_launch &L, wgm_cta *c, wgm_ste
         }
         int want = 0;
         if (res == 1) {
-          wgm_st_relaxed_gpu(&st->bar_count, 0);
+          const unsigned old = (unsigned)wgm_atom_exch_acqrel_gpu_s(&sd->arrive, 0);
           n = wgm_ld_acquire_gpu(kng);
-          if (wgm_ld_acquire_gpu(&A.sd->pending) == 0) {
+          slow = ((old >> 16) != 0 || wgm_ld_acquire_gpu(&st->groups_to_kill) > 0) ? 1 : 0;
+          if (wgm_ld_acquire_gpu(&sd->pending) == 0) {
             int spare = wgm_ld_acquire_gpu(&st->available_workgroups) - A.reserve;
             want = min(spare, WGM_SERVE_FORK_MAX);
             if (want > 0 && !wgm_try_lock(&st->pool_lock)) want = 0;
@@ -453,7 +519,7 @@ static __device__ int wgm_serve_barrier(const wgm_launch &L, wgm_cta *c, wgm_ste
       __syncwarp();
       const int want = s_want;
       int got = 0;
-      if (want > 0) got = wgm_pool_claim(A.sd, nslots, want, s_claim);
+      if (want > 0) got = wgm_pool_claim(sd, nslots, want, s_claim);
       __syncwarp();
       if (threadIdx.x == 0 && res == 1) {
         if (want > 0) {
@@ -463,6 +529,7 @@ static __device__ int wgm_serve_barrier(const wgm_launch &L, wgm_cta *c, wgm_ste
           rc.w[WGM_RC_ROUND] = nxt.round;
           rc.w[WGM_RC_GEN] = g + 1;
           rc.w[WGM_RC_NGROUPS] = n + got;
+          rc.w[WGM_RC_SERVE_SLOW] = slow;
           for (int k = 0; k < got; k++) {
             const int slot = s_claim[k];
             st->k_group_ids[1][slot] = n + k;
@@ -473,7 +540,7 @@ static __device__ int wgm_serve_barrier(const wgm_launch &L, wgm_cta *c, wgm_ste
             atomicAdd(&st->k_executing[1][0], got);
             wgm_atom_add_acqrel_sys(&L.hf->persistent_flag, got);
             atomicAdd(&st->available_workgroups, -got);
-            atomicAdd(&A.sd->forks, got);
+            atomicAdd(&sd->forks, got);
             for (int k = 0; k < got; k++)
               wgm_st_release_gpu(&st->task_array[s_claim[k]], WGM_TASK_PERSIST);
           }
@@ -481,14 +548,17 @@ static __device__ int wgm_serve_barrier(const wgm_launch &L, wgm_cta *c, wgm_ste
           n += got;
         }
         wgm_st_relaxed_gpu(&st->bar_num_groups, n);
-        wgm_st_release_gpu(&st->bar_gen, g + 1);
+        wgm_st_release_gpu_u64(&sd->gate, (unsigned)(g + 1) | ((unsigned long long)slow << 32));
       }
     }
     if (threadIdx.x == 0) {
       c->gen = g + 1;
-      if (res == 1) c->ngroups = wgm_ld_acquire_gpu(&st->bar_num_groups);
+      /* the group count changes only at resizing barriers; after one it is
+       * the count the master published with the release */
+      if (res == 1 && resize) c->ngroups = wgm_ld_acquire_gpu(&st->bar_num_groups);
       if (res == -1) c->ok = 0;
       c->tmp[1] = res;
+      c->tmp[3] = slow > 0 ? 1 : 0;
     }
   }
   __syncthreads();
@@ -559,11 +629,13 @@ static __device__ bool wgm_serve_scheduler(const wgm_launch &L, const wgm_serve_
       wgm_st_relaxed_gpu(&st->bar_num_groups, P);
       wgm_st_relaxed_gpu(&st->k_executing[1][0], P);
       wgm_st_relaxed_gpu(&st->groups_to_kill, 0);
-      wgm_st_relaxed_gpu(&st->bar_count, 0);
+      wgm_st_relaxed_gpu(&sd->arrive, 0);
       wgm_st_release_sys(&L.hf->persistent_flag, P);
     }
-    rc.w[WGM_RC_GEN] = wgm_bcast(lane == 0 ? wgm_ld_acquire_gpu(&st->bar_gen) : 0);
+    rc.w[WGM_RC_GEN] =
+        wgm_bcast(lane == 0 ? (int)(unsigned)wgm_ld_acquire_gpu_u64(&sd->gate) : 0);
     rc.w[WGM_RC_NGROUPS] = P;
+    rc.w[WGM_RC_SERVE_SLOW] = 1; /* the job's first barrier resizes */
     for (int done = 0; done < P;) {
       const int want = min(P - done, WGM_SERVE_FORK_MAX);
       const int got = wgm_pool_claim(sd, nslots, want, s_claim);
@@ -575,6 +647,7 @@ static __device__ bool wgm_serve_scheduler(const wgm_launch &L, const wgm_serve_
     if (lane == 0) wgm_unlock(&st->pool_lock);
   }
   int seen = 0, started = 0;
+  unsigned fork_gen = 0xffffffffu; /* gate generation of the last fork request */
   wgm_spin idle = wgm_idle_start(L, A.idle_ns);
   for (;;) {
     bool progress = false;
@@ -609,7 +682,11 @@ static __device__ bool wgm_serve_scheduler(const wgm_launch &L, const wgm_serve_
       if (avail < G) {
         if (lane == 0) {
           int tk = wgm_ld_relaxed_gpu(&st->groups_to_kill);
-          if (tk < G - avail) wgm_st_release_gpu(&st->groups_to_kill, G - avail);
+          if (tk < G - avail) {
+            wgm_st_release_gpu(&st->groups_to_kill, G - avail);
+            /* the job's next barrier resizes */
+            atomicAdd(&sd->arrive, WGM_SERVE_RESIZE_FLAG);
+          }
           wgm_unlock(&st->pool_lock);
         }
         __syncwarp();
@@ -648,6 +725,17 @@ static __device__ bool wgm_serve_scheduler(const wgm_launch &L, const wgm_serve_
       }
       started++;
       progress = true;
+    }
+    /* free groups the job could take back: ask for a resizing barrier, at
+     * most once per barrier generation */
+    if (lane == 0 && started == seen &&
+        wgm_ld_acquire_gpu(&st->k_executing[1][0]) > 0 &&
+        wgm_ld_acquire_gpu(&st->available_workgroups) - A.reserve >= WGM_SERVE_FORK_MIN) {
+      const unsigned gen = (unsigned)wgm_ld_acquire_gpu_u64(&sd->gate);
+      if (gen != fork_gen) {
+        fork_gen = gen;
+        atomicAdd(&sd->arrive, WGM_SERVE_RESIZE_FLAG);
+      }
     }
     /* end: host done, every request finished, the persistent job left */
     int fin = 0;
