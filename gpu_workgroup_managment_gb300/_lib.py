@@ -96,6 +96,8 @@ _PROTOS = {
     "wgm_app_register": (_I, [_P, C.POINTER(WgmAppVtable), C.POINTER(_P)]),
     "wgm_batch_configure_sssp_dense": (_I, [_P, C.c_double]),
     "wgm_batch_sssp_dense_info": (_I, [_P, C.POINTER(C.c_double)]),
+    "wgm_barrier_bench_cluster": (_I, [_P, _I, _I, _I, _I, C.POINTER(C.c_double),
+                                       C.POINTER(C.c_double), C.POINTER(_I)]),
     "wgm_profiler_start": (_I, [_P]),
     "wgm_profiler_stop": (_I, [_P]),
     "wgm_app_check": (_I, [_P, C.POINTER(_I)]),

@@ -225,3 +225,37 @@ cudaError_t wgm_launch_barrier_bench(const wgm_launch &L, const wgm_barrier_benc
   wgm_k_barrier_bench<<<grid, block, 0, s>>>(L, a);
   return cudaGetLastError();
 }
+
+/* The barrier microbenchmark as a cluster grid: `clusters` clusters of
+ * `csize` CTAs (WGM_BARRIER_CLUSTER needs whole clusters). */
+cudaError_t wgm_barrier_bench_clusters(int csize, int block, int *clusters) {
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = (unsigned)csize;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3((unsigned)csize, 1, 1);
+  cfg.blockDim = dim3((unsigned)block, 1, 1);
+  cfg.dynamicSmemBytes = 0;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaOccupancyMaxActiveClusters(clusters, (void *)wgm_k_barrier_bench, &cfg);
+}
+
+cudaError_t wgm_launch_barrier_bench_cluster(const wgm_launch &L, const wgm_barrier_bench_args &a,
+                                             int clusters, int csize, int block, cudaStream_t s) {
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = (unsigned)csize;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3((unsigned)(clusters * csize), 1, 1);
+  cfg.blockDim = dim3((unsigned)block, 1, 1);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, wgm_k_barrier_bench, L, a);
+}

@@ -58,5 +58,8 @@ cudaError_t wgm_launch_c4(const wgm_launch &L, const wgm_c4_args &a, int grid, i
                           cudaStream_t s);
 cudaError_t wgm_launch_barrier_bench(const wgm_launch &L, const wgm_barrier_bench_args &a,
                                      int grid, int block, cudaStream_t s);
+cudaError_t wgm_barrier_bench_clusters(int csize, int block, int *clusters);
+cudaError_t wgm_launch_barrier_bench_cluster(const wgm_launch &L, const wgm_barrier_bench_args &a,
+                                             int clusters, int csize, int block, cudaStream_t s);
 
 #endif

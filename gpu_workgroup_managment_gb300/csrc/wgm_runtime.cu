@@ -382,6 +382,57 @@ extern "C" int wgm_barrier_bench(wgm_runtime *rt, int threads_per_wg, int num_wg
   return WGM_OK;
 }
 
+extern "C" int wgm_barrier_bench_cluster(wgm_runtime *rt, int threads_per_wg, int cluster_size,
+                                         int num_clusters, int iterations, double *ns_per_barrier,
+                                         double *kernel_ms, int *groups) {
+  if (!rt || threads_per_wg < 32 || threads_per_wg > 1024 || threads_per_wg % 32 ||
+      iterations < 1 || cluster_size < 1 || cluster_size > 8)
+    return WGM_ERR_INVALID;
+  cudaSetDevice(rt->device);
+  int fit = 0;
+  cudaError_t e = wgm_barrier_bench_clusters(cluster_size, threads_per_wg, &fit);
+  if (e != cudaSuccess) return wgm_cuda_fail(rt, e);
+  if (fit < 1) return WGM_ERR_TOO_MANY_GROUPS;
+  const int clusters = num_clusters > 0 ? std::min(num_clusters, fit) : fit;
+  if ((long)clusters * cluster_size > WGM_MAX_GROUPS) return WGM_ERR_TOO_MANY_GROUPS;
+  int saved = rt->cfg.barrier_kind;
+  rt->cfg.barrier_kind = WGM_BARRIER_CLUSTER;
+  wgm_launch L = wgm_make_launch(rt, clusters * cluster_size, 0, 0);
+  rt->cfg.barrier_kind = saved;
+  wgm_barrier_bench_args a;
+  a.iterations = iterations;
+  a.groups_out = (int *)rt->d_scratch;
+  a.t_first = (unsigned long long *)(rt->d_scratch + 8);
+  a.t_last = (unsigned long long *)(rt->d_scratch + 16);
+  e = cudaEventRecord(rt->ev0, rt->stream);
+  if (e == cudaSuccess)
+    e = wgm_launch_barrier_bench_cluster(L, a, clusters, cluster_size, threads_per_wg,
+                                         rt->stream);
+  if (e == cudaSuccess) e = cudaEventRecord(rt->ev1, rt->stream);
+  if (e != cudaSuccess) return wgm_cuda_fail(rt, e);
+  int st = wgm_stream_wait(rt, rt->stream);
+  int f = wgm_finish_launch(rt, nullptr, nullptr);
+  if (!st) st = f;
+  if (st) return st;
+  unsigned char host[64];
+  e = cudaMemcpy(host, rt->d_scratch, 64, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return wgm_cuda_fail(rt, e);
+  int ngroups = 0;
+  unsigned long long t0 = 0, t1 = 0;
+  std::memcpy(&ngroups, host, sizeof(int));
+  std::memcpy(&t0, host + 8, 8);
+  std::memcpy(&t1, host + 16, 8);
+  if (groups) *groups = ngroups;
+  /* every CTA must have been discovered for whole clusters */
+  if (ngroups != clusters * cluster_size) return WGM_ERR_TIMEOUT;
+  long nb = (long)iterations * 10 - 1;
+  if (ns_per_barrier) *ns_per_barrier = nb > 0 ? (double)(t1 - t0) / (double)nb : 0.0;
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, rt->ev0, rt->ev1);
+  if (kernel_ms) *kernel_ms = ms;
+  return WGM_OK;
+}
+
 extern "C" int wgm_timer_start(wgm_runtime *rt) {
   if (!rt) return WGM_ERR_INVALID;
   cudaSetDevice(rt->device);

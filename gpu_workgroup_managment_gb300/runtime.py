@@ -122,6 +122,17 @@ class Runtime:
         return {"ns_per_barrier": ns.value, "kernel_ms": ms.value, "groups": g.value,
                 "barriers": iterations * 10}
 
+    def barrier_bench_cluster(self, iterations: int = 1000, threads_per_wg: int = 256,
+                              cluster_size: int = 8, num_clusters: int = 0) -> dict:
+        """os_freq over every co-resident cluster of cluster_size CTAs, with the
+        cluster barrier (hardware cluster barrier + one leader per cluster)."""
+        ns, ms, g = C.c_double(), C.c_double(), C.c_int()
+        check(lib.wgm_barrier_bench_cluster(self._h, threads_per_wg, cluster_size, num_clusters,
+                                            iterations, C.byref(ns), C.byref(ms), C.byref(g)),
+              "barrier_bench_cluster")
+        return {"ns_per_barrier": ns.value, "kernel_ms": ms.value, "groups": g.value,
+                "barriers": iterations * 10, "cluster_size": cluster_size}
+
     def synchronize(self) -> None:
         check(lib.wgm_synchronize(self._h), "wgm_synchronize")
 

@@ -52,6 +52,9 @@ extern "C" {
 #define WGM_BARRIER_COUNT 3 /* monotonic arrival counter, waiters poll it */
 #define WGM_BARRIER_SPREAD 4 /* counter, generation released on 16 lines */
 #define WGM_BARRIER_AUTO 5   /* COUNT up to 384 groups, SENSE above (the default) */
+#define WGM_BARRIER_CLUSTER 6 /* CTAs of a thread-block cluster meet at the hardware
+                                 cluster barrier, one leader per cluster at a counting
+                                 barrier (wgm_barrier_bench_cluster) */
 
 /* ---- persistent apps (the reference selects them by macro, skel.cpp:50-77) */
 #define WGM_APP_LONESTAR_BFS 1
@@ -144,6 +147,12 @@ int wgm_hw_occupancy_bound(wgm_runtime *rt, int app_kind, int threads_per_wg, in
 int wgm_barrier_bench(wgm_runtime *rt, int threads_per_wg, int num_wgs, int iterations,
                       int barrier_kind, double *ns_per_barrier, double *kernel_ms,
                       int *groups);
+/* The same over every co-resident cluster of cluster_size CTAs (1-8),
+ * launched as a cluster grid, with WGM_BARRIER_CLUSTER (no reference
+ * counterpart: OpenCL has no clusters).  num_clusters <= 0: as many as fit. */
+int wgm_barrier_bench_cluster(wgm_runtime *rt, int threads_per_wg, int cluster_size,
+                              int num_clusters, int iterations, double *ns_per_barrier,
+                              double *kernel_ms, int *groups);
 
 /* ---- persistent app plugins -------------------------------------------- */
 /* persistent_app_name / persistent_kernel_name (e.g. bfs.h:192-198). */

@@ -75,6 +75,8 @@
  * barrier for a few hundred CTAs and the slowest for a thousand. */
 #define WGM_BARRIER_AUTO 5
 #define WGM_BARRIER_AUTO_COUNT_MAX 384
+/* cluster barrier: launches with a cluster dimension only */
+#define WGM_BARRIER_CLUSTER 6
 
 #define WGM_POLL_CLOSED 0x40000000
 

@@ -493,6 +493,68 @@ __device__ __forceinline__ bool wgm_barrier_xf(const wgm_launch &L, wgm_cta *c,
   return c->ok && wgm_ld_relaxed_gpu(&L.st->dev_error) == 0;
 }
 
+/* Thread-block clusters (launches with a cluster dimension). */
+__device__ __forceinline__ unsigned wgm_cluster_rank() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ unsigned wgm_cluster_size() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+  return r;
+}
+/* Every thread of every CTA of the cluster: the hardware cluster barrier
+ * (release on arrival, acquire on the wait, cluster scope). */
+__device__ __forceinline__ void wgm_cluster_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\t"
+               "barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+/* Store v into the same shared-memory word of the cluster's CTA `rank`. */
+__device__ __forceinline__ void wgm_st_cluster_peer(int *smem_word, unsigned rank, int v) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(smem_word);
+  unsigned ra;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(a), "r"(rank));
+  asm volatile("st.shared::cluster.u32 [%0], %1;" ::"r"(ra), "r"(v) : "memory");
+}
+
+/* Cluster barrier (WGM_BARRIER_CLUSTER; the launch has a cluster dimension
+ * and every discovered CTA's cluster is whole).  The CTAs of a cluster meet
+ * at the hardware cluster barrier; the cluster's rank-0 CTA alone takes part
+ * in a counting barrier over the clusters (one red.release per cluster,
+ * ld.acquire polls), then copies its outcome into the other CTAs' shared
+ * memory and releases them with a second cluster barrier.  With 8 CTAs per
+ * cluster the L2 line sees one arrival and one poller per 8 CTAs, which is
+ * what makes a barrier over every co-resident 256-thread CTA cheaper than
+ * the single-counter barriers.  Cumulativity carries every CTA's writes
+ * before the barrier through its cluster's release/acquire and the leaders'
+ * gpu-scope release/acquire to every CTA after it. */
+__device__ __forceinline__ bool wgm_barrier_cluster(const wgm_launch &L, wgm_cta *c, int ngroups) {
+  const unsigned csize = wgm_cluster_size(), rank = wgm_cluster_rank();
+  wgm_cluster_sync();
+  if (rank == 0 && threadIdx.x < 32) {
+    int ok = c->ok;
+    if (threadIdx.x == 0) {
+      int *ctr = &L.st->bar_arrivals[(L.gen & 1) * WGM_LINE];
+      const unsigned target = (unsigned)c->tmp[2] + (unsigned)(ngroups / (int)csize);
+      c->tmp[2] = (int)target;
+      wgm_red_add_release_gpu(ctr, 1);
+      wgm_spin s = wgm_spin_start(L);
+      while ((int)((unsigned)wgm_ld_acquire_gpu(ctr) - target) < 0) {
+        if (wgm_spin_giveup(L, s, WGM_SITE_BARRIER)) {
+          ok = 0;
+          break;
+        }
+      }
+      c->ok = ok;
+    }
+    ok = __shfl_sync(0xffffffffu, ok, 0);
+    for (unsigned r = 1 + threadIdx.x; r < csize; r += 32) wgm_st_cluster_peer(&c->ok, r, ok);
+  }
+  wgm_cluster_sync();
+  return c->ok;
+}
+
 __device__ __forceinline__ bool wgm_barrier(const wgm_launch &L, wgm_cta *c) {
   /* Every 1024 barriers each CTA looks at the host abort word once (a few
    * ms of barriers), so a run the host gives up on ends soon even when no
@@ -511,6 +573,8 @@ __device__ __forceinline__ bool wgm_barrier(const wgm_launch &L, wgm_cta *c) {
       return wgm_barrier_count(L, c, c->ngroups);
     case WGM_BARRIER_SPREAD:
       return wgm_barrier_spread(L, c, c->ngroups);
+    case WGM_BARRIER_CLUSTER:
+      return wgm_barrier_cluster(L, c, c->ngroups);
     case WGM_BARRIER_AUTO:
       if (c->ngroups <= WGM_BARRIER_AUTO_COUNT_MAX) return wgm_barrier_count(L, c, c->ngroups);
       return wgm_barrier_sense(L, c, c->ngroups);
