@@ -481,6 +481,8 @@ def _served(rt, rates=(1000, 5000, 20000), reps: int = 20, reserve: int = 96) ->
                          "persist_kept": alone["persist_ms"] / st["persist_ms"],
                          "kept_vs_standalone": standalone / st["persist_ms"],
                          "kills": st["kills"], "forks": st["forks"],
+                         "persist_groups_mean": st["persist_groups_mean"],
+                         "persist_groups_min": st["persist_groups_min"],
                          "waited_for_memory": st["waited_for_memory"]})
         out["runs"] = runs
         # requests alone (no persistent job) at the lowest rate, for context

@@ -68,7 +68,8 @@ class WgmServeStats(C.Structure):
                 ("persist_reps", C.c_int), ("kills", C.c_int), ("forks", C.c_int),
                 ("groups", C.c_int), ("run_ms", C.c_double), ("exec_p50_us", C.c_double),
                 ("exec_p99_us", C.c_double), ("wait_p50_us", C.c_double),
-                ("wait_p99_us", C.c_double)]
+                ("wait_p99_us", C.c_double), ("persist_groups_mean", C.c_double),
+                ("persist_groups_min", C.c_int)]
 
 
 class WgmGraphDesc(C.Structure):
@@ -98,6 +99,7 @@ _PROTOS = {
     "wgm_batch_sssp_dense_info": (_I, [_P, C.POINTER(C.c_double)]),
     "wgm_barrier_bench_cluster": (_I, [_P, _I, _I, _I, _I, C.POINTER(C.c_double),
                                        C.POINTER(C.c_double), C.POINTER(_I)]),
+    "wgm_serve_groups_trace": (_I, [_P, _P, _P, C.c_int64, C.POINTER(C.c_int64)]),
     "wgm_profiler_start": (_I, [_P]),
     "wgm_profiler_stop": (_I, [_P]),
     "wgm_app_check": (_I, [_P, C.POINTER(_I)]),

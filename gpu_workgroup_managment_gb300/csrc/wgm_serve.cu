@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -180,6 +181,9 @@ struct wgm_serve_req_log {
 
 struct wgm_serve {
   wgm_runtime *rt = nullptr;
+  /* the persistent job's group count sampled every millisecond of the last
+   * run (CL_Communicator's groups-over-time series) */
+  std::vector<std::pair<int64_t, int32_t>> gtrace;
   wgm_app *color = nullptr, *bfs = nullptr;
   /* resident datasets */
   std::vector<wgm_serve_graph> graphs;
@@ -527,6 +531,7 @@ extern "C" int wgm_serve_run(wgm_serve *s, const wgm_serve_config *cfg, wgm_serv
   s->diag.clear();
   s->log.clear();
   s->results.clear();
+  s->gtrace.clear();
 
   wgm_serve_args A;
   std::memset(&A, 0, sizeof(A));
@@ -584,10 +589,16 @@ extern "C" int wgm_serve_run(wgm_serve *s, const wgm_serve_config *cfg, wgm_serv
   int64_t head = 0, waited_mem = 0;
   size_t next = 0;
   bool stream_open = true;
-  uint64_t persist_done_at = 0;
+  uint64_t persist_done_at = 0, next_sample = 0;
   const int reps = A.reps;
   for (;;) {
     const uint64_t now = wgm_serve_now() - t0;
+    /* cl_communicator.h:186-200: the persistent group count every 1 ms */
+    if (reps > 0 && !persist_done_at && now >= next_sample) {
+      s->gtrace.emplace_back((int64_t)now,
+                             (int32_t)__atomic_load_n(&s->hs_h->persist_groups, __ATOMIC_ACQUIRE));
+      next_sample = now + 1000000ull;
+    }
     if (now > run_budget)
       return wgm_serve_fail_run(s, WGM_ERR_TIMEOUT, "run budget", head, inflight.size(),
                                 waiting.size() - wait_head, next, arr.size());
@@ -748,6 +759,16 @@ extern "C" int wgm_serve_run(wgm_serve *s, const wgm_serve_config *cfg, wgm_serv
     st->persist_reps = sd.persist_done;
     st->kills = sd.kills;
     st->forks = sd.forks;
+    if (!s->gtrace.empty()) {
+      double sum = 0;
+      int mn = INT_MAX;
+      for (const auto &p : s->gtrace) {
+        sum += p.second;
+        mn = std::min(mn, (int)p.second);
+      }
+      st->persist_groups_mean = sum / (double)s->gtrace.size();
+      st->persist_groups_min = mn;
+    }
     st->groups = __atomic_load_n(&rt->hf->discovered, __ATOMIC_ACQUIRE);
     st->run_ms = (double)t_end / 1e6;
   }
@@ -798,6 +819,22 @@ extern "C" int wgm_serve_exec_times(wgm_serve *s, int64_t n, int64_t *exec_ns) {
     const unsigned long long t0 = i * 2 < s->rtimes.size() ? s->rtimes[2 * i] : 0;
     const unsigned long long t1 = i * 2 + 1 < s->rtimes.size() ? s->rtimes[2 * i + 1] : 0;
     exec_ns[i] = (t0 && t1 >= t0 && s->log[i].done_ns) ? (int64_t)(t1 - t0) : -1;
+  }
+  return WGM_OK;
+}
+
+/* The groups-over-time series of the last run (print_groups_time_data,
+ * cl_communicator.h:241): sample k at t_ns[k] (from the launch) saw the
+ * persistent job on groups[k] groups.  NULL arrays: *count only. */
+extern "C" int wgm_serve_groups_trace(wgm_serve *s, int64_t *t_ns, int32_t *groups,
+                                      int64_t capacity, int64_t *count) {
+  if (!s || !count) return WGM_ERR_INVALID;
+  *count = (int64_t)s->gtrace.size();
+  if (!t_ns && !groups) return WGM_OK;
+  const int64_t n = std::min<int64_t>(capacity, (int64_t)s->gtrace.size());
+  for (int64_t k = 0; k < n; k++) {
+    if (t_ns) t_ns[k] = s->gtrace[k].first;
+    if (groups) groups[k] = s->gtrace[k].second;
   }
   return WGM_OK;
 }

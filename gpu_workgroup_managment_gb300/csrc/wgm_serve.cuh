@@ -99,7 +99,8 @@ struct wgm_serve_host {
   int seen;      /* scheduler: requests read from the ring */
   int started;   /* scheduler: requests given a team */
   int persist_reps; /* persistent repetitions completed */
-  int pad1[WGM_LINE - 3];
+  int persist_groups; /* groups of the persistent job, as of its last resize */
+  int pad1[WGM_LINE - 4];
 };
 
 struct wgm_serve_args {
@@ -548,6 +549,7 @@ static __device__ int wgm_serve_barrier(const wgm_launch &L, wgm_cta *c, wgm_ste
           n += got;
         }
         wgm_st_relaxed_gpu(&st->bar_num_groups, n);
+        wgm_st_relaxed_sys(&A.hs->persist_groups, n); /* the host's groups-over-time trace */
         wgm_st_release_gpu_u64(&sd->gate, (unsigned)(g + 1) | ((unsigned long long)slow << 32));
       }
     }
@@ -630,6 +632,7 @@ static __device__ bool wgm_serve_scheduler(const wgm_launch &L, const wgm_serve_
       wgm_st_relaxed_gpu(&st->k_executing[1][0], P);
       wgm_st_relaxed_gpu(&st->groups_to_kill, 0);
       wgm_st_relaxed_gpu(&sd->arrive, 0);
+      wgm_st_relaxed_sys(&A.hs->persist_groups, P);
       wgm_st_release_sys(&L.hf->persistent_flag, P);
     }
     rc.w[WGM_RC_GEN] =

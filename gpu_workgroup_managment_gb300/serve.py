@@ -71,6 +71,18 @@ class Serve:
             check(rc, "wgm_serve_run (" + buf.value.decode() + ")")
         return {k: getattr(st, k) for k, _ in WgmServeStats._fields_}
 
+    def groups_trace(self) -> tuple[np.ndarray, np.ndarray]:
+        """(t_ns, groups): the persistent job's group count every 1 ms of the
+        last run."""
+        n = C.c_int64(0)
+        check(lib.wgm_serve_groups_trace(self._h, None, None, 0, C.byref(n)))
+        t = np.zeros(n.value, np.int64)
+        g = np.zeros(n.value, np.int32)
+        if n.value:
+            check(lib.wgm_serve_groups_trace(self._h, t.ctypes.data, g.ctypes.data, n.value,
+                                             C.byref(n)))
+        return t, g
+
     def requests(self) -> dict:
         n = C.c_int64(0)
         check(lib.wgm_serve_requests(self._h, C.byref(n), None, None, None, None, None))

@@ -480,6 +480,10 @@ typedef struct wgm_serve_stats {
    * = device time from team assignment to the last group's end; wait = the
    * rest of the latency (admission, ring, waiting for groups, completion seen) */
   double exec_p50_us, exec_p99_us, wait_p50_us, wait_p99_us;
+  /* the persistent job's group count over the run, sampled every 1 ms
+   * (cl_communicator.h:186-200): mean and least */
+  double persist_groups_mean;
+  int persist_groups_min;
 } wgm_serve_stats;
 /* color/bfs: the persistent job's apps (both NULL: requests only), created
  * with wgm_app_create on the same graph.  graphs: BFS query graphs; vecs:
@@ -505,6 +509,11 @@ int wgm_serve_requests(wgm_serve *s, int64_t *count, int32_t *kind, int32_t *arg
 int wgm_serve_result(wgm_serve *s, int64_t i, void *out, int64_t bytes);
 /* Device execution time (ns) of each request of the last run, -1 if none. */
 int wgm_serve_exec_times(wgm_serve *s, int64_t n, int64_t *exec_ns);
+/* The persistent job's group count sampled every millisecond of the last
+ * run (CL_Communicator::print_groups_time_data, cl_communicator.h:186-241):
+ * t_ns from the launch, groups at that time; NULL arrays give *count only. */
+int wgm_serve_groups_trace(wgm_serve *s, int64_t *t_ns, int32_t *groups, int64_t capacity,
+                           int64_t *count);
 /* Where the last failed run stood (host and device counters), "" if none. */
 int wgm_serve_diag(wgm_serve *s, char *buf, size_t len);
 int wgm_serve_destroy(wgm_serve *s);

@@ -105,6 +105,11 @@ def test_persistent_job_cedes_and_takes_back_groups(data):
             assert st["completed"] == st["arrived"] > 0
             assert np.array_equal(ca.result(), oracle.color(pg, nv))
             assert np.array_equal(ba.result(), oracle.lonestar_bfs(pg, src))
+            # the 1 ms groups-over-time trace saw the job shrink and grow back
+            t, g = sv.groups_trace()
+            assert len(t) == len(g) > 0 and np.all(np.diff(t) > 0)
+            assert g.min() == st["persist_groups_min"] and g.min() < g.max()
+            assert g.min() <= st["persist_groups_mean"] <= g.max()
 
 
 def test_admission_waits_for_memory(data):
