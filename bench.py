@@ -485,6 +485,8 @@ def _served(rt, rates=(1000, 5000, 20000), reps: int = 20, reserve: int = 96) ->
                          "persist_groups_min": st["persist_groups_min"],
                          "waited_for_memory": st["waited_for_memory"]})
         out["runs"] = runs
+        out["checked"] = _served_check(sv, ca, ba, qg, vecs, mats, g, src, nv, reps, reserve,
+                                       rates[-1])
         # requests alone (no persistent job) at the lowest rate, for context
         st = sv.run(rate=rates[0], duration_s=0.5, seed=11, bfs_groups=32,
                     bfs_edges_per_group=1 << 16, reduce_groups=4, matmul_groups=4)
@@ -524,7 +526,49 @@ def _summary(ex: dict) -> dict:
     out["c5"] = [{"rate": r.get("rate_offered"), "p99_us": _r(r.get("p99_us")),
                   "kept_sa": _r(r.get("kept_vs_standalone")), "kills": r.get("kills")}
                  for r in sv.get("runs", [])]
+    out["c5_checked"] = sv.get("checked", {}).get("ok")
     return out
+
+
+def _served_check(sv, ca, ba, qg, vecs, mats, g, src, nv, reps, reserve, rate) -> dict:
+    """Correctness at the benchmarked configuration: one more run at `rate`
+    with every request's output kept.  The resident job's colours and BFS
+    levels must equal its standalone launches' (bit for bit); every reduce
+    must equal the vector's minimum; up to 200 BFS queries must equal the
+    oracle's levels; every product must be within 1e-4 (relative L-inf) of a
+    float64 product."""
+    from oracle import oracle
+    ca.run()
+    ba.run()
+    want_c, want_b = ca.result().copy(), ba.result().copy()
+    sv.run(rate=rate, duration_s=60.0, reps=reps, seed=23, reserve=reserve, bfs_groups=32,
+           bfs_edges_per_group=1 << 16, reduce_groups=4, matmul_groups=4, max_in_flight=512,
+           keep_results=True)
+    ok_job = bool(np.array_equal(ca.result(), want_c) and np.array_equal(ba.result(), want_b))
+    rq = sv.requests()
+    n_bfs = n_red = n_mm = bad = 0
+    worst = 0.0
+    for i, (k, a0, a1) in enumerate(zip(rq["kind"], rq["arg0"], rq["arg1"])):
+        if rq["latency_ns"][i] < 0:
+            bad += 1
+            continue
+        r = sv.result(i, int(k), int(a0))
+        if k == 1 and n_bfs < 200:
+            n_bfs += 1
+            bad += not np.array_equal(r, oracle.lonestar_bfs(qg[a0], int(a1)))
+        elif k == 2:
+            n_red += 1
+            bad += float(r[0]) != float(vecs[a0].min())
+        elif k == 3:
+            n_mm += 1
+            ref = mats[a0, 0].astype(np.float64) @ mats[a0, 1].astype(np.float64)
+            err = float(np.max(np.abs(r - ref)) / np.max(np.abs(ref)))
+            worst = max(worst, err)
+            bad += err > 1e-4
+    return {"requests": int(len(rq["kind"])), "bfs_checked": n_bfs, "reduce_checked": n_red,
+            "matmul_checked": n_mm, "matmul_rel_linf_max": worst, "mismatches": int(bad),
+            "persistent_job_equal_to_standalone": ok_job,
+            "ok": bool(ok_job and bad == 0)}
 
 
 def main() -> int:

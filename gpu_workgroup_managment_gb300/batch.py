@@ -108,7 +108,7 @@ class Batch:
         check(lib.wgm_batch_configure_sssp(self._h, float(delta_mult), int(far_cap)),
               "configure_sssp")
 
-    def configure_sssp_dense(self, light_mult: float = 0.2) -> None:
+    def configure_sssp_dense(self, light_mult: float = 0.0) -> None:
         """SSSP jobs on graphs of average degree >= 6: buckets of light_mult x
         the mean weight, heavy edges relaxed once per bucket (0: off)."""
         check(lib.wgm_batch_configure_sssp_dense(self._h, float(light_mult)),

@@ -115,8 +115,13 @@ struct wgm_batch {
   int far_cap_cfg = 0;
   /* SSSP jobs on dense graphs (average degree >= WGM_BATCH_DENSE_DEGREE):
    * buckets of light_mult x the mean weight with heavy edges deferred
-   * (wgm_batch_job.light); 0: the schedule of the other SSSP jobs */
-  double light_mult = 0.2;
+   * (wgm_batch_job.light); 0 (the default): the schedule of the other SSSP
+   * jobs.  Off by default: on the 512-graph batch at fixed shapes the RMAT
+   * SSSP jobs ran 6-58 % longer with it (widths 0.05-1 x the mean weight):
+   * their levels grew from ~11 to 27-135, and the relaxations the split
+   * saves are mostly the failed ones the distance pre-check already makes
+   * cheap.  The autotuner still tries 0.1, 0.2 and 0.4. */
+  double light_mult = 0.0;
   std::vector<double> gmeanw; /* mean weight per graph (1 without weights) */
   int teams_grid = 0; /* grid the team sizes were computed for (0 = stale) */
   cudaGraph_t graph = nullptr;
@@ -985,7 +990,7 @@ extern "C" int wgm_batch_autotune(wgm_batch *b, int reps, int *best_threads,
      * deferred), 0 = their schedule is the others' */
     const double l0 = b->light_mult;
     double bl = l0;
-    for (double lm : {0.0, 0.1, 0.4}) {
+    for (double lm : {0.0, 0.1, 0.2, 0.4}) {
       if (lm == l0) continue;
       s = wgm_batch_configure_sssp_dense(b, lm);
       double ms = 0;

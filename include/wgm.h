@@ -371,12 +371,12 @@ int wgm_batch_configure_local(wgm_batch *b, int rounds);
  * same for every setting; only the work and the level count change. */
 int wgm_batch_configure_sssp(wgm_batch *b, double delta_mult, int far_cap);
 int wgm_batch_sssp_info(wgm_batch *b, double *delta_mult, int *far_cap);
-/* SSSP jobs on dense graphs (average degree at least 6) instead use buckets
- * of light_mult x the mean weight (default 0.2) and relax heavy edges -
- * weight at least the bucket width - once per bucket, delta-stepping's
- * light/heavy split: on RMAT graphs the Bellman-Ford bucket reads every edge
- * about four times, the split about twice.  0 gives them the schedule of
- * wgm_batch_configure_sssp.  Distances do not change. */
+/* SSSP jobs on dense graphs (average degree at least 6) can instead use
+ * buckets of light_mult x the mean weight and relax heavy edges - weight at
+ * least the bucket width - once per bucket (delta-stepping's light/heavy
+ * split).  0 (the default) gives them the schedule of
+ * wgm_batch_configure_sssp; the autotuner tries 0.1-0.4.  Distances do not
+ * change. */
 int wgm_batch_configure_sssp_dense(wgm_batch *b, double light_mult);
 int wgm_batch_sssp_dense_info(wgm_batch *b, double *light_mult);
 /* Register budget of the batched kernel (no reference counterpart): 64, 80

@@ -36,6 +36,29 @@ def test_barrier_bench(kind):
         assert 0 < res["ns_per_barrier"] < 100000
 
 
+@pytest.mark.parametrize("threads,csize", [(256, 8), (256, 2), (1024, 4)])
+def test_cluster_barrier_bench(threads, csize):
+    """The cluster barrier on a cluster grid: every CTA of every co-resident
+    cluster is discovered, and 10,000 barriers complete."""
+    with Runtime() as r:
+        res = r.barrier_bench_cluster(iterations=1000, threads_per_wg=threads,
+                                      cluster_size=csize)
+        assert res["groups"] >= r.sm_count() * (1 if threads == 1024 else 2)
+        assert res["groups"] % csize == 0
+        assert 0 < res["ns_per_barrier"] < 100000
+
+
+def test_cluster_barrier_kind_on_a_plain_launch():
+    """WGM_BARRIER_CLUSTER on a launch without clusters: every CTA is its own
+    one-CTA cluster, so it is a counting barrier; a persistent BFS using it
+    still equals the oracle."""
+    g = graphs.lonestar_view(graphs.grid(40, 40))
+    with Runtime(barrier_kind=6) as r:
+        with PersistentApp(r, "lonestar_bfs", g) as a:
+            a.run()
+            assert np.array_equal(a.result(), oracle.lonestar_bfs(g, 0))
+
+
 def test_handshake_run(rt):
     g = graphs.lonestar_view(graphs.grid(64, 64))
     with Runtime(host_handshake=1) as r:
