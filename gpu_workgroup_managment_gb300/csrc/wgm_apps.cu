@@ -147,7 +147,8 @@ static void wgm_app_free_buffers(wgm_app *a) {
                   a->d_oct_input, a->d_oct_second, a->d_oct_pools, a->d_oct_tree,
                   a->d_oct_ctr, a->d_oct_locks, a->d_oct_heads,
                   a->d_c4_board, a->d_c4_nodes, a->d_c4_pool, a->d_c4_locks,
-                  a->d_c4_heads, a->d_c4_ctr, a->d_tcv};
+                  a->d_c4_heads, a->d_c4_ctr, a->d_tcv, a->d_tcv4, a->d_cmax, a->d_cq,
+                  a->d_cqctl};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   a->hubs = wgm_dev_hubs();
@@ -434,6 +435,12 @@ extern "C" int wgm_app_set_bc_sources(wgm_app *a, int32_t num_sources) {
   return WGM_OK;
 }
 
+extern "C" int wgm_app_set_color_mode(wgm_app *a, int32_t mode) {
+  if (!a || a->kind != WGM_APP_PANNOTIA_COLOR || mode < 0 || mode > 1) return WGM_ERR_INVALID;
+  a->color_mode = mode;
+  return WGM_OK;
+}
+
 extern "C" int wgm_app_set_pagerank(wgm_app *a, float damping, int iterations) {
   if (!a || a->kind != WGM_APP_PAGERANK || iterations < 0 || !(damping >= 0.f && damping <= 1.f))
     return WGM_ERR_INVALID;
@@ -606,6 +613,35 @@ int wgm_app_fill_mega(wgm_app *a, wgm_mega_args *A) {
   return WGM_ERR_INVALID;
 }
 
+/* Colour without rounds: its buffers, on first use. */
+static cudaError_t wgm_color_async_alloc(wgm_app *a) {
+  if (a->d_tcv4) return cudaSuccess;
+  const int64_t ET = a->E; /* in-edges: the graph's, or its transpose's (same count) */
+  a->cq_cap = (int)std::min<int64_t>(INT32_MAX - 64, (int64_t)a->V + (ET + 31) / 32 + 64);
+  cudaError_t e = wgm_dmalloc(&a->d_tcv4, (size_t)std::max<int64_t>(ET, 1));
+  if (e == cudaSuccess) e = wgm_dmalloc(&a->d_cmax, (size_t)a->V);
+  if (e == cudaSuccess) e = wgm_dmalloc(&a->d_cq, 4 * (size_t)a->cq_cap);
+  if (e == cudaSuccess) e = wgm_dmalloc(&a->d_cqctl, 5 * (size_t)WGM_LINE);
+  return e;
+}
+
+static wgm_color_async_args wgm_color_async_view(const wgm_app *a) {
+  wgm_color_async_args q;
+  q.tcv4 = a->d_tcv4;
+  q.cmax = a->d_cmax;
+  q.q_start = a->d_cq;
+  q.q_cnt = a->d_cq + (size_t)a->cq_cap;
+  q.q_val = a->d_cq + 2 * (size_t)a->cq_cap;
+  q.q_col = a->d_cq + 3 * (size_t)a->cq_cap;
+  q.qcap = a->cq_cap;
+  q.ctl = a->d_cqctl;
+  return q;
+}
+
+static bool wgm_color_async_on(const wgm_app *a) {
+  return a->kind == WGM_APP_PANNOTIA_COLOR && a->color_mode == 1;
+}
+
 /* Enqueue the app's standalone persistent kernel on `stream`. */
 static cudaError_t wgm_app_enqueue(wgm_app *a, const wgm_launch &L, int grid, int block,
                                    cudaStream_t stream) {
@@ -622,6 +658,11 @@ static cudaError_t wgm_app_enqueue(wgm_app *a, const wgm_launch &L, int grid, in
     case WGM_APP_LONESTAR_SSSP:
       return wgm_launch_lonestar(a->kind == WGM_APP_LONESTAR_SSSP, L, A.ls, grid, block, stream);
     case WGM_APP_PANNOTIA_COLOR:
+      if (wgm_color_async_on(a)) {
+        cudaError_t e = wgm_color_async_alloc(a);
+        if (e != cudaSuccess) return e;
+        return wgm_launch_color_async(L, A.color, wgm_color_async_view(a), grid, block, stream);
+      }
       return wgm_launch_color(L, A.color, grid, block, stream);
     case WGM_APP_PANNOTIA_MIS:
       return wgm_launch_mis(L, A.mis, grid, block, stream);
@@ -651,8 +692,17 @@ int wgm_plugin_hw_bound(wgm_app *a, int mega, int block, int *groups) {
 
 static int wgm_pick_grid(wgm_app *a, int num_wgs, int block, int *grid) {
   int hw = 0;
-  int s = a->kind == WGM_APP_PLUGIN ? wgm_plugin_hw_bound(a, 0, block, &hw)
-                                    : wgm_hw_bound_for(a->rt, wgm_kind_to_kernel(a->kind), block, &hw);
+  int s = WGM_OK;
+  if (a->kind == WGM_APP_PLUGIN) {
+    s = wgm_plugin_hw_bound(a, 0, block, &hw);
+  } else if (wgm_color_async_on(a)) {
+    int per_sm = 0;
+    cudaError_t e = wgm_color_async_per_sm(block, &per_sm);
+    if (e != cudaSuccess) return wgm_cuda_fail(a->rt, e);
+    hw = std::min(per_sm * a->rt->prop.multiProcessorCount, WGM_MAX_GROUPS);
+  } else {
+    s = wgm_hw_bound_for(a->rt, wgm_kind_to_kernel(a->kind), block, &hw);
+  }
   if (s) return s;
   if (hw < 1) return WGM_ERR_INVALID;
   *grid = (num_wgs > 0) ? std::min(num_wgs, hw) : hw;
@@ -660,7 +710,7 @@ static int wgm_pick_grid(wgm_app *a, int num_wgs, int block, int *grid) {
    * RMAT-20) carry little work each and end in a grid barrier, so fewer
    * groups win: 304 x 256 threads ran RMAT-20 in 8.6 ms against 9.7 ms on
    * all 608 co-resident CTAs (and take the counting barrier). */
-  if (num_wgs <= 0 && a->kind == WGM_APP_PANNOTIA_COLOR) {
+  if (num_wgs <= 0 && a->kind == WGM_APP_PANNOTIA_COLOR && !wgm_color_async_on(a)) {
     const int sms = a->rt->prop.multiProcessorCount;
     *grid = std::min(hw, std::max(sms, sms * 512 / std::max(block, 1)));
   }

@@ -866,6 +866,235 @@ static __device__ int wgm_phase_color(const wgm_launch &Lc, wgm_cta *c, const wg
 }
 
 /* ------------------------------------------------------------------------ */
+/* Pannotia colour without rounds (standalone runs)                          */
+/* ------------------------------------------------------------------------ */
+
+/* colour(v) = 1 + the largest colour among v's larger out-neighbours (1 if
+ * none; degree-1 vertices 1), the recurrence wgm_phase_color computes a
+ * round at a time.  Nothing forces rounds: a vertex can take its colour the
+ * moment its last larger out-neighbour has one.  So after the same counts
+ * (wgm_phase_color's target 3) every warp works from a queue of release
+ * pieces - up to 32 in-edges of a coloured vertex with its value and colour
+ * - and, for every in-neighbour w smaller than it, raises cmax[w] to
+ * colour + 1 and takes one off pending[w] with an acq_rel atomic; the lane
+ * that takes the last one (it reads every raise of cmax[w], ordered before
+ * the other decrements) colours w with cmax[w] and queues w's in-edges.  A
+ * vertex of at most 32 in-edges goes to its warp's own stack in shared
+ * memory and is released by that warp next, so a chain of colours costs
+ * about two L2 round trips per link instead of a grid barrier per round;
+ * larger ones go to the global queue in pieces.  Degree-1 vertices start at
+ * pending 0 (coloured 1) and releases only take them below 0, so they are
+ * never coloured again - the reference's quirk (color.cl:46).  Colours are
+ * the round-based form's, bit for bit; the run reports the largest colour
+ * as its round count. */
+#define WGM_CA_STACK 64
+struct wgm_color_async_args {
+  int4 *tcv4;   /* [in-edges] {in-neighbour w, bits of w's value, w's first
+                   in-edge, w's in-degree} */
+  int *cmax;    /* [V] 1 + the largest releaser colour so far */
+  int *q_start, *q_cnt, *q_val, *q_col; /* [qcap] release pieces (q_cnt -1 until
+                                           written, with release) */
+  int qcap;
+  int *ctl;     /* lines: 0 queue head, 1 tail, 2 pieces done, 3 pieces in all,
+                   4 largest colour */
+};
+struct wgm_ca_stack { /* per warp, shared memory: pieces of one edge window */
+  int start[WGM_CA_STACK], cnt[WGM_CA_STACK], val[WGM_CA_STACK], col[WGM_CA_STACK];
+  int n;
+};
+
+/* Init (between barriers): colours, pending counts, cmax, the in-edge
+ * records, the queue's ready words and the control lines. */
+__device__ __forceinline__ void wgm_color_async_init(const wgm_cta *c, const wgm_color_args &a,
+                                                     const wgm_color_async_args &q) {
+  const wgm_split s(c);
+  const int V = a.V;
+  for (int i = s.tid; i < V; i += s.nth) {
+    a.color[i] = -1;
+    a.pending[i] = 0;
+    q.cmax[i] = 0;
+  }
+  const int ET = __ldg(&a.trow[V]);
+  for (int e = s.tid; e < ET; e += s.nth) {
+    const int w = __ldg(&a.tcol[e]);
+    const int t0 = __ldg(&a.trow[w]);
+    q.tcv4[e] = make_int4(w, __float_as_int(__ldg(&a.node_value[w])), t0,
+                          __ldg(&a.trow[w + 1]) - t0);
+  }
+  for (int i = s.tid; i < q.qcap; i += s.nth) q.q_cnt[i] = -1;
+  if (c->id == 0 && threadIdx.x < 5) q.ctl[threadIdx.x * WGM_LINE] = 0;
+}
+
+/* Queue the release pieces of the flagged lanes' vertices (vertex record
+ * rec = tcv4-style {w, value bits, first in-edge, in-degree}, colour cw):
+ * one-piece vertices onto the warp's stack while it has room, the rest onto
+ * the global queue.  Warp-collective.  Returns false on a full queue. */
+__device__ __forceinline__ bool wgm_ca_push(bool flag, int4 rec, int cw,
+                                            const wgm_color_async_args &q, wgm_ca_stack *st) {
+  const int lane = wgm_lane();
+  const int deg = flag ? rec.w : 0;
+  bool local = deg > 0 && deg <= 32;
+  const unsigned lm = __ballot_sync(WGM_FULL, local);
+  const int nloc = __popc(lm);
+  int n0 = 0;
+  if (lane == 0) n0 = st->n;
+  n0 = __shfl_sync(WGM_FULL, n0, 0);
+  if (n0 + nloc > WGM_CA_STACK) local = false;
+  if (local) {
+    const int k = n0 + __popc(lm & wgm_lanemask_lt());
+    st->start[k] = rec.z;
+    st->cnt[k] = deg;
+    st->val[k] = rec.y;
+    st->col[k] = cw;
+  }
+  __syncwarp();
+  if (lane == 0 && n0 + nloc <= WGM_CA_STACK) st->n = n0 + nloc;
+  __syncwarp();
+  const int np = (deg > 0 && !local) ? (deg + 31) >> 5 : 0;
+  const int incl = wgm_warp_incl_scan(np);
+  const int total = __shfl_sync(WGM_FULL, incl, 31);
+  if (total == 0) return true;
+  int base = 0;
+  if (lane == 31) base = atomicAdd(&q.ctl[1 * WGM_LINE], total);
+  base = __shfl_sync(WGM_FULL, base, 31);
+  if (base + total > q.qcap) return false;
+  const int first = base + incl - np;
+  /* a few pieces per lane, else the whole warp writes one vertex's pieces */
+  if (np <= 4) {
+    for (int k = 0; k < np; k++) {
+      const int slot = first + k;
+      q.q_start[slot] = rec.z + 32 * k;
+      q.q_val[slot] = rec.y;
+      q.q_col[slot] = cw;
+      wgm_st_release_gpu(&q.q_cnt[slot], min(32, deg - 32 * k));
+    }
+  }
+  unsigned big = __ballot_sync(WGM_FULL, np > 4);
+  while (big) {
+    const int j = __ffs(big) - 1;
+    big &= big - 1;
+    const int bz = __shfl_sync(WGM_FULL, rec.z, j), by = __shfl_sync(WGM_FULL, rec.y, j);
+    const int bd = __shfl_sync(WGM_FULL, deg, j), bf = __shfl_sync(WGM_FULL, first, j);
+    const int bc = __shfl_sync(WGM_FULL, cw, j);
+    for (int k = lane; k < (bd + 31) >> 5; k += 32) {
+      q.q_start[bf + k] = bz + 32 * k;
+      q.q_val[bf + k] = by;
+      q.q_col[bf + k] = bc;
+      wgm_st_release_gpu(&q.q_cnt[bf + k], min(32, bd - 32 * k));
+    }
+  }
+  return true;
+}
+
+/* Seeding (between barriers, after the counts): every vertex without a
+ * larger out-neighbour takes colour 1 and is queued; the pieces of every
+ * vertex's in-edges are counted (each vertex is coloured exactly once). */
+__device__ __forceinline__ bool wgm_color_async_seed(const wgm_cta *c, const wgm_color_args &a,
+                                                     const wgm_color_async_args &q,
+                                                     wgm_ca_stack *st) {
+  const wgm_split s(c);
+  const int V = a.V, lane = s.lane;
+  bool ok = true;
+  int pieces = 0;
+  for (int b = s.gw * 32; b < V; b += s.NW * 32) {
+    const int i = b + lane;
+    int4 rec = make_int4(0, 0, 0, 0);
+    bool f = false;
+    if (i < V) {
+      const int t0 = __ldg(&a.trow[i]);
+      rec = make_int4(i, __float_as_int(__ldg(&a.node_value[i])), t0, __ldg(&a.trow[i + 1]) - t0);
+      pieces += (rec.w + 31) >> 5;
+      f = __ldcg(&a.pending[i]) == 0;
+      if (f) a.color[i] = 1;
+    }
+    /* seeds go to the global queue: any warp may take them */
+    if (lane == 0) st->n = WGM_CA_STACK;
+    __syncwarp();
+    ok &= wgm_ca_push(f, rec, 1, q, st);
+    __syncwarp();
+  }
+  if (lane == 0) st->n = 0;
+  for (int o = 16; o > 0; o >>= 1) pieces += __shfl_xor_sync(WGM_FULL, pieces, o);
+  if (lane == 0 && pieces) atomicAdd(&q.ctl[3 * WGM_LINE], pieces);
+  if (lane == 0 && V > 0) atomicMax(&q.ctl[4 * WGM_LINE], 1);
+  return ok;
+}
+
+/* The release loop (no barrier): returns false when a wait gave up or the
+ * queue overflowed. */
+__device__ __forceinline__ bool wgm_color_async_run(const wgm_launch &L, const wgm_color_args &a,
+                                                    const wgm_color_async_args &q,
+                                                    wgm_ca_stack *st) {
+  const int lane = wgm_lane();
+  const int T = __ldcg(&q.ctl[3 * WGM_LINE]);
+  bool ok = true;
+  int cmax_seen = 0;
+  for (;;) {
+    int start = 0, cnt = 0, val = 0, col = 0, have = 0;
+    if (lane == 0) {
+      if (st->n > 0) {
+        const int k = --st->n;
+        start = st->start[k];
+        cnt = st->cnt[k];
+        val = st->val[k];
+        col = st->col[k];
+        have = 1;
+      } else {
+        const int i = atomicAdd(&q.ctl[0], 1);
+        if (i < T && i < q.qcap) {
+          wgm_spin sp = wgm_spin_start(L);
+          for (;;) {
+            cnt = wgm_ld_acquire_gpu(&q.q_cnt[i]);
+            if (cnt >= 0) {
+              have = 1;
+              break;
+            }
+            /* every piece was released elsewhere: slot i stays empty */
+            if ((sp.n & 15u) == 15u && wgm_ld_relaxed_gpu(&q.ctl[2 * WGM_LINE]) >= T) break;
+            if (wgm_spin_giveup(L, sp, WGM_SITE_QUEUE)) {
+              ok = false;
+              break;
+            }
+          }
+          if (have) {
+            start = __ldcg(&q.q_start[i]);
+            val = __ldcg(&q.q_val[i]);
+            col = __ldcg(&q.q_col[i]);
+          }
+        }
+      }
+    }
+    have = __shfl_sync(WGM_FULL, have, 0);
+    if (!have) break;
+    start = __shfl_sync(WGM_FULL, start, 0);
+    cnt = __shfl_sync(WGM_FULL, cnt, 0);
+    val = __shfl_sync(WGM_FULL, val, 0);
+    col = __shfl_sync(WGM_FULL, col, 0);
+    bool ready = false;
+    int4 rec = make_int4(0, 0, 0, 0);
+    int cw = 0;
+    if (lane < cnt) {
+      rec = __ldcg(&q.tcv4[start + lane]); /* written by this launch's init */
+      /* w has the released vertex as a larger out-neighbour */
+      if (__int_as_float(rec.y) < __int_as_float(val)) {
+        atomicMax(&q.cmax[rec.x], col + 1);
+        ready = wgm_atom_add_acqrel_gpu(&a.pending[rec.x], -1) == 1;
+        if (ready) {
+          cw = __ldcg(&q.cmax[rec.x]);
+          a.color[rec.x] = cw;
+          cmax_seen = max(cmax_seen, cw);
+        }
+      }
+    }
+    ok &= wgm_ca_push(ready, rec, cw, q, st);
+    if (lane == 0) wgm_red_add_release_gpu(&q.ctl[2 * WGM_LINE], 1);
+  }
+  for (int o = 16; o > 0; o >>= 1) cmax_seen = max(cmax_seen, __shfl_xor_sync(WGM_FULL, cmax_seen, o));
+  if (lane == 0 && cmax_seen) atomicMax(&q.ctl[4 * WGM_LINE], cmax_seen);
+  return ok;
+}
+
+/* ------------------------------------------------------------------------ */
 /* Pannotia MIS                                                              */
 /* ------------------------------------------------------------------------ */
 

@@ -59,6 +59,12 @@ struct wgm_app {
   /* colour: in-edge CSR when the graph is not symmetric (else the graph) */
   int *d_trow = nullptr, *d_tcol = nullptr;
   int2 *d_tcv = nullptr; /* colour: in-edges beside their neighbour's value */
+  /* colour without rounds (standalone runs, color_mode 1): allocated at the
+   * first such run */
+  int color_mode = 1;
+  int4 *d_tcv4 = nullptr;
+  int *d_cmax = nullptr, *d_cq = nullptr, *d_cqctl = nullptr;
+  int cq_cap = 0;
   int source = 0;
   float damping = 0.85f;
   float dang0 = 0.f;

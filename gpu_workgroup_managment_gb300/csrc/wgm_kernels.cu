@@ -62,6 +62,47 @@ __global__ void __launch_bounds__(1024) wgm_k_mis(wgm_launch L, wgm_mis_args a) 
   WGM_PERSISTENT_EPILOGUE
 }
 
+/* Pannotia colour without rounds (wgm_color_async_run): the counts of
+ * wgm_phase_color between plain barriers, then the release loop, then one
+ * barrier before the round count (the largest colour) is written.  Dynamic
+ * shared memory: one release stack per warp. */
+__global__ void __launch_bounds__(1024) wgm_k_color_async(wgm_launch L, wgm_color_args a,
+                                                          wgm_color_async_args q) {
+  WGM_PERSISTENT_PROLOGUE
+  extern __shared__ wgm_ca_stack wgm_ca_stacks[];
+  wgm_ca_stack *st = &wgm_ca_stacks[threadIdx.x >> 5];
+  bool ok = true;
+  wgm_color_async_init(&c, a, q);
+  if (wgm_barrier(L, &c)) {
+    wgm_step nx;
+    wgm_phase_color(L, &c, a, &sm, wgm_step{3, 0}, &nx); /* larger out-neighbours */
+    if (wgm_barrier(L, &c)) {
+      ok = wgm_color_async_seed(&c, a, q, st);
+      if (wgm_barrier(L, &c)) {
+        ok &= wgm_color_async_run(L, a, q, st);
+        if (!ok && threadIdx.x % 32 == 0) wgm_fail(L, WGM_DEV_OVERFLOW, WGM_SITE_QUEUE, 0);
+        if (wgm_barrier(L, &c) && c.id == 0 && threadIdx.x == 0 && a.rounds_out)
+          *a.rounds_out = __ldcg(&q.ctl[4 * WGM_LINE]);
+      }
+    }
+  }
+  WGM_PERSISTENT_EPILOGUE
+}
+
+size_t wgm_color_async_smem(int block) { return (size_t)(block / 32) * sizeof(wgm_ca_stack); }
+
+cudaError_t wgm_color_async_per_sm(int block, int *per_sm) {
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, wgm_k_color_async, block,
+                                                       wgm_color_async_smem(block));
+}
+
+cudaError_t wgm_launch_color_async(const wgm_launch &L, const wgm_color_args &a,
+                                   const wgm_color_async_args &q, int grid, int block,
+                                   cudaStream_t s) {
+  wgm_k_color_async<<<grid, block, wgm_color_async_smem(block), s>>>(L, a, q);
+  return cudaGetLastError();
+}
+
 /* 40 registers (no spills): six 256-thread CTAs per SM instead of four */
 __global__ void __maxnreg__(40) wgm_k_psssp(wgm_launch L, wgm_psssp_args a) {
   WGM_PERSISTENT_PROLOGUE

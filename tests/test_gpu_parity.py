@@ -116,8 +116,8 @@ def test_star_and_edge_cases(rt):
 
 
 def test_color_default_groups():
-    """Colour on the default group count takes 512 threads per SM (two
-    256-thread CTAs); an explicit count is honoured; the colours are the
+    """Colour in rounds on the default group count takes 512 threads per SM
+    (two 256-thread CTAs); an explicit count is honoured; the colours are the
     oracle's either way."""
     import torch
     sms = torch.cuda.get_device_properties(0).multi_processor_count
@@ -125,7 +125,8 @@ def test_color_default_groups():
     nv = graphs.seeded_node_values(g.num_nodes, 3)
     want = oracle.color(g, nv)
     for tpw, groups in ((256, 2 * sms), (128, 4 * sms), (1024, sms)):
-        with Runtime(threads_per_wg=tpw) as r, PersistentApp(r, "color", g, node_values=nv) as a:
+        with Runtime(threads_per_wg=tpw) as r, \
+                PersistentApp(r, "color", g, node_values=nv, color_mode=0) as a:
             st = a.run()
             assert st.groups == groups, (tpw, st.groups)
             assert np.array_equal(a.result(), want)
@@ -319,6 +320,47 @@ def _drop_edges(g, keep_frac, seed):
     return graphs.Graph(rp, g.col[keep].astype(np.int32))
 
 
+def _star_of_leaves(n):
+    """Vertex 0 joined to n leaves (every leaf has degree 1), plus a path
+    0-n+1-n+2 so the hub also has higher-degree neighbours."""
+    rows = [list(range(1, n + 1)) + [n + 1]] + [[0]] * n + [[0, n + 2], [n + 1]]
+    rp = np.zeros(len(rows) + 1, np.int32)
+    rp[1:] = np.cumsum([len(r) for r in rows])
+    return graphs.Graph(rp, np.array([c for r in rows for c in r], np.int32))
+
+
+@pytest.mark.parametrize("which", ["rmat", "grid", "star", "directed", "hubs"])
+def test_color_without_rounds(which):
+    """Colour without rounds (the standalone default) against the oracle and
+    against the round form: same colours, same round count (the largest
+    colour), on a small graph count, a high-diameter grid, degree-1 leaves
+    (color.cl:46), a directed subgraph and a low hub threshold."""
+    cfg = {}
+    if which == "rmat":
+        g = graphs.rmat(14, 16, seed=31)
+    elif which == "grid":
+        g = graphs.grid(90, 70)
+    elif which == "star":
+        g = _star_of_leaves(3000)
+    elif which == "directed":
+        g = _drop_edges(graphs.rmat(12, 8, seed=8), 0.6, 9)
+    else:
+        g = graphs.rmat(12, 16, seed=4)
+        cfg = dict(hub_threshold=8)
+    nv = graphs.seeded_node_values(g.num_nodes, 23)
+    want = oracle.color(g, nv)
+    with Runtime(**cfg) as r:
+        with PersistentApp(r, "color", g, node_values=nv, color_mode=1) as a:
+            s1 = [a.run(), a.run(13)]
+            c1 = a.result()
+        with PersistentApp(r, "color", g, node_values=nv, color_mode=0) as a:
+            s0 = a.run()
+            c0 = a.result()
+    assert np.array_equal(c1, want) and np.array_equal(c0, want)
+    assert all(s.rounds == s0.rounds == int(want.max()) for s in s1)
+    assert s1[1].groups == 13
+
+
 @pytest.mark.parametrize("kind", ["symmetric", "directed", "unsorted"])
 def test_color_graph_shapes(kind):
     """Colour on a symmetric RMAT with hubs, on a directed subgraph (the
@@ -337,6 +379,8 @@ def test_color_graph_shapes(kind):
         g = graphs.Graph(g.row_ptr, col)
     nv = graphs.seeded_node_values(g.num_nodes, 17)
     for cfg in (dict(), dict(hub_threshold=16)):
-        with Runtime(**cfg) as r, PersistentApp(r, "color", g, node_values=nv) as a:
-            a.run()
-            assert np.array_equal(a.result(), oracle.color(g, nv)), (kind, cfg)
+        for mode in (0, 1):
+            with Runtime(**cfg) as r, \
+                    PersistentApp(r, "color", g, node_values=nv, color_mode=mode) as a:
+                a.run()
+                assert np.array_equal(a.result(), oracle.color(g, nv)), (kind, cfg, mode)
