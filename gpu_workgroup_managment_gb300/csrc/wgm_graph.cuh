@@ -879,15 +879,18 @@ static __device__ int wgm_phase_color(const wgm_launch &Lc, wgm_cta *c, const wg
  * colour + 1 and takes one off pending[w] with an acq_rel atomic; the lane
  * that takes the last one (it reads every raise of cmax[w], ordered before
  * the other decrements) colours w with cmax[w] and queues w's in-edges.  A
- * vertex of at most 32 in-edges goes to its warp's own stack in shared
- * memory and is released by that warp next, so a chain of colours costs
- * about two L2 round trips per link instead of a grid barrier per round;
- * larger ones go to the global queue in pieces.  Degree-1 vertices start at
+ * vertex of at most WGM_CA_LOCAL_MAX in-edges goes to its warp's own stack
+ * in shared memory and is released by that warp next, 32 edges a step, so
+ * a chain of colours costs about two L2 round trips per link instead of a
+ * grid barrier per round; larger ones go to the global queue in pieces.  Degree-1 vertices start at
  * pending 0 (coloured 1) and releases only take them below 0, so they are
  * never coloured again - the reference's quirk (color.cl:46).  Colours are
  * the round-based form's, bit for bit; the run reports the largest colour
  * as its round count. */
 #define WGM_CA_STACK 64
+/* vertices of at most this many in-edges stay on their warp's stack (released
+ * 32 edges per step); larger ones go to the global queue in pieces */
+#define WGM_CA_LOCAL_MAX 1024
 struct wgm_color_async_args {
   int4 *tcv4;   /* [in-edges] {in-neighbour w, bits of w's value, w's first
                    in-edge, w's in-degree} */
@@ -933,7 +936,7 @@ __device__ __forceinline__ bool wgm_ca_push(bool flag, int4 rec, int cw,
                                             const wgm_color_async_args &q, wgm_ca_stack *st) {
   const int lane = wgm_lane();
   const int deg = flag ? rec.w : 0;
-  bool local = deg > 0 && deg <= 32;
+  bool local = deg > 0 && deg <= WGM_CA_LOCAL_MAX;
   const unsigned lm = __ballot_sync(WGM_FULL, local);
   const int nloc = __popc(lm);
   int n0 = 0;
@@ -1029,17 +1032,28 @@ __device__ __forceinline__ bool wgm_color_async_run(const wgm_launch &L, const w
   const int T = __ldcg(&q.ctl[3 * WGM_LINE]);
   bool ok = true;
   int cmax_seen = 0;
+  int mydone = 0; /* 32-edge steps released by this warp, not yet counted */
   for (;;) {
     int start = 0, cnt = 0, val = 0, col = 0, have = 0;
     if (lane == 0) {
       if (st->n > 0) {
-        const int k = --st->n;
+        const int k = st->n - 1;
         start = st->start[k];
         cnt = st->cnt[k];
         val = st->val[k];
         col = st->col[k];
         have = 1;
+        if (cnt > 32) { /* the rest of its in-edges stays on the stack */
+          st->start[k] = start + 32;
+          st->cnt[k] = cnt - 32;
+          cnt = 32;
+        } else {
+          st->n = k;
+        }
       } else {
+        /* the steps this warp released count before it waits */
+        if (mydone) wgm_red_add_release_gpu(&q.ctl[2 * WGM_LINE], mydone);
+        mydone = 0;
         const int i = atomicAdd(&q.ctl[0], 1);
         if (i < T && i < q.qcap) {
           wgm_spin sp = wgm_spin_start(L);
@@ -1050,11 +1064,13 @@ __device__ __forceinline__ bool wgm_color_async_run(const wgm_launch &L, const w
               break;
             }
             /* every piece was released elsewhere: slot i stays empty */
-            if ((sp.n & 15u) == 15u && wgm_ld_relaxed_gpu(&q.ctl[2 * WGM_LINE]) >= T) break;
+            if ((sp.n & 7u) == 7u && wgm_ld_relaxed_gpu(&q.ctl[2 * WGM_LINE]) >= T) break;
             if (wgm_spin_giveup(L, sp, WGM_SITE_QUEUE)) {
               ok = false;
               break;
             }
+            /* a waiting warp polls gently: the releasing ones need the L2 */
+            if (sp.n > 4) __nanosleep(100);
           }
           if (have) {
             start = __ldcg(&q.q_start[i]);
@@ -1087,8 +1103,9 @@ __device__ __forceinline__ bool wgm_color_async_run(const wgm_launch &L, const w
       }
     }
     ok &= wgm_ca_push(ready, rec, cw, q, st);
-    if (lane == 0) wgm_red_add_release_gpu(&q.ctl[2 * WGM_LINE], 1);
+    mydone++;
   }
+  if (lane == 0 && mydone) wgm_red_add_release_gpu(&q.ctl[2 * WGM_LINE], mydone);
   for (int o = 16; o > 0; o >>= 1) cmax_seen = max(cmax_seen, __shfl_xor_sync(WGM_FULL, cmax_seen, o));
   if (lane == 0 && cmax_seen) atomicMax(&q.ctl[4 * WGM_LINE], cmax_seen);
   return ok;
