@@ -879,18 +879,25 @@ static __device__ int wgm_phase_color(const wgm_launch &Lc, wgm_cta *c, const wg
  * colour + 1 and takes one off pending[w] with an acq_rel atomic; the lane
  * that takes the last one (it reads every raise of cmax[w], ordered before
  * the other decrements) colours w with cmax[w] and queues w's in-edges.  A
- * vertex of at most WGM_CA_LOCAL_MAX in-edges goes to its warp's own stack
- * in shared memory and is released by that warp next, 32 edges a step, so
- * a chain of colours costs about two L2 round trips per link instead of a
- * grid barrier per round; larger ones go to the global queue in pieces.  Degree-1 vertices start at
+ * vertex of at most 32 in-edges goes to its warp's own stack in shared
+ * memory and is released by that warp next; larger ones go to the global
+ * queue in pieces.  Measured against the round form it loses: on RMAT-20
+ * 16 ms against 8.3 ms (1629 colours, ~10 us per link of the longest chain
+ * against ~5 us per round), because that chain runs through high-degree
+ * vertices whose releases pass the global queue (a reservation, the piece
+ * written and seen, its fields read) where a round spreads them over every
+ * warp behind one barrier.  So rounds stay the default.  Degree-1 vertices start at
  * pending 0 (coloured 1) and releases only take them below 0, so they are
  * never coloured again - the reference's quirk (color.cl:46).  Colours are
  * the round-based form's, bit for bit; the run reports the largest colour
  * as its round count. */
 #define WGM_CA_STACK 64
-/* vertices of at most this many in-edges stay on their warp's stack (released
- * 32 edges per step); larger ones go to the global queue in pieces */
-#define WGM_CA_LOCAL_MAX 1024
+/* vertices of at most this many in-edges stay on their warp's stack;
+ * larger ones go to the global queue in pieces.  Keeping up to 1024 on the
+ * stack (32 edges a step) made RMAT-20 5x slower: the longest colour chains
+ * run through high-degree vertices, whose releases must spread over many
+ * warps at once. */
+#define WGM_CA_LOCAL_MAX 32
 struct wgm_color_async_args {
   int4 *tcv4;   /* [in-edges] {in-neighbour w, bits of w's value, w's first
                    in-edge, w's in-degree} */

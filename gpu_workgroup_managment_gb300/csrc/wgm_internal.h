@@ -61,7 +61,7 @@ struct wgm_app {
   int2 *d_tcv = nullptr; /* colour: in-edges beside their neighbour's value */
   /* colour without rounds (standalone runs, color_mode 1): allocated at the
    * first such run */
-  int color_mode = 1;
+  int color_mode = 0;
   int4 *d_tcv4 = nullptr;
   int *d_cmax = nullptr, *d_cq = nullptr, *d_cqctl = nullptr;
   int cq_cap = 0;

@@ -170,11 +170,12 @@ int wgm_app_set_source(wgm_app *app, int32_t source);
 int wgm_app_set_node_values(wgm_app *app, const float *node_value);
 int wgm_app_set_pagerank(wgm_app *app, float damping, int iterations);
 /* How a standalone Pannotia colour run proceeds (no reference counterpart):
- * 1 (the default) without rounds - a vertex is coloured as soon as its last
- * larger out-neighbour is, the warp that colours it releasing its smaller
- * neighbours next; 0 a grid barrier per round (color.cl's structure; the
- * megakernel and the served form always run rounds, where they resize).
- * Same colours, same round count (the largest colour). */
+ * 0 (the default) a grid barrier per round (color.cl's structure; the
+ * megakernel and the served form always run rounds, where they resize);
+ * 1 without rounds - a vertex is coloured as soon as its last larger
+ * out-neighbour is, the warp that colours it releasing its smaller
+ * neighbours next (slower on RMAT graphs: 16 ms against 8.3 ms at scale
+ * 20).  Same colours, same round count (the largest colour). */
 int wgm_app_set_color_mode(wgm_app *app, int32_t mode);
 /* Betweenness centrality from sources 0 .. num_sources-1 (bc.cl:160-235
  * loops over every vertex; a smaller count bounds the run on big graphs). */
