@@ -331,7 +331,7 @@ def _star_of_leaves(n):
 
 @pytest.mark.parametrize("which", ["rmat", "grid", "star", "directed", "hubs"])
 def test_color_without_rounds(which):
-    """Colour without rounds (the standalone default) against the oracle and
+    """Colour without rounds (the option of standalone runs) against the oracle and
     against the round form: same colours, same round count (the largest
     colour), on a small graph count, a high-diameter grid, degree-1 leaves
     (color.cl:46), a directed subgraph and a low hub threshold."""
