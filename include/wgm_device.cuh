@@ -564,6 +564,13 @@ __device__ __forceinline__ bool wgm_barrier(const wgm_launch &L, wgm_cta *c) {
     wgm_fail(L, WGM_DEV_ABORTED, WGM_SITE_BARRIER, c->id);
     c->ok = 0;
   }
+  /* one group: a CTA barrier is the whole barrier (its threads see each
+   * other's global writes after it); no L2 round trip.  Its own failures
+   * and the host abort above clear c->ok. */
+  if (c->ngroups == 1) {
+    __syncthreads();
+    return c->ok;
+  }
   switch (L.barrier_kind) {
     case WGM_BARRIER_XF:
       return wgm_barrier_xf(L, c, c->ngroups);
