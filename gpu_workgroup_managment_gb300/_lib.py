@@ -101,6 +101,7 @@ _PROTOS = {
                                        C.POINTER(C.c_double), C.POINTER(_I)]),
     "wgm_serve_groups_trace": (_I, [_P, _P, _P, C.c_int64, C.POINTER(C.c_int64)]),
     "wgm_app_set_color_mode": (_I, [_P, C.c_int32]),
+    "wgm_app_set_bfs_mode": (_I, [_P, C.c_int32]),
     "wgm_profiler_start": (_I, [_P]),
     "wgm_profiler_stop": (_I, [_P]),
     "wgm_app_check": (_I, [_P, C.POINTER(_I)]),

@@ -428,6 +428,43 @@ static int wgm_bc_cta_launch(wgm_runtime *rt, wgm_app *a, cudaStream_t s) {
   return WGM_OK;
 }
 
+/* Lonestar BFS on one CTA (wgm_bfs_cta): chosen by default for graphs of
+ * at most WGM_BFS_CTA_AUTO_V vertices and average degree at most 8, whose
+ * levels carry little work each; possible up to WGM_BFS_CTA_MAX_V vertices
+ * (the visited bits in shared memory). */
+#define WGM_BFS_CTA_AUTO_V 65536
+#define WGM_BFS_CTA_MAX_V (1 << 20)
+static bool wgm_bfs_cta_on(const wgm_app *a) {
+  if (a->kind != WGM_APP_LONESTAR_BFS || a->V > WGM_BFS_CTA_MAX_V) return false;
+  if (a->bfs_mode >= 0) return a->bfs_mode == 1;
+  return a->V <= WGM_BFS_CTA_AUTO_V && a->E <= 8LL * a->V;
+}
+
+static int wgm_bfs_cta_launch(wgm_runtime *rt, wgm_app *a, cudaStream_t s) {
+  wgm_mega_args A;
+  std::memset(&A, 0, sizeof(A));
+  int st = wgm_app_fill_mega(a, &A);
+  if (st) return st;
+  /* the frontier buffers take what shared memory the visited bits leave */
+  const long long avail = (long long)rt->prop.sharedMemPerBlockOptin - 1024 -
+                          (long long)((a->V + 31) / 32) * 4;
+  const int F = (int)std::min<long long>(1 << 16, avail / 8);
+  if (F < 256) return WGM_ERR_INVALID;
+  if (rt->cfg.host_handshake) return WGM_ERR_INVALID; /* no discovery, no handshake */
+  cudaError_t e = wgm_launch_bfs_cta(A.ls, a->d_wl_start, a->wl_cap, F, &rt->hf_dev->status,
+                                     1024, s);
+  if (e != cudaSuccess) return wgm_cuda_fail(rt, e);
+  return WGM_OK;
+}
+
+extern "C" int wgm_app_set_bfs_mode(wgm_app *a, int32_t mode) {
+  if (!a || a->kind != WGM_APP_LONESTAR_BFS || mode < -1 || mode > 1 ||
+      (mode == 1 && a->V > WGM_BFS_CTA_MAX_V))
+    return WGM_ERR_INVALID;
+  a->bfs_mode = mode;
+  return WGM_OK;
+}
+
 extern "C" int wgm_app_set_bc_sources(wgm_app *a, int32_t num_sources) {
   if (!a || a->kind != WGM_APP_PANNOTIA_BC || num_sources < 0 || num_sources > a->V)
     return WGM_ERR_INVALID;
@@ -750,6 +787,8 @@ extern "C" int wgm_launch_persistent(wgm_runtime *rt, wgm_app *a, int num_wgs, v
   cudaSetDevice(rt->device);
   if (a->kind == WGM_APP_PANNOTIA_BC && a->bc_mode == 1)
     return wgm_bc_cta_launch(rt, a, stream ? (cudaStream_t)stream : rt->stream);
+  if (wgm_bfs_cta_on(a) && num_wgs <= 1 && !rt->cfg.host_handshake)
+    return wgm_bfs_cta_launch(rt, a, stream ? (cudaStream_t)stream : rt->stream);
   int block = wgm_block_size(rt), grid = 0;
   int s = wgm_pick_grid(a, num_wgs, block, &grid);
   if (s) return s;
@@ -767,17 +806,23 @@ extern "C" int wgm_run_persistent(wgm_runtime *rt, wgm_app *a, int num_wgs,
                                   wgm_run_stats *stats) {
   if (!rt || !a || a->rt != rt) return WGM_ERR_INVALID;
   cudaSetDevice(rt->device);
-  if (a->kind == WGM_APP_PANNOTIA_BC && a->bc_mode == 1) {
+  const bool bfs_cta = wgm_bfs_cta_on(a) && num_wgs <= 1 && !rt->cfg.host_handshake;
+  if ((a->kind == WGM_APP_PANNOTIA_BC && a->bc_mode == 1) || bfs_cta) {
     cudaError_t e = cudaEventRecord(rt->ev0, rt->stream);
     if (e != cudaSuccess) return wgm_cuda_fail(rt, e);
-    int s = wgm_bc_cta_launch(rt, a, rt->stream);
+    int s = bfs_cta ? wgm_bfs_cta_launch(rt, a, rt->stream) : wgm_bc_cta_launch(rt, a, rt->stream);
     if (s) return s;
     e = cudaEventRecord(rt->ev1, rt->stream);
     if (e != cudaSuccess) return wgm_cuda_fail(rt, e);
     s = wgm_stream_wait(rt, rt->stream);
     if (s) return s;
+    if (bfs_cta) { /* a frontier past every buffer reports an overflow */
+      s = wgm_finish_launch(rt, nullptr, nullptr);
+      if (s) return s;
+    }
     if (stats) {
       std::memset(stats, 0, sizeof(*stats));
+      stats->groups = bfs_cta ? 1 : 0;
       float ms = 0.f;
       cudaEventElapsedTime(&ms, rt->ev0, rt->ev1);
       stats->kernel_ms = ms;

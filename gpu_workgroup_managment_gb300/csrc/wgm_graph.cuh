@@ -496,6 +496,81 @@ __device__ __forceinline__ bool wgm_ls_level(const wgm_launch &Lc, wgm_cta *c,
   return ok;
 }
 
+/* Lonestar BFS on one CTA (standalone runs of small graphs, bfs_mode 1).
+ * A level of a high-diameter graph carries a few hundred vertices, and the
+ * grid form pays a chain of dependent L2 round trips per level (counter,
+ * worklist pieces, columns, the claiming CAS, the pushed rows, the barrier):
+ * ~4 us on the 256x256 grid whether 1 or 152 CTAs run it.  Here the whole
+ * traversal lives in one CTA: visited bits in shared memory, claimed with a
+ * shared-memory atomicOr; the frontier in shared memory (vertices past its
+ * capacity spill to global memory); level counters triple-buffered in shared
+ * memory, so a level is one __syncthreads and two global round trips (row
+ * pointers, then columns).  Same levels as the Lonestar kernel: the source
+ * is level 0, a vertex first reached while level L runs gets L, out-of-range
+ * columns are skipped (bfs.cl:116), the loader quirk's negative last degree
+ * walks nothing, and the level count is the first level with an empty
+ * frontier. */
+struct wgm_bfs_cta_smem {
+  unsigned *bits; /* [ceil(V/32)] visited */
+  int *front;     /* [2][F] frontier buffers */
+  int F;
+};
+
+__device__ __forceinline__ void wgm_bfs_cta(const wgm_lonestar_args &a, int *spill, int spill_cap,
+                                            const wgm_bfs_cta_smem &S, int *s_cnt) {
+  const int V = a.V, nw = (V + 31) >> 5;
+  for (int i = threadIdx.x; i < nw; i += blockDim.x) S.bits[i] = 0u;
+  for (int i = threadIdx.x; i < V; i += blockDim.x)
+    a.dist[i] = (i == a.source) ? 0u : WGM_LONESTAR_INF;
+  if (threadIdx.x == 0) {
+    s_cnt[0] = 0;
+    s_cnt[1] = 1;
+    s_cnt[2] = 0;
+    s_cnt[3] = 0; /* overflow */
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    S.bits[a.source >> 5] = 1u << (a.source & 31);
+    S.front[S.F] = a.source; /* level 1 reads buffer 1 */
+  }
+  __syncthreads();
+  int L = 1;
+  for (;;) {
+    const int n = s_cnt[L % 3];
+    if (n == 0) break;
+    if (L > V + 1) break;
+    const int *in = S.front + (size_t)(L & 1) * S.F;
+    int *out = S.front + (size_t)((L + 1) & 1) * S.F;
+    const int *in_sp = spill + (size_t)(L & 1) * spill_cap;
+    int *out_sp = spill + (size_t)((L + 1) & 1) * spill_cap;
+    int *oc = &s_cnt[(L + 1) % 3];
+    if (threadIdx.x == 0) s_cnt[(L + 2) % 3] = 0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      const int v = i < S.F ? in[i] : __ldcg(&in_sp[i - S.F]);
+      const int s = __ldg(&a.row[v]);
+      const int e = s + max(__ldg(&a.row[v + 1]) - s, 0);
+      for (int j = s; j < e; j++) {
+        const int u = __ldg(&a.col[j]);
+        if ((unsigned)u >= (unsigned)V) continue;
+        const unsigned bit = 1u << (u & 31);
+        if (S.bits[u >> 5] & bit) continue;
+        if (atomicOr(&S.bits[u >> 5], bit) & bit) continue;
+        a.dist[u] = (unsigned)L;
+        const int k = atomicAdd(oc, 1);
+        if (k < S.F)
+          out[k] = u;
+        else if (k - S.F < spill_cap)
+          out_sp[k - S.F] = u;
+        else
+          s_cnt[3] = 1;
+      }
+    }
+    __syncthreads();
+    L++;
+  }
+  if (threadIdx.x == 0 && a.levels_out) *a.levels_out = L;
+}
+
 /* Persistent BFS/SSSP phases: (0) device-side init; (1,L) level L.  One
  * barrier per level (the reference uses two, bfs.cl:282,295): the piece
  * counters are triple-buffered by level, so the counter a level fills was

@@ -62,6 +62,7 @@ struct wgm_app {
   /* colour without rounds (standalone runs, color_mode 1): allocated at the
    * first such run */
   int color_mode = 0;
+  int bfs_mode = -1; /* Lonestar BFS: -1 automatic, 0 grid, 1 one CTA */
   int4 *d_tcv4 = nullptr;
   int *d_cmax = nullptr, *d_cq = nullptr, *d_cqctl = nullptr;
   int cq_cap = 0;

@@ -103,6 +103,35 @@ cudaError_t wgm_launch_color_async(const wgm_launch &L, const wgm_color_args &a,
   return cudaGetLastError();
 }
 
+/* Lonestar BFS on one CTA (wgm_bfs_cta): a plain one-CTA launch, no
+ * discovery and no grid barrier.  Dynamic shared memory: the visited bits,
+ * then the two frontier buffers of F vertices each. */
+__global__ void __launch_bounds__(1024) wgm_k_bfs_cta(wgm_lonestar_args a, int *spill,
+                                                      int spill_cap, int F, int *status) {
+  extern __shared__ unsigned wgm_bfs_cta_dyn[];
+  __shared__ int s_cnt[4];
+  wgm_bfs_cta_smem S;
+  S.bits = wgm_bfs_cta_dyn;
+  S.front = reinterpret_cast<int *>(wgm_bfs_cta_dyn + ((a.V + 31) >> 5));
+  S.F = F;
+  wgm_bfs_cta(a, spill, spill_cap, S, s_cnt);
+  if (threadIdx.x == 0 && s_cnt[3] && status) *status = WGM_DEV_OVERFLOW;
+}
+
+size_t wgm_bfs_cta_smem_bytes(int V, int F) {
+  return (size_t)((V + 31) / 32) * 4 + (size_t)2 * F * 4;
+}
+
+cudaError_t wgm_launch_bfs_cta(const wgm_lonestar_args &a, int *spill, int spill_cap, int F,
+                               int *status, int block, cudaStream_t s) {
+  const size_t smem = wgm_bfs_cta_smem_bytes(a.V, F);
+  cudaError_t e = cudaFuncSetAttribute(wgm_k_bfs_cta, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return e;
+  wgm_k_bfs_cta<<<1, block, smem, s>>>(a, spill, spill_cap, F, status);
+  return cudaGetLastError();
+}
+
 /* 40 registers (no spills): six 256-thread CTAs per SM instead of four */
 __global__ void __maxnreg__(40) wgm_k_psssp(wgm_launch L, wgm_psssp_args a) {
   WGM_PERSISTENT_PROLOGUE

@@ -45,6 +45,9 @@ cudaError_t wgm_launch_color(const wgm_launch &L, const wgm_color_args &a, int g
                              cudaStream_t s);
 cudaError_t wgm_launch_mis(const wgm_launch &L, const wgm_mis_args &a, int grid, int block,
                            cudaStream_t s);
+size_t wgm_bfs_cta_smem_bytes(int V, int F);
+cudaError_t wgm_launch_bfs_cta(const wgm_lonestar_args &a, int *spill, int spill_cap, int F,
+                               int *status, int block, cudaStream_t s);
 size_t wgm_color_async_smem(int block);
 cudaError_t wgm_color_async_per_sm(int block, int *per_sm);
 cudaError_t wgm_launch_color_async(const wgm_launch &L, const wgm_color_args &a,

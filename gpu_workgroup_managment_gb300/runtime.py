@@ -181,7 +181,8 @@ class PersistentApp:
     def __init__(self, rt: Runtime, app: str | int, graph: Graph, source: int = 0,
                  node_values: np.ndarray | None = None, damping: float = 0.85,
                  iterations: int = 20, bc_sources: int | None = None,
-                 bc_mode: int | None = None, color_mode: int | None = None):
+                 bc_mode: int | None = None, color_mode: int | None = None,
+                 bfs_mode: int | None = None):
         self.rt = rt
         self.kind = APPS[app] if isinstance(app, str) else app
         self.graph = graph
@@ -202,6 +203,8 @@ class PersistentApp:
             check(lib.wgm_app_set_bc_mode(self._h, bc_mode))
         if self.kind == L.APP_PANNOTIA_COLOR and color_mode is not None:
             check(lib.wgm_app_set_color_mode(self._h, color_mode))
+        if self.kind == L.APP_LONESTAR_BFS and bfs_mode is not None:
+            check(lib.wgm_app_set_bfs_mode(self._h, bfs_mode))
 
     @property
     def name(self) -> str:

@@ -177,6 +177,15 @@ int wgm_app_set_pagerank(wgm_app *app, float damping, int iterations);
  * neighbours next (slower on RMAT graphs: 16 ms against 8.3 ms at scale
  * 20).  Same colours, same round count (the largest colour). */
 int wgm_app_set_color_mode(wgm_app *app, int32_t mode);
+/* How a standalone Lonestar BFS run proceeds (no reference counterpart):
+ * 0 the reference's shape - discovered groups, a grid barrier per level;
+ * 1 one CTA, the visited set and the frontier in shared memory and
+ * __syncthreads as the level barrier (graphs of at most 2^20 vertices);
+ * -1 (the default) 1 for graphs of at most 65,536 vertices and average
+ * degree at most 8 when num_wgs <= 1 and without the host handshake, else
+ * 0.  An explicit num_wgs > 1 always runs the grid form.  Same levels, same
+ * level count.  The megakernel always runs the grid form. */
+int wgm_app_set_bfs_mode(wgm_app *app, int32_t mode);
 /* Betweenness centrality from sources 0 .. num_sources-1 (bc.cl:160-235
  * loops over every vertex; a smaller count bounds the run on big graphs). */
 int wgm_app_set_bc_sources(wgm_app *app, int32_t num_sources);

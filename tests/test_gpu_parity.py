@@ -156,7 +156,9 @@ def test_lonestar_default_groups():
                     assert np.array_equal(a.result(), want), app
                     full = a.run(1 << 20).groups
                     assert np.array_equal(a.result(), want), app
-                    assert st.groups == (sms if small else full), (app, st.groups, full)
+                    # the small grid's BFS runs on one CTA (bfs_mode -1 picks it)
+                    expect = (1 if app == "lonestar_bfs" else sms) if small else full
+                    assert st.groups == expect, (app, st.groups, full)
         # Pannotia SSSP: 1024 threads per SM on the grid
         with PersistentApp(r, "sssp", gg, source=0) as a:
             st = a.run()
@@ -203,6 +205,52 @@ def test_repeated_runs_and_reupload(rt):
             a.upload(graphs.lonestar_view(h))
             a.run()
             assert np.array_equal(a.result(), oracle.lonestar_bfs(graphs.lonestar_view(h), 3))
+
+
+@pytest.mark.parametrize("which", ["grid", "lonestar_grid", "rmat", "star", "isolated",
+                                   "path"])
+def test_bfs_one_cta(which):
+    """Lonestar BFS on one CTA against the oracle and the grid form: same
+    levels, same level count, on grids (with the loader's last-edge quirk),
+    a small RMAT graph with hubs, a star of degree-1 leaves, an isolated
+    source and a long path whose frontier is one vertex for 20,000 levels;
+    the automatic mode picks one CTA only for small sparse graphs."""
+    src = 0
+    if which == "grid":
+        g = graphs.grid(120, 200)
+    elif which == "lonestar_grid":
+        g = graphs.lonestar_view(graphs.grid(256, 256))
+    elif which == "rmat":
+        g = graphs.rmat(13, 16, seed=6)
+        src = graphs.max_degree_vertex(g)
+    elif which == "star":
+        g = _star_of_leaves(5000)
+        src = 17
+    elif which == "isolated":
+        g = graphs.rmat(10, 4, seed=3)
+        src = int(np.flatnonzero(g.degrees() == 0)[0])
+    else:
+        V = 20000
+        rp = np.concatenate([[0, 1], np.arange(3, 2 * V - 1, 2), [2 * V - 2]]).astype(np.int32)
+        col = np.empty(2 * V - 2, np.int32)
+        col[0] = 1
+        for v in range(1, V - 1):
+            col[rp[v]], col[rp[v] + 1] = v - 1, v + 1
+        col[-1] = V - 2
+        g = graphs.Graph(rp, col)
+    want = oracle.lonestar_bfs(g, src)
+    with Runtime() as r:
+        out = {}
+        for mode in (-1, 0, 1):
+            with PersistentApp(r, "lonestar_bfs", g, source=src, bfs_mode=mode) as a:
+                st = a.run()
+                out[mode] = (a.result(), st.rounds, st.groups)
+        assert np.array_equal(out[1][0], want) and np.array_equal(out[0][0], want)
+        assert np.array_equal(out[-1][0], want)
+        assert out[1][1] == out[0][1] == out[-1][1]
+        assert out[1][2] == 1 and out[0][2] > 1
+        sparse_small = g.num_nodes <= 65536 and g.num_edges <= 8 * g.num_nodes
+        assert (out[-1][2] == 1) == sparse_small
 
 
 def test_c1_grid_256_bfs_full_size(rt):
