@@ -291,16 +291,25 @@ def _best(app, k: int = 5):
 
 def _c1(rt, barrier_ns) -> dict:
     """C1: plain persistent BFS on the 256x256 4-neighbour grid from vertex 0
-    (Lonestar view), one launch per run, CUDA events, best of 5.  Bytes_alg
+    (Lonestar view), one launch per run, CUDA events, best of 5; the grid
+    form (discovered groups, a grid barrier per level) and, beside it, the
+    one-CTA form.  Bytes_alg
     = 8 E_t + 20 V_r; ns per level and the barrier's share of it.  CPU
     baseline: the oracle's level-synchronous restatement of bfs.cl on every
     host core and on one."""
     from gpu_workgroup_managment_gb300 import PersistentApp, graphs
     from oracle import oracle
     g = graphs.lonestar_view(graphs.grid(256, 256))
-    with PersistentApp(rt, "lonestar_bfs", g) as a:
+    # the configuration as defined: discovered groups, a grid barrier per level
+    with PersistentApp(rt, "lonestar_bfs", g, bfs_mode=0) as a:
         st = _best(a)
         d = a.result()
+    # the same BFS on one CTA (the default for a graph this small and sparse)
+    with PersistentApp(rt, "lonestar_bfs", g, bfs_mode=1) as a:
+        st1 = _best(a)
+        d1 = a.result()
+    if not np.array_equal(d1, d) or st1.rounds != st.rounds:
+        raise SystemExit("C1 BFS on one CTA differs from the grid form")
     reached = d != INF
     et, vr = int(np.diff(g.row_ptr)[reached].clip(min=0).sum()), int(reached.sum())
     peak, kind = _peak_hbm()
@@ -316,7 +325,9 @@ def _c1(rt, barrier_ns) -> dict:
            "frac_of_" + kind: (8 * et + 20 * vr) / s / 1e9 / peak,
            "cpu_baseline": {"ms": t_omp * 1e3, "gteps": et / t_omp / 1e9,
                             "cores": oracle.threads(), "ms_1core": t_one * 1e3,
-                            "kind": "port", "sample": "the whole BFS, best of 3"}}
+                            "kind": "port", "sample": "the whole BFS, best of 3"},
+           "one_cta": {"ms": st1.kernel_ms, "ns_per_level": st1.kernel_ms * 1e6 / max(st1.rounds, 1),
+                       "gteps": et / (st1.kernel_ms * 1e-3) / 1e9}}
     if barrier_ns:
         out["barrier_share"] = barrier_ns * st.rounds / (st.kernel_ms * 1e6)
     return out
@@ -515,7 +526,9 @@ def _summary(ex: dict) -> dict:
                          "ctas_1024t": ex.get("barrier_ctas_1024_threads")}
     c1 = ex.get("c1_bfs_grid256", {})
     out["c1"] = {"ms": _r(c1.get("ms")), "ns_per_level": _r(c1.get("ns_per_level")),
-                 "cpu_ms": _r(c1.get("cpu_baseline", {}).get("ms"))}
+                 "one_cta_ms": _r(c1.get("one_cta", {}).get("ms")),
+                 "cpu_ms": _r(c1.get("cpu_baseline", {}).get("ms")),
+                 "cpu_1core_ms": _r(c1.get("cpu_baseline", {}).get("ms_1core"))}
     c2 = ex.get("c2_rmat20", {})
     out["c2"] = {k: {"ms": _r(c2.get(k, {}).get("ms")), "cpu_ms": _r(c2.get(k, {}).get("cpu_ms"))}
                  for k in ("lonestar_sssp", "color", "mis")}

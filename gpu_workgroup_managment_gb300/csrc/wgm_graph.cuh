@@ -508,8 +508,8 @@ __device__ __forceinline__ bool wgm_ls_level(const wgm_launch &Lc, wgm_cta *c,
  * pointers, then columns).  Same levels as the Lonestar kernel: the source
  * is level 0, a vertex first reached while level L runs gets L, out-of-range
  * columns are skipped (bfs.cl:116), the loader quirk's negative last degree
- * walks nothing, and the level count is the first level with an empty
- * frontier. */
+ * walks nothing, and the level count is the first level whose frontier
+ * walks no edge (the grid form never queues a vertex without edges). */
 struct wgm_bfs_cta_smem {
   unsigned *bits; /* [ceil(V/32)] visited */
   int *front;     /* [2][F] frontier buffers */
@@ -527,6 +527,7 @@ __device__ __forceinline__ void wgm_bfs_cta(const wgm_lonestar_args &a, int *spi
     s_cnt[1] = 1;
     s_cnt[2] = 0;
     s_cnt[3] = 0; /* overflow */
+    for (int k = 4; k < 7; k++) s_cnt[k] = 0; /* the level walked an edge, by L mod 3 */
   }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -544,11 +545,15 @@ __device__ __forceinline__ void wgm_bfs_cta(const wgm_lonestar_args &a, int *spi
     const int *in_sp = spill + (size_t)(L & 1) * spill_cap;
     int *out_sp = spill + (size_t)((L + 1) & 1) * spill_cap;
     int *oc = &s_cnt[(L + 1) % 3];
-    if (threadIdx.x == 0) s_cnt[(L + 2) % 3] = 0;
+    if (threadIdx.x == 0) {
+      s_cnt[(L + 2) % 3] = 0;
+      s_cnt[4 + (L + 2) % 3] = 0;
+    }
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
       const int v = i < S.F ? in[i] : __ldcg(&in_sp[i - S.F]);
       const int s = __ldg(&a.row[v]);
       const int e = s + max(__ldg(&a.row[v + 1]) - s, 0);
+      if (e > s) s_cnt[4 + L % 3] = 1;
       for (int j = s; j < e; j++) {
         const int u = __ldg(&a.col[j]);
         if ((unsigned)u >= (unsigned)V) continue;
@@ -566,6 +571,9 @@ __device__ __forceinline__ void wgm_bfs_cta(const wgm_lonestar_args &a, int *spi
       }
     }
     __syncthreads();
+    /* the grid form queues no vertex without edges (it has no pieces): a
+     * level that walked no edge is where its frontier was empty */
+    if (!s_cnt[4 + L % 3]) break;
     L++;
   }
   if (threadIdx.x == 0 && a.levels_out) *a.levels_out = L;

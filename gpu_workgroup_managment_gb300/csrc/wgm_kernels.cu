@@ -109,7 +109,7 @@ cudaError_t wgm_launch_color_async(const wgm_launch &L, const wgm_color_args &a,
 __global__ void __launch_bounds__(1024) wgm_k_bfs_cta(wgm_lonestar_args a, int *spill,
                                                       int spill_cap, int F, int *status) {
   extern __shared__ unsigned wgm_bfs_cta_dyn[];
-  __shared__ int s_cnt[4];
+  __shared__ int s_cnt[8];
   wgm_bfs_cta_smem S;
   S.bits = wgm_bfs_cta_dyn;
   S.front = reinterpret_cast<int *>(wgm_bfs_cta_dyn + ((a.V + 31) >> 5));
