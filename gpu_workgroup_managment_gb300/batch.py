@@ -161,6 +161,13 @@ class Batch:
                                       lv.ctypes.data), "wgm_batch_job_stats")
         return {"start_ns": st, "end_ns": en, "team": tm, "levels": lv}
 
+    def job_work(self) -> np.ndarray:
+        """Edges each job of the last batched launch walked (caller's order);
+        a vertex visited again counts its edges again."""
+        w = np.empty(len(self.jobs), np.int64)
+        check(lib.wgm_batch_job_work(self._h, w.ctypes.data), "wgm_batch_job_work")
+        return w
+
     def reorder_by_last_run(self) -> None:
         """Queue the jobs longest first by their device time in the last
         batched launch."""

@@ -23,8 +23,11 @@
  * 768 and 640 threads let ptxas use 64, 80 and 96 registers per thread.
  * At 64 the K-window walkers spill (hundreds of MB of local-memory traffic
  * per launch); at 96 nothing spills but fewer warps fit on an SM.  The
- * autotuner picks (wgm_batch_configure_kernel). */
-template <int MAXT>
+ * autotuner picks (wgm_batch_configure_kernel).  ASYNC: the warp-local
+ * continuation (lq_rounds > 0) is its own instantiation, so the plain
+ * kernel inlines four job loops, not eight: the extra code raised the plain
+ * kernel's spills and slowed every job by 15-20 % when it was inlined. */
+template <int MAXT, bool ASYNC>
 __global__ void __launch_bounds__(MAXT) wgm_k_batch(wgm_batch_args B) {
   __shared__ wgm_warp_smem sm;
   extern __shared__ wgm_lq wgm_lqs[]; /* one local queue per warp */
@@ -39,23 +42,12 @@ __global__ void __launch_bounds__(MAXT) wgm_k_batch(wgm_batch_args B) {
     const int2 sr = B.slots[slot];
     const wgm_batch_job j = B.jobs[sr.x];
     if (sr.y == 0 && threadIdx.x == 0) B.times[2 * sr.x] = wgm_globaltimer();
-    const bool async = B.lq_rounds > 0;
     if (j.team <= 1) {
-      if (j.algo == 0) {
-        if (async) wgm_cta_lonestar<false, true>(B, j, sr.x, s_cnt, &sm, q);
-        else wgm_cta_lonestar<false, false>(B, j, sr.x, s_cnt, &sm, q);
-      } else {
-        if (async) wgm_cta_lonestar<true, true>(B, j, sr.x, s_cnt, &sm, q);
-        else wgm_cta_lonestar<true, false>(B, j, sr.x, s_cnt, &sm, q);
-      }
+      if (j.algo == 0) wgm_cta_lonestar<false, ASYNC>(B, j, sr.x, s_cnt, &sm, q);
+      else wgm_cta_lonestar<true, ASYNC>(B, j, sr.x, s_cnt, &sm, q);
     } else {
-      if (j.algo == 0) {
-        if (async) wgm_team_lonestar<false, true>(B, j, sr.x, sr.y, &sm, q);
-        else wgm_team_lonestar<false, false>(B, j, sr.x, sr.y, &sm, q);
-      } else {
-        if (async) wgm_team_lonestar<true, true>(B, j, sr.x, sr.y, &sm, q);
-        else wgm_team_lonestar<true, false>(B, j, sr.x, sr.y, &sm, q);
-      }
+      if (j.algo == 0) wgm_team_lonestar<false, ASYNC>(B, j, sr.x, sr.y, &sm, q);
+      else wgm_team_lonestar<true, ASYNC>(B, j, sr.x, sr.y, &sm, q);
     }
     if (sr.y == 0 && threadIdx.x == 0) B.times[2 * sr.x + 1] = wgm_globaltimer();
     __syncthreads();
@@ -67,19 +59,26 @@ static size_t wgm_batch_dyn_smem(int threads) { return (size_t)(threads / 32) * 
 
 static const int wgm_batch_kmax[3] = {1024, 768, 640};   /* threads per CTA */
 static const int wgm_batch_kregs[3] = {64, 80, 96};      /* register budget */
-static const void *wgm_batch_kfn(int v) {
+static const void *wgm_batch_kfn(int v, bool async = false) {
   switch (v) {
-    case 1: return (const void *)wgm_k_batch<768>;
-    case 2: return (const void *)wgm_k_batch<640>;
-    default: return (const void *)wgm_k_batch<1024>;
+    case 1: return async ? (const void *)wgm_k_batch<768, true> : (const void *)wgm_k_batch<768, false>;
+    case 2: return async ? (const void *)wgm_k_batch<640, true> : (const void *)wgm_k_batch<640, false>;
+    default:
+      return async ? (const void *)wgm_k_batch<1024, true> : (const void *)wgm_k_batch<1024, false>;
   }
 }
 static int wgm_batch_per_sm(int v, int threads) {
-  int per_sm = 0;
-  if (threads > wgm_batch_kmax[v] ||
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wgm_batch_kfn(v), threads,
-                                                    wgm_batch_dyn_smem(threads)) != cudaSuccess)
-    return 0;
+  /* the smaller of the two instantiations' occupancies: a grid sized from
+   * it fits on the GPU whichever runs, which the teams' waits rely on */
+  int per_sm = 1 << 30;
+  for (int a = 0; a < 2; a++) {
+    int n = 0;
+    if (threads > wgm_batch_kmax[v] ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, wgm_batch_kfn(v, a == 1), threads,
+                                                      wgm_batch_dyn_smem(threads)) != cudaSuccess)
+      return 0;
+    per_sm = std::min(per_sm, n);
+  }
   return per_sm;
 }
 
@@ -504,10 +503,14 @@ static cudaError_t wgm_batch_enqueue(wgm_batch *b, int grid, cudaStream_t s, int
     B.dist = b->ar[1].dist;
   }
   const size_t smem = wgm_batch_dyn_smem(b->threads);
-  switch (b->kvar) {
-    case 1: wgm_k_batch<768><<<grid, b->threads, smem, s>>>(B); break;
-    case 2: wgm_k_batch<640><<<grid, b->threads, smem, s>>>(B); break;
-    default: wgm_k_batch<1024><<<grid, b->threads, smem, s>>>(B); break;
+  const bool async = b->lq_rounds > 0;
+  switch (b->kvar * 2 + (async ? 1 : 0)) {
+    case 2: wgm_k_batch<768, false><<<grid, b->threads, smem, s>>>(B); break;
+    case 3: wgm_k_batch<768, true><<<grid, b->threads, smem, s>>>(B); break;
+    case 4: wgm_k_batch<640, false><<<grid, b->threads, smem, s>>>(B); break;
+    case 5: wgm_k_batch<640, true><<<grid, b->threads, smem, s>>>(B); break;
+    case 1: wgm_k_batch<1024, true><<<grid, b->threads, smem, s>>>(B); break;
+    default: wgm_k_batch<1024, false><<<grid, b->threads, smem, s>>>(B); break;
   }
   return cudaGetLastError();
 }
@@ -1078,6 +1081,28 @@ extern "C" int wgm_batch_job_stats(wgm_batch *b, int64_t *start_ns, int64_t *end
     if (end_ns) end_ns[k] = (int64_t)(t[2 * q + 1] - t0);
     if (team) team[k] = b->jobs[q].team;
     if (levels) levels[k] = lv[q];
+  }
+  return WGM_OK;
+}
+
+/* Edges each job of the last batched launch walked (caller's order): the
+ * degree of every vertex visit summed, so a job that relaxes each reached
+ * vertex once walks its component's edges and re-relaxations count again. */
+extern "C" int wgm_batch_job_work(wgm_batch *b, int64_t *edges_walked) {
+  if (!b || !edges_walked) return WGM_ERR_INVALID;
+  cudaSetDevice(b->rt->device);
+  const size_t n = (size_t)(1 + WGM_BATCH_CTL_LINES_PER_JOB * b->njobs) * WGM_LINE;
+  std::vector<int> ctl(n);
+  cudaError_t e = cudaStreamSynchronize(b->rt->stream);
+  if (e == cudaSuccess) e = cudaMemcpy(ctl.data(), b->d_ctl, n * 4, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return wgm_cuda_fail(b->rt, e);
+  for (int k = 0; k < b->njobs; k++) {
+    const int q = b->queue_of[k];
+    const size_t at = (size_t)(1 + q * WGM_BATCH_CTL_LINES_PER_JOB + 3) * WGM_LINE +
+                      WGM_BATCH_WORK_OFF;
+    unsigned long long w;
+    std::memcpy(&w, &ctl[at], 8);
+    edges_walked[k] = (int64_t)w;
   }
   return WGM_OK;
 }

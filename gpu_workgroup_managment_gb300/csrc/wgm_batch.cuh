@@ -37,6 +37,17 @@
 #define WGM_BATCH_PRECHECK false
 #endif
 
+/* Edge windows per warp batch in the batched kernel.  Fewer than the
+ * standalone walker's four: the batched kernel is one function inlining
+ * every job loop, so each window's registers are scarce, and a warp's
+ * pieces on the batch's small and sparse graphs rarely fill four windows.
+ * Measured on the 512-graph batch at 512 x 2 CTAs, 64 registers: 9.07 ms
+ * with 4 windows, 8.05 with 3, 7.5 with 2, 8.9 with 1 (the same order at
+ * 256 x 3 / 80 registers and 1024 x 1). */
+#ifndef WGM_BATCH_LS_K
+#define WGM_BATCH_LS_K 2
+#endif
+
 struct wgm_batch_job {
   int V;
   int algo;   /* 0 = BFS, 1 = SSSP */
@@ -425,6 +436,18 @@ __device__ __forceinline__ void wgm_heavy_note(const int *row, int P, bool valid
   wgm_out_push_vertices(row, P, first, src, h);
 }
 
+/* Edges a job walked (relaxations tried, every visit of a vertex counts its
+ * edges again): a 64-bit counter at int offset 24 of the job's arrival line,
+ * cleared with the control block before each launch.  One atomic per warp
+ * when the job ends. */
+#define WGM_BATCH_WORK_OFF 24
+__device__ __forceinline__ void wgm_batch_add_work(int *arr_line, unsigned long long walked) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) walked += __shfl_xor_sync(WGM_FULL, walked, o);
+  if (wgm_lane() == 0 && walked)
+    atomicAdd(reinterpret_cast<unsigned long long *>(arr_line + WGM_BATCH_WORK_OFF), walked);
+}
+
 /* One job on one CTA.  s_cnt: 3 shared level counters, then (s_cnt[4..7])
  * the two far-list counts and least parked distances, then (s_cnt[8..9])
  * the two heavy-list counts. */
@@ -474,6 +497,7 @@ __device__ void wgm_cta_lonestar(const wgm_batch_args &B, const wgm_batch_job &j
   int *hcnt = s_cnt + 8;
   wgm_nf_state ns{nf ? j.delta : 0xffffffffu, 0, -1, false};
   const int Lmax = nf ? (defer ? 8 : 4) * V + 16 : V + 2;
+  unsigned long long walked = 0;
   int L = 1;
   for (;;) {
     const int n = s_cnt[L % 3];
@@ -554,6 +578,7 @@ __device__ void wgm_cta_lonestar(const wgm_batch_args &B, const wgm_batch_job &j
         start = ls[lb + i];
         deg = lc[lb + i];
         src = lu[lb + i];
+        walked += deg;
       }
       if (defer && step == 0)
         wgm_heavy_note(row, j.piece, valid, start, src, H, ns.ep & 1, ns.ep, &hcnt[ns.ep & 1]);
@@ -561,8 +586,8 @@ __device__ void wgm_cta_lonestar(const wgm_batch_args &B, const wgm_batch_job &j
         wgm_ls_chunk_async<SSSP>(row, col, wt, dist, stamp, V, j.piece, L, start, deg, src, o,
                                  q, 0);
       else
-        wgm_ls_chunk<SSSP, WGM_BATCH_PRECHECK || SSSP, PACK>(row, col, wt, dw, stamp, V, j.piece, L,
-                                                     start, deg, src, o);
+        wgm_ls_chunk<SSSP, WGM_BATCH_PRECHECK || SSSP, PACK, WGM_BATCH_LS_K>(
+            row, col, wt, dw, stamp, V, j.piece, L, start, deg, src, o);
     }
     if (ASYNC) wgm_ls_local_rounds<SSSP>(row, col, wt, dist, stamp, V, j.piece, L, o, q,
                                          B.lq_rounds);
@@ -573,6 +598,8 @@ __device__ void wgm_cta_lonestar(const wgm_batch_args &B, const wgm_batch_job &j
   if (PACK)
     for (int i = threadIdx.x; i < V; i += blockDim.x) dist[i] = dw[2 * i + 1];
   if (threadIdx.x == 0 && B.levels) B.levels[job] = L;
+  wgm_batch_add_work(B.ctl + (size_t)(1 + job * WGM_BATCH_CTL_LINES_PER_JOB + 3) * WGM_LINE,
+                     walked);
 }
 
 /* Team barrier: a counting barrier on the job's arrival line.  An arrival
@@ -726,6 +753,7 @@ __device__ int wgm_team_ls_run(const wgm_ls_job &J, wgm_warp_smem *sm, int *err,
   int *hcnt = J.arr + 16;
   wgm_nf_state ns{nf ? J.delta : 0xffffffffu, 0, -1, false};
   const int Lmax = nf ? (defer ? 8 : 4) * V + 16 : V + 2;
+  unsigned long long walked = 0;
   int L = 1;
   for (;;) {
     int step = 0, nfar = 0; /* 0: level, 1: split, 2: clear only, 3: heavy */
@@ -808,6 +836,7 @@ __device__ int wgm_team_ls_run(const wgm_ls_job &J, wgm_warp_smem *sm, int *err,
         start = __ldcg(&ls[lb + i]);
         deg = __ldcg(&lc[lb + i]);
         if (SSSP || ASYNC) src = __ldcg(&lu[lb + i]);
+        walked += deg;
       }
       if (defer && step == 0)
         wgm_heavy_note(J.row, J.piece, valid, start, src, H, ns.ep & 1, ns.ep,
@@ -816,8 +845,8 @@ __device__ int wgm_team_ls_run(const wgm_ls_job &J, wgm_warp_smem *sm, int *err,
         wgm_ls_chunk_async<SSSP>(J.row, J.col, J.wt, J.dist, J.stamp, V, J.piece, L, start, deg,
                                  src, o, q, 0);
       else
-        wgm_ls_chunk<SSSP, WGM_BATCH_PRECHECK || SSSP, PACK>(J.row, J.col, J.wt, dw, J.stamp, V,
-                                                     J.piece, L, start, deg, src, o);
+        wgm_ls_chunk<SSSP, WGM_BATCH_PRECHECK || SSSP, PACK, WGM_BATCH_LS_K>(
+            J.row, J.col, J.wt, dw, J.stamp, V, J.piece, L, start, deg, src, o);
     }
     if (ASYNC)
       wgm_ls_local_rounds<SSSP>(J.row, J.col, J.wt, J.dist, J.stamp, V, J.piece, L, o, q,
@@ -831,6 +860,7 @@ __device__ int wgm_team_ls_run(const wgm_ls_job &J, wgm_warp_smem *sm, int *err,
    * last relaxation: the words are final, each member copies its share */
   if (PACK)
     for (int i = tid; i < V; i += nth) J.dist[i] = dw[2 * i + 1];
+  wgm_batch_add_work(J.arr, walked);
   return L;
 }
 

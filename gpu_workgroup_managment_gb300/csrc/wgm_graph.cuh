@@ -238,6 +238,14 @@ struct wgm_ls_out {
   unsigned wlo = 0, whi = 0xffffffffu;
 };
 
+/* Store one piece at list slot `slot`. */
+__device__ __forceinline__ void wgm_out_put(const wgm_ls_out &o, int slot, int start, int cnt,
+                                            int u) {
+  o.o_start[slot] = start;
+  o.o_cnt[slot] = cnt;
+  if (o.o_u) o.o_u[slot] = u;
+}
+
 /* Reserve n slots of the output list; returns the first. */
 __device__ __forceinline__ int wgm_out_reserve(const wgm_ls_out &o, int n) {
   if (o.counter64) return (int)(unsigned)atomicAdd(o.counter64, (unsigned long long)n);
@@ -263,17 +271,14 @@ __device__ __forceinline__ bool wgm_out_push_vertices(const int *row, int P, boo
   base = __shfl_sync(WGM_FULL, base, 31);
   if (base + total > o.cap) return false;
   const int s = base + incl - np;
-  for (int q = 0; q < np; q++) {
-    o.o_start[s + q] = rs + q * P;
-    o.o_cnt[s + q] = min(P, dg - q * P);
-    if (o.o_u) o.o_u[s + q] = u;
-  }
+  for (int q = 0; q < np; q++) wgm_out_put(o, s + q, rs + q * P, min(P, dg - q * P), u);
   return true;
 }
 
-/* Edges per lane per batch of the chunk walker: a warp relaxes 32*K edges
- * with every memory step of the K windows issued together, so K chains of
- * loads and atomics are in flight per lane instead of one. */
+/* Edges per lane per batch of the chunk walker (its default; callers may
+ * pick another): a warp relaxes 32*K edges with every memory step of the K
+ * windows issued together, so K chains of loads and atomics are in flight
+ * per lane instead of one. */
 #ifndef WGM_LS_K
 #define WGM_LS_K 4
 #endif
@@ -295,22 +300,148 @@ __device__ __forceinline__ bool wgm_out_push_vertices(const int *row, int P, boo
  * is already L found the vertex queued for L+1 by another lane this level
  * (its tag was set by that earlier lowering).  That is the stamp exchange's
  * rule without its dependent round trip; distances read the high halves. */
-template <bool SSSP, bool PRE = true, bool PACK = false>
+/* Pieces of a vertex with d edges: ceil(d / P), by a shift when P is a
+ * power of two (lg = log2 P; -1 otherwise).  P is uniform across the warp,
+ * so the branch is too. */
+__device__ __forceinline__ int wgm_pieces(int d, int P, int lg) {
+  return lg >= 0 ? (d + P - 1) >> lg : (d + P - 1) / P;
+}
+__device__ __forceinline__ int wgm_piece_log2(int P) { return (P & (P - 1)) ? -1 : __ffs(P) - 1; }
+
+/* The tail of a relaxation batch, shared by the walkers: lane k-slot holds
+ * a destination u[k] whose relaxation succeeded (f[k]), its row start rs[k]
+ * and row end d[k] (read beside the atomic), and (SSSP) its new distance
+ * alt[k].  Unpacked SSSP exchanges the level stamp (one queueing per level);
+ * a vertex without edges is not queued; near-far parks a vertex at or above
+ * the threshold in the far list; the rest are queued as pieces with one
+ * warp scan and one counter reservation for the whole batch. */
+template <int K, bool SSSP, bool PACK>
+__device__ __forceinline__ bool wgm_ls_push_batch(const int *row, int *stamp, int P, int lg,
+                                                  int L, int (&u)[K], int (&rs)[K], int (&d)[K],
+                                                  const unsigned (&alt)[K], bool (&f)[K],
+                                                  const wgm_ls_out &o) {
+  const int lane = wgm_lane();
+  bool ok = true;
+  int np[K];
+  int mine = 0, fmine = 0;
+  bool fr[K];
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    if (SSSP && !PACK && f[k]) f[k] = atomicExch(&stamp[u[k]], L) != L;
+    d[k] = f[k] ? max(d[k] - rs[k], 0) : 0; /* a vertex without edges is not queued */
+    /* near-far: a distance at or above the threshold waits in the far list */
+    fr[k] = PACK && d[k] > 0 && alt[k] >= o.T;
+    if (fr[k]) d[k] = 0;
+    fmine += fr[k] ? 1 : 0;
+    np[k] = wgm_pieces(d[k], P, lg);
+    mine += np[k];
+  }
+  const int pincl = wgm_warp_incl_scan(mine);
+  const int ptotal = __shfl_sync(WGM_FULL, pincl, 31);
+  int fincl = 0, ftotal = 0;
+  if (PACK && __any_sync(WGM_FULL, fmine != 0)) {
+    fincl = wgm_warp_incl_scan(fmine);
+    ftotal = __shfl_sync(WGM_FULL, fincl, 31);
+  }
+  if (ptotal == 0 && ftotal == 0) return true;
+  /* the piece and far reservations go out together */
+  int pbase = 0, fbase = 0;
+  if (lane == 31) {
+    if (ptotal) pbase = wgm_out_reserve(o, ptotal);
+    if (PACK && ftotal) fbase = atomicAdd(o.far_cnt, ftotal);
+  }
+  pbase = __shfl_sync(WGM_FULL, pbase, 31);
+  if (PACK && ftotal) {
+    fbase = __shfl_sync(WGM_FULL, fbase, 31);
+    int fs = fbase + fincl - fmine;
+    unsigned m = 0xffffffffu;
+    bool spill[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      spill[k] = false;
+      if (fr[k]) {
+        if (fs < o.far_cap) {
+          o.far_list[fs] = u[k];
+          m = min(m, alt[k]);
+        } else {
+          spill[k] = true; /* far list full: relax it now instead */
+        }
+        fs++;
+      }
+    }
+#pragma unroll
+    for (int x = 16; x > 0; x >>= 1) m = min(m, __shfl_xor_sync(WGM_FULL, m, x));
+    if (lane == 0 && m != 0xffffffffu) atomicMin(o.far_min, m);
+#pragma unroll
+    for (int k = 0; k < K; k++)
+      if (__any_sync(WGM_FULL, spill[k]))
+        ok &= wgm_out_push_vertices(row, P, spill[k], u[k], o);
+  }
+  if (ptotal == 0) return ok;
+  if (pbase + ptotal > o.cap) return false;
+  int slot = pbase + pincl - mine;
+  int sl[K];
+  bool big = false;
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    sl[k] = slot;
+    if (np[k] <= WGM_LS_LANE_PIECES)
+      for (int q = 0; q < np[k]; q++)
+        wgm_out_put(o, slot + q, rs[k] + q * P, min(P, d[k] - q * P), u[k]);
+    else
+      big = true;
+    slot += np[k];
+  }
+  /* high-degree vertices: the whole warp writes their pieces */
+  if (__any_sync(WGM_FULL, big)) {
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      unsigned bb = __ballot_sync(WGM_FULL, np[k] > WGM_LS_LANE_PIECES);
+      while (bb) {
+        const int j = __ffs(bb) - 1;
+        bb &= bb - 1;
+        const int bs = __shfl_sync(WGM_FULL, rs[k], j), bd = __shfl_sync(WGM_FULL, d[k], j);
+        const int bu = __shfl_sync(WGM_FULL, u[k], j), bsl = __shfl_sync(WGM_FULL, sl[k], j);
+        const int bn = wgm_pieces(bd, P, lg);
+        for (int q = lane; q < bn; q += 32)
+          wgm_out_put(o, bsl + q, bs + q * P, min(P, bd - q * P), bu);
+      }
+    }
+  }
+  return ok;
+}
+
+/* Relax the edges of one chunk (one piece per lane: first edge `start`,
+ * `deg` edges, source distance `dv` for SSSP) and queue the improved
+ * vertices as pieces of the next level.  Per batch of 32*K edges:
+ *   col/wt loads -> dist pre-check -> atomic (CAS for BFS, min for SSSP)
+ *   with row[u], row[u+1] fetched beside it -> SSSP stamp exchange ->
+ *   one warp scan and one counter atomic for every piece of the batch.
+ * The relaxation rules are stated above wgm_ls_push; the order of
+ * relaxations inside a level does not change the fixpoint. */
+/* PACK (SSSP only): `dist` points at 64-bit words {low: level tag, high:
+ * distance} instead of a dist[] / stamp[] pair.  One 64-bit atomicMin of
+ * (alt << 32 | L) then both relaxes and deduplicates: it lowered the
+ * distance iff the old high half exceeds alt, and a lowering whose old tag
+ * is already L found the vertex queued for L+1 by another lane this level
+ * (its tag was set by that earlier lowering).  That is the stamp exchange's
+ * rule without its dependent round trip; distances read the high halves. */
+template <bool SSSP, bool PRE = true, bool PACK = false, int K = WGM_LS_K>
 __device__ __forceinline__ bool wgm_ls_chunk(const int *row, const int *col, const unsigned *wt,
                                              unsigned *dist, int *stamp, int V, int P, int L,
                                              int start, int deg, int src,
                                              const wgm_ls_out &o) {
   static_assert(SSSP || !PACK, "the packed word carries SSSP distances");
-  constexpr int K = WGM_LS_K;
   constexpr int DS = PACK ? 2 : 1, DH = PACK ? 1 : 0; /* distance word of v: DS*v+DH */
   const int lane = wgm_lane();
+  const int lg = wgm_piece_log2(P);
   const int incl = wgm_warp_incl_scan(deg);
   const int total = __shfl_sync(WGM_FULL, incl, 31);
   const int off = incl - deg;
   const int base = start - off;
   bool ok = true;
   for (int w = 0; w < total; w += 32 * K) {
-    int e[K], u[K], rs[K], d[K], np[K], sv[K];
+    int e[K], u[K], rs[K], d[K], sv[K];
     unsigned alt[K];
     bool f[K];
 #pragma unroll
@@ -326,6 +457,7 @@ __device__ __forceinline__ bool wgm_ls_chunk(const int *row, const int *col, con
 #pragma unroll
     for (int k = 0; k < K; k++) {
       u[k] = f[k] ? __ldg(&col[e[k]]) : -1;
+      alt[k] = 0;
       if (SSSP) {
         unsigned wk = f[k] ? __ldg(&wt[e[k]]) : WGM_LONESTAR_INF;
         unsigned dvk = f[k] ? __ldcg(&dist[DS * sv[k] + DH]) : 0u;
@@ -359,96 +491,7 @@ __device__ __forceinline__ bool wgm_ls_chunk(const int *row, const int *col, con
         d[k] = __ldg(&row[u[k] + 1]);
       }
     }
-    int mine = 0, fmine = 0;
-    bool fr[K];
-#pragma unroll
-    for (int k = 0; k < K; k++) {
-      if (SSSP && !PACK && f[k]) f[k] = atomicExch(&stamp[u[k]], L) != L;
-      d[k] = f[k] ? max(d[k] - rs[k], 0) : 0; /* a vertex without edges is not queued */
-      /* near-far: a distance at or above the threshold waits in the far list */
-      fr[k] = PACK && d[k] > 0 && alt[k] >= o.T;
-      if (fr[k]) d[k] = 0;
-      fmine += fr[k] ? 1 : 0;
-      np[k] = (d[k] + P - 1) / P;
-      mine += np[k];
-    }
-    const int pincl = wgm_warp_incl_scan(mine);
-    const int ptotal = __shfl_sync(WGM_FULL, pincl, 31);
-    int fincl = 0, ftotal = 0;
-    if (PACK && __any_sync(WGM_FULL, fmine != 0)) {
-      fincl = wgm_warp_incl_scan(fmine);
-      ftotal = __shfl_sync(WGM_FULL, fincl, 31);
-    }
-    if (ptotal == 0 && ftotal == 0) continue;
-    /* the piece and far reservations go out together */
-    int pbase = 0, fbase = 0;
-    if (lane == 31) {
-      if (ptotal) pbase = wgm_out_reserve(o, ptotal);
-      if (PACK && ftotal) fbase = atomicAdd(o.far_cnt, ftotal);
-    }
-    pbase = __shfl_sync(WGM_FULL, pbase, 31);
-    if (PACK && ftotal) {
-      fbase = __shfl_sync(WGM_FULL, fbase, 31);
-      int fs = fbase + fincl - fmine;
-      unsigned m = 0xffffffffu;
-      bool spill[K];
-#pragma unroll
-      for (int k = 0; k < K; k++) {
-        spill[k] = false;
-        if (fr[k]) {
-          if (fs < o.far_cap) {
-            o.far_list[fs] = u[k];
-            m = min(m, alt[k]);
-          } else {
-            spill[k] = true; /* far list full: relax it now instead */
-          }
-          fs++;
-        }
-      }
-#pragma unroll
-      for (int x = 16; x > 0; x >>= 1) m = min(m, __shfl_xor_sync(WGM_FULL, m, x));
-      if (lane == 0 && m != 0xffffffffu) atomicMin(o.far_min, m);
-#pragma unroll
-      for (int k = 0; k < K; k++)
-        if (__any_sync(WGM_FULL, spill[k]))
-          ok &= wgm_out_push_vertices(row, P, spill[k], u[k], o);
-    }
-    if (ptotal == 0) continue;
-    if (pbase + ptotal > o.cap) {
-      ok = false;
-      continue;
-    }
-    int slot = pbase + pincl - mine;
-    int sl[K];
-#pragma unroll
-    for (int k = 0; k < K; k++) {
-      sl[k] = slot;
-      if (np[k] <= WGM_LS_LANE_PIECES) {
-        for (int q = 0; q < np[k]; q++) {
-          o.o_start[slot + q] = rs[k] + q * P;
-          o.o_cnt[slot + q] = min(P, d[k] - q * P);
-          if (o.o_u) o.o_u[slot + q] = u[k];
-        }
-      }
-      slot += np[k];
-    }
-    /* high-degree vertices: the whole warp writes their pieces */
-#pragma unroll
-    for (int k = 0; k < K; k++) {
-      unsigned big = __ballot_sync(WGM_FULL, np[k] > WGM_LS_LANE_PIECES);
-      while (big) {
-        const int j = __ffs(big) - 1;
-        big &= big - 1;
-        const int bs = __shfl_sync(WGM_FULL, rs[k], j), bd = __shfl_sync(WGM_FULL, d[k], j);
-        const int bu = __shfl_sync(WGM_FULL, u[k], j), bsl = __shfl_sync(WGM_FULL, sl[k], j);
-        const int bn = (bd + P - 1) / P;
-        for (int q = lane; q < bn; q += 32) {
-          o.o_start[bsl + q] = bs + q * P;
-          o.o_cnt[bsl + q] = min(P, bd - q * P);
-          if (o.o_u) o.o_u[bsl + q] = bu;
-        }
-      }
-    }
+    ok &= wgm_ls_push_batch<K, SSSP, PACK>(row, stamp, P, lg, L, u, rs, d, alt, f, o);
   }
   return ok;
 }

@@ -435,6 +435,10 @@ int wgm_batch_read_all(wgm_batch *b, uint32_t *out, int64_t n);
  * (ns from the earliest start), team size, levels run. */
 int wgm_batch_job_stats(wgm_batch *b, int64_t *start_ns, int64_t *end_ns, int32_t *team,
                         int32_t *levels);
+/* Per job (caller's order) of the last batched launch: edges walked, every
+ * visit of a vertex counting its edges (the component's edge count for a job
+ * that relaxes each vertex once; more where distances are lowered again). */
+int wgm_batch_job_work(wgm_batch *b, int64_t *edges_walked);
 int wgm_batch_info(wgm_batch *b, int64_t *total_nodes, int64_t *total_edges, int *threads,
                    int *ctas_per_sm, int *piece);
 /* Queue the jobs longest first by their device time in the last batched

@@ -210,6 +210,34 @@ def test_batch_edge_cases():
                 assert np.array_equal(b.result(k), want[k]), ("near-far", mult, k)
 
 
+LONESTAR_INF = 1000000000  # MYINFINITY of the Lonestar kernels: unreached
+
+
+@pytest.mark.parametrize("team_edges,threads", [(0, 512), (1500, 256), (300, 128)])
+def test_batch_job_work(small_batch, team_edges, threads):
+    """Edges walked per job: a BFS job visits every reached vertex once, so
+    it walks exactly their edges; an SSSP job walks them at least once (more
+    where distances are lowered again), on single CTAs and teams."""
+    gs, jobs = small_batch
+    want = _oracle(gs, jobs)
+    with Runtime() as rt, Batch(rt, gs, jobs) as b:
+        b.configure(threads, 0, 0)
+        b.configure_teams(team_edges, 0)
+        b.run()
+        work = b.job_work()
+        teams = b.job_stats()["team"]
+        for k, (gi, algo, _) in enumerate(jobs):
+            g = gs[gi]
+            deg = np.maximum(np.diff(g.row_ptr.astype(np.int64)), 0)
+            reached = int(deg[want[k] != LONESTAR_INF].sum())
+            if algo == "bfs":
+                assert work[k] == reached, (k, work[k], reached)
+            else:
+                assert work[k] >= reached, (k, work[k], reached)
+        if team_edges:
+            assert teams.max() > 1
+
+
 def test_batch_autotune_picks_a_valid_config(small_batch):
     gs, jobs = small_batch
     gs, jobs = gs[:12], [j for j in jobs if j[0] < 12]
