@@ -174,6 +174,7 @@ _PROTOS = {
     "wgm_batch_graph_offsets": (_I, [_P, _P, _P]),
     "wgm_batch_job_stats": (_I, [_P, _P, _P, _P, _P]),
     "wgm_batch_job_work": (_I, [_P, _P]),
+    "wgm_batch_configure_bfs_one_cta": (_I, [_P, C.c_double]),
     "wgm_batch_reorder_by_last_run": (_I, [_P]),
     "wgm_serve_create": (_I, [_P, _P, _P, _I, _P, _I, _I, _P, _I, _I, _P, C.c_int64, _P]),
     "wgm_serve_run": (_I, [_P, _P, _P]),

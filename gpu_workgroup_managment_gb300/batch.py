@@ -108,6 +108,12 @@ class Batch:
         check(lib.wgm_batch_configure_sssp(self._h, float(delta_mult), int(far_cap)),
               "configure_sssp")
 
+    def configure_bfs_one_cta(self, max_avg_degree: float = 5.0) -> None:
+        """BFS jobs on graphs of average degree <= max_avg_degree run on one
+        CTA whatever their size (0: teams by edges for every job)."""
+        check(lib.wgm_batch_configure_bfs_one_cta(self._h, float(max_avg_degree)),
+              "wgm_batch_configure_bfs_one_cta")
+
     def configure_sssp_dense(self, light_mult: float = 0.0) -> None:
         """SSSP jobs on graphs of average degree >= 6: buckets of light_mult x
         the mean weight, heavy edges relaxed once per bucket (0: off)."""

@@ -23,12 +23,22 @@
  * 768 and 640 threads let ptxas use 64, 80 and 96 registers per thread.
  * At 64 the K-window walkers spill (hundreds of MB of local-memory traffic
  * per launch); at 96 nothing spills but fewer warps fit on an SM.  The
- * autotuner picks (wgm_batch_configure_kernel).  ASYNC: the warp-local
- * continuation (lq_rounds > 0) is its own instantiation, so the plain
- * kernel inlines four job loops, not eight: the extra code raised the plain
- * kernel's spills and slowed every job by 15-20 % when it was inlined. */
-template <int MAXT, bool ASYNC>
+ * autotuner picks (wgm_batch_configure_kernel).  Each mode (plain, the
+ * warp-local continuation when lq_rounds > 0, heavy-edge deferral when a
+ * job has light > 0) is its own instantiation: code inlined into the plain
+ * kernel that a launch never runs raised its spills and slowed every job
+ * 10-20 % in measurements. */
+/* Kernel modes: the plain job loops, the warp-local continuation, and the
+ * near-far schedule with heavy edges deferred (each its own instantiation:
+ * code a launch does not run still costs the others registers). */
+#define WGM_BATCH_MODE_PLAIN 0
+#define WGM_BATCH_MODE_ASYNC 1
+#define WGM_BATCH_MODE_DEFER 2
+
+template <int MAXT, int MODE>
 __global__ void __launch_bounds__(MAXT) wgm_k_batch(wgm_batch_args B) {
+  constexpr bool ASYNC = MODE == WGM_BATCH_MODE_ASYNC;
+  constexpr bool DEFER = MODE == WGM_BATCH_MODE_DEFER;
   __shared__ wgm_warp_smem sm;
   extern __shared__ wgm_lq wgm_lqs[]; /* one local queue per warp */
   wgm_lq *q = &wgm_lqs[threadIdx.x >> 5];
@@ -44,10 +54,10 @@ __global__ void __launch_bounds__(MAXT) wgm_k_batch(wgm_batch_args B) {
     if (sr.y == 0 && threadIdx.x == 0) B.times[2 * sr.x] = wgm_globaltimer();
     if (j.team <= 1) {
       if (j.algo == 0) wgm_cta_lonestar<false, ASYNC>(B, j, sr.x, s_cnt, &sm, q);
-      else wgm_cta_lonestar<true, ASYNC>(B, j, sr.x, s_cnt, &sm, q);
+      else wgm_cta_lonestar<true, ASYNC, DEFER>(B, j, sr.x, s_cnt, &sm, q);
     } else {
       if (j.algo == 0) wgm_team_lonestar<false, ASYNC>(B, j, sr.x, sr.y, &sm, q);
-      else wgm_team_lonestar<true, ASYNC>(B, j, sr.x, sr.y, &sm, q);
+      else wgm_team_lonestar<true, ASYNC, DEFER>(B, j, sr.x, sr.y, &sm, q);
     }
     if (sr.y == 0 && threadIdx.x == 0) B.times[2 * sr.x + 1] = wgm_globaltimer();
     __syncthreads();
@@ -59,22 +69,29 @@ static size_t wgm_batch_dyn_smem(int threads) { return (size_t)(threads / 32) * 
 
 static const int wgm_batch_kmax[3] = {1024, 768, 640};   /* threads per CTA */
 static const int wgm_batch_kregs[3] = {64, 80, 96};      /* register budget */
-static const void *wgm_batch_kfn(int v, bool async = false) {
+template <int MAXT>
+static const void *wgm_batch_kfn_t(int mode) {
+  switch (mode) {
+    case WGM_BATCH_MODE_ASYNC: return (const void *)wgm_k_batch<MAXT, WGM_BATCH_MODE_ASYNC>;
+    case WGM_BATCH_MODE_DEFER: return (const void *)wgm_k_batch<MAXT, WGM_BATCH_MODE_DEFER>;
+    default: return (const void *)wgm_k_batch<MAXT, WGM_BATCH_MODE_PLAIN>;
+  }
+}
+static const void *wgm_batch_kfn(int v, int mode = WGM_BATCH_MODE_PLAIN) {
   switch (v) {
-    case 1: return async ? (const void *)wgm_k_batch<768, true> : (const void *)wgm_k_batch<768, false>;
-    case 2: return async ? (const void *)wgm_k_batch<640, true> : (const void *)wgm_k_batch<640, false>;
-    default:
-      return async ? (const void *)wgm_k_batch<1024, true> : (const void *)wgm_k_batch<1024, false>;
+    case 1: return wgm_batch_kfn_t<768>(mode);
+    case 2: return wgm_batch_kfn_t<640>(mode);
+    default: return wgm_batch_kfn_t<1024>(mode);
   }
 }
 static int wgm_batch_per_sm(int v, int threads) {
-  /* the smaller of the two instantiations' occupancies: a grid sized from
-   * it fits on the GPU whichever runs, which the teams' waits rely on */
+  /* the smallest of the modes' occupancies: a grid sized from it fits on
+   * the GPU whichever runs, which the teams' waits rely on */
   int per_sm = 1 << 30;
-  for (int a = 0; a < 2; a++) {
+  for (int mode = 0; mode < 3; mode++) {
     int n = 0;
     if (threads > wgm_batch_kmax[v] ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, wgm_batch_kfn(v, a == 1), threads,
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, wgm_batch_kfn(v, mode), threads,
                                                       wgm_batch_dyn_smem(threads)) != cudaSuccess)
       return 0;
     per_sm = std::min(per_sm, n);
@@ -121,6 +138,13 @@ struct wgm_batch {
    * saves are mostly the failed ones the distance pre-check already makes
    * cheap.  The autotuner still tries 0.1, 0.2 and 0.4. */
   double light_mult = 0.0;
+  /* BFS jobs on graphs of average degree at most this run on one CTA
+   * whatever their size (0: teams by edges for every job).  Their levels
+   * are short chains over small frontiers: a 512x512 grid BFS takes ~3 ms
+   * on one CTA against ~4 ms on a team of four (16 CTA-ms), and BFS jobs
+   * are not the batch's critical path (the SSSP jobs on the same grids
+   * are). */
+  double bfs_one_cta_deg = 5.0;
   std::vector<double> gmeanw; /* mean weight per graph (1 without weights) */
   int teams_grid = 0; /* grid the team sizes were computed for (0 = stale) */
   cudaGraph_t graph = nullptr;
@@ -297,7 +321,7 @@ extern "C" int wgm_batch_create(wgm_runtime *rt, int num_graphs, const wgm_graph
     j.col_off = b->g_col_off[g];
     j.graph = g;
     j.team = 1;
-    j.boost = 1;
+    j.boost = 100;
     j.dist_off = dist_at[k];
     /* every job: claims of the warp-local queues, or (SSSP) one 64-bit
      * {level tag, distance} word per vertex; offsets stay even, so the
@@ -452,8 +476,12 @@ static int wgm_batch_teams(wgm_batch *b, int grid) {
   std::vector<int2> slots;
   for (int q = 0; q < b->njobs; q++) {
     wgm_batch_job &j = b->jobs[q];
-    long long g = (b->gE[j.graph] + te - 1) / te * std::max(j.boost, 1);
+    const long long g0 = (b->gE[j.graph] + te - 1) / te;
+    long long g = (g0 * std::max(j.boost, 100) + 99) / 100;
     j.team = (int)std::max(1LL, std::min<long long>(g, mt));
+    if (j.algo == 0 && b->bfs_one_cta_deg > 0 &&
+        (double)b->gE[j.graph] <= b->bfs_one_cta_deg * (double)b->gV[j.graph])
+      j.team = 1;
     for (int r = 0; r < j.team; r++) slots.push_back(make_int2(q, r));
   }
   cudaError_t e = cudaSuccess;
@@ -503,14 +531,29 @@ static cudaError_t wgm_batch_enqueue(wgm_batch *b, int grid, cudaStream_t s, int
     B.dist = b->ar[1].dist;
   }
   const size_t smem = wgm_batch_dyn_smem(b->threads);
-  const bool async = b->lq_rounds > 0;
-  switch (b->kvar * 2 + (async ? 1 : 0)) {
-    case 2: wgm_k_batch<768, false><<<grid, b->threads, smem, s>>>(B); break;
-    case 3: wgm_k_batch<768, true><<<grid, b->threads, smem, s>>>(B); break;
-    case 4: wgm_k_batch<640, false><<<grid, b->threads, smem, s>>>(B); break;
-    case 5: wgm_k_batch<640, true><<<grid, b->threads, smem, s>>>(B); break;
-    case 1: wgm_k_batch<1024, true><<<grid, b->threads, smem, s>>>(B); break;
-    default: wgm_k_batch<1024, false><<<grid, b->threads, smem, s>>>(B); break;
+  int mode = WGM_BATCH_MODE_PLAIN;
+  if (b->lq_rounds > 0) {
+    mode = WGM_BATCH_MODE_ASYNC;
+  } else {
+    for (const auto &j : b->jobs)
+      if (j.light > 0) mode = WGM_BATCH_MODE_DEFER;
+  }
+  switch (b->kvar * 3 + mode) {
+#define WGM_BATCH_LAUNCH(V, T)                                      \
+  case V * 3 + WGM_BATCH_MODE_PLAIN:                                \
+    wgm_k_batch<T, WGM_BATCH_MODE_PLAIN><<<grid, b->threads, smem, s>>>(B); \
+    break;                                                          \
+  case V * 3 + WGM_BATCH_MODE_ASYNC:                                \
+    wgm_k_batch<T, WGM_BATCH_MODE_ASYNC><<<grid, b->threads, smem, s>>>(B); \
+    break;                                                          \
+  case V * 3 + WGM_BATCH_MODE_DEFER:                                \
+    wgm_k_batch<T, WGM_BATCH_MODE_DEFER><<<grid, b->threads, smem, s>>>(B); \
+    break;
+    WGM_BATCH_LAUNCH(0, 1024)
+    WGM_BATCH_LAUNCH(1, 768)
+    WGM_BATCH_LAUNCH(2, 640)
+#undef WGM_BATCH_LAUNCH
+    default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
 }
@@ -561,6 +604,16 @@ extern "C" int wgm_batch_configure_sssp(wgm_batch *b, double delta_mult, int far
   wgm_batch_set_deltas(b);
   int st = wgm_batch_relayout(b);
   if (st) return st;
+  wgm_batch_free_graph(b);
+  return WGM_OK;
+}
+
+extern "C" int wgm_batch_configure_bfs_one_cta(wgm_batch *b, double max_avg_degree) {
+  if (!b || !(max_avg_degree >= 0) || max_avg_degree > 1e6) return WGM_ERR_INVALID;
+  cudaSetDevice(b->rt->device);
+  cudaStreamSynchronize(b->rt->stream);
+  b->bfs_one_cta_deg = max_avg_degree;
+  b->teams_grid = 0;
   wgm_batch_free_graph(b);
   return WGM_OK;
 }
@@ -948,7 +1001,7 @@ extern "C" int wgm_batch_autotune(wgm_batch *b, int reps, int *best_threads,
   b->kvar = bv;
   /* 3. team size again at the winning shape */
   const long long base = bte;
-  for (double f : {0.5, 0.75, 1.5, 2.0}) {
+  for (double f : {0.5, 0.75, 0.85, 1.2, 1.5, 2.0}) {
     long long te = std::max(1LL << 12, (long long)(base * f));
     double ms = 0;
     int s = point(bt, bc, bp, te, &ms);
@@ -1007,11 +1060,15 @@ extern "C" int wgm_batch_autotune(wgm_batch *b, int reps, int *best_threads,
     s = wgm_batch_configure_sssp_dense(b, bl);
     if (s) return s;
   }
-  /* 5. critical path: the jobs that run longest double their team, while
-   * that shortens the launch */
+  /* 5. critical path: the jobs that run longest (over 0.8 x the launch)
+   * grow their team by a quarter, while that shortens the launch; a step
+   * that does not is undone and the search ends.  Quarter steps: on the
+   * 512-graph batch the SSSP jobs on the 512x512 grids are the critical
+   * path, and their best team (5 CTAs) sits between the edge rule's 4 and
+   * a doubling's 8. */
   s = point(bt, bc, bp, bte, &best);
   if (s) return s;
-  for (int it = 0; it < 6; it++) {
+  for (int it = 0; it < 10; it++) {
     std::vector<unsigned long long> t(2 * (size_t)b->njobs);
     if (cudaMemcpy(t.data(), b->d_times, t.size() * 8, cudaMemcpyDeviceToHost) != cudaSuccess)
       break;
@@ -1025,8 +1082,8 @@ extern "C" int wgm_batch_autotune(wgm_batch *b, int reps, int *best_threads,
     int boosted = 0;
     for (int q = 0; q < b->njobs; q++) {
       saved[b->jobs[q].dist_off] = b->jobs[q].boost;
-      if ((double)(t[2 * q + 1] - t[2 * q]) > 0.6 * span && b->jobs[q].team < grid_of(bt, bc) / 4) {
-        b->jobs[q].boost *= 2;
+      if ((double)(t[2 * q + 1] - t[2 * q]) > 0.8 * span && b->jobs[q].team < grid_of(bt, bc) / 4) {
+        b->jobs[q].boost = b->jobs[q].boost * 5 / 4;
         boosted++;
       }
     }

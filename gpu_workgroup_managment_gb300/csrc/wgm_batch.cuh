@@ -68,7 +68,8 @@ struct wgm_batch_job {
                      each) and a settle stamp per vertex after the far lists */
   int graph; /* graph index (host bookkeeping) */
   int team;  /* CTAs working on the job */
-  int boost; /* host: team multiplier from the critical-path pass */
+  int boost; /* host: team size in percent of the edge rule's (critical-path
+                pass of the autotuner; 100 = the rule) */
 };
 
 /* Control block, cleared before every launch: line 0 = queue head, then per
@@ -451,7 +452,7 @@ __device__ __forceinline__ void wgm_batch_add_work(int *arr_line, unsigned long 
 /* One job on one CTA.  s_cnt: 3 shared level counters, then (s_cnt[4..7])
  * the two far-list counts and least parked distances, then (s_cnt[8..9])
  * the two heavy-list counts. */
-template <bool SSSP, bool ASYNC>
+template <bool SSSP, bool ASYNC, bool DEFER = false>
 __device__ void wgm_cta_lonestar(const wgm_batch_args &B, const wgm_batch_job &j, int job,
                                  int *s_cnt, wgm_warp_smem *sm, wgm_lq *q) {
   const int V = j.V;
@@ -470,7 +471,7 @@ __device__ void wgm_cta_lonestar(const wgm_batch_args &B, const wgm_batch_job &j
   constexpr bool PACK = SSSP && !ASYNC;
   unsigned *dw = PACK ? reinterpret_cast<unsigned *>(stamp) : dist;
   const bool nf = PACK && j.delta > 0;
-  const bool defer = nf && j.light > 0;
+  const bool defer = DEFER && nf && j.light > 0;
   int *far = wl_u + 2 * (size_t)cap;
   wgm_heavy_lists H;
   H.buf = far + 2 * (size_t)j.far_cap;
@@ -707,7 +708,7 @@ struct wgm_ls_job {
  * level with the level counters triple-buffered in the job's control lines.
  * Returns the number of levels (the Lonestar iteration count), or -1 when a
  * team wait failed. */
-template <bool SSSP, bool ASYNC = false>
+template <bool SSSP, bool ASYNC = false, bool DEFER = false>
 __device__ int wgm_team_ls_run(const wgm_ls_job &J, wgm_warp_smem *sm, int *err,
                                unsigned long long spin_ns, wgm_lq *q = nullptr) {
   const int V = J.V, G = J.G, rank = J.rank, cap = J.cap;
@@ -717,7 +718,7 @@ __device__ int wgm_team_ls_run(const wgm_ls_job &J, wgm_warp_smem *sm, int *err,
   constexpr bool PACK = SSSP && !ASYNC; /* as in wgm_cta_lonestar */
   unsigned *dw = PACK ? reinterpret_cast<unsigned *>(J.stamp) : J.dist;
   const bool nf = PACK && J.delta > 0;
-  const bool defer = nf && J.light > 0;
+  const bool defer = DEFER && nf && J.light > 0;
   wgm_heavy_lists H;
   H.buf = J.wl_u + 2 * (size_t)cap + 2 * (size_t)J.far_cap;
   H.settle = H.buf + 6 * (size_t)cap;
@@ -865,7 +866,7 @@ __device__ int wgm_team_ls_run(const wgm_ls_job &J, wgm_warp_smem *sm, int *err,
 }
 
 /* One batch job on a team of G > 1 CTAs; this CTA is member `rank`. */
-template <bool SSSP, bool ASYNC>
+template <bool SSSP, bool ASYNC, bool DEFER = false>
 __device__ void wgm_team_lonestar(const wgm_batch_args &B, const wgm_batch_job &j, int job,
                                   int rank, wgm_warp_smem *sm, wgm_lq *q) {
   wgm_ls_job J;
@@ -890,7 +891,7 @@ __device__ void wgm_team_lonestar(const wgm_batch_args &B, const wgm_batch_job &
   J.cnt = ctl;
   J.arr = ctl + 3 * WGM_LINE;
   J.lq_rounds = B.lq_rounds;
-  const int L = wgm_team_ls_run<SSSP, ASYNC>(J, sm, B.err, B.spin_ns, q);
+  const int L = wgm_team_ls_run<SSSP, ASYNC, DEFER>(J, sm, B.err, B.spin_ns, q);
   if (L > 0 && rank == 0 && threadIdx.x == 0 && B.levels) B.levels[job] = L;
 }
 

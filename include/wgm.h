@@ -396,6 +396,12 @@ int wgm_batch_sssp_info(wgm_batch *b, double *delta_mult, int *far_cap);
  * change. */
 int wgm_batch_configure_sssp_dense(wgm_batch *b, double light_mult);
 int wgm_batch_sssp_dense_info(wgm_batch *b, double *light_mult);
+/* BFS jobs on graphs of average degree at most max_avg_degree (default 5:
+ * grids, meshes, road-like graphs; 0: none) run on one CTA whatever their
+ * edge count: their levels are chains of dependent round trips over small
+ * frontiers, which a team speeds up little at several times the CTA time.
+ * Distances do not change. */
+int wgm_batch_configure_bfs_one_cta(wgm_batch *b, double max_avg_degree);
 /* Register budget of the batched kernel (no reference counterpart): 64, 80
  * or 96 registers per thread (blocks of at most 1024, 768, 640 threads);
  * fewer registers fit more warps on an SM, more avoid spilling. */

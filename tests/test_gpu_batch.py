@@ -199,6 +199,7 @@ def test_batch_edge_cases():
         b.run()
         for k in range(len(jobs)):
             assert np.array_equal(b.result(k), want[k]), k
+        b.configure_bfs_one_cta(0)  # BFS on the star and the grid on teams too
         b.configure_teams(100, 4)  # the star and the grid on teams
         b.run()
         for k in range(len(jobs)):
@@ -223,6 +224,7 @@ def test_batch_job_work(small_batch, team_edges, threads):
     with Runtime() as rt, Batch(rt, gs, jobs) as b:
         b.configure(threads, 0, 0)
         b.configure_teams(team_edges, 0)
+        b.configure_bfs_one_cta(0 if team_edges == 300 else 5.0)
         b.run()
         work = b.job_work()
         teams = b.job_stats()["team"]
@@ -232,6 +234,8 @@ def test_batch_job_work(small_batch, team_edges, threads):
             reached = int(deg[want[k] != LONESTAR_INF].sum())
             if algo == "bfs":
                 assert work[k] == reached, (k, work[k], reached)
+                if team_edges != 300 and g.num_edges <= 5 * g.num_nodes:
+                    assert teams[k] == 1, k  # low-degree BFS on one CTA
             else:
                 assert work[k] >= reached, (k, work[k], reached)
         if team_edges:
