@@ -42,7 +42,7 @@ __global__ void __launch_bounds__(MAXT) wgm_k_batch(wgm_batch_args B) {
   __shared__ wgm_warp_smem sm;
   extern __shared__ wgm_lq wgm_lqs[]; /* one local queue per warp */
   wgm_lq *q = &wgm_lqs[threadIdx.x >> 5];
-  __shared__ int s_cnt[10];
+  __shared__ int s_cnt[WGM_BATCH_SCNT];
   __shared__ int s_slot;
   for (;;) {
     if (threadIdx.x == 0) s_slot = atomicAdd(&B.ctl[0], 1);

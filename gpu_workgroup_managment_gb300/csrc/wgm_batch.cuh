@@ -48,6 +48,10 @@
 #define WGM_BATCH_LS_K 2
 #endif
 
+/* Shared-memory counters of a one-CTA job: three level counters, far-list
+ * counts and least distances, heavy-list counts, three chunk-grab counters. */
+#define WGM_BATCH_SCNT 13
+
 struct wgm_batch_job {
   int V;
   int algo;   /* 0 = BFS, 1 = SSSP */
@@ -487,7 +491,8 @@ __device__ void wgm_cta_lonestar(const wgm_batch_args &B, const wgm_batch_job &j
       stamp[i] = 0;
     }
   }
-  if (threadIdx.x < 10) s_cnt[threadIdx.x] = (threadIdx.x == 6 || threadIdx.x == 7) ? (int)0xffffffffu : 0;
+  if (threadIdx.x < WGM_BATCH_SCNT)
+    s_cnt[threadIdx.x] = (threadIdx.x == 6 || threadIdx.x == 7) ? (int)0xffffffffu : 0;
   if (lane == 0) q->n[0] = q->n[1] = 0;
   __syncthreads();
   if (threadIdx.x < 32)
@@ -515,9 +520,11 @@ __device__ void wgm_cta_lonestar(const wgm_batch_args &B, const wgm_batch_job &j
       }
     }
     if (L > Lmax) break;
-    /* the counter of level L-1, read before the previous barrier */
+    /* the counter of level L-1, read before the previous barrier; the grab
+     * counter of level L-1, whose last grab came before that barrier */
     if (threadIdx.x == 0) {
       s_cnt[(L + 2) % 3] = 0;
+      s_cnt[10 + (L + 2) % 3] = 0;
       if (ns.pend >= 0) {
         fctl[ns.pend] = 0;
         fctl[2 + ns.pend] = (int)0xffffffffu;
@@ -572,7 +579,16 @@ __device__ void wgm_cta_lonestar(const wgm_batch_args &B, const wgm_batch_job &j
     /* pieces per warp: 32, or fewer when the list is short, so a small
      * frontier spreads over every warp instead of queueing on a few */
     const int per = max(1, min(32, (m + nw - 1) / nw));
-    for (int b = warp * per; b < m; b += nw * per) {
+    /* warps take chunks of `per` pieces from a shared-memory counter as
+     * they finish the last, so a warp that drew heavy pieces does not hold
+     * the level's barrier while the others wait (level L's counter was
+     * cleared at level L-2) */
+    int *grab = &s_cnt[10 + L % 3];
+    for (;;) {
+      int b = 0;
+      if (lane == 0) b = atomicAdd(grab, per);
+      b = __shfl_sync(WGM_FULL, b, 0);
+      if (b >= m) break;
       int i = b + lane, deg = 0, start = 0, src = 0;
       const bool valid = lane < per && i < m;
       if (valid) {
@@ -713,6 +729,8 @@ __device__ int wgm_team_ls_run(const wgm_ls_job &J, wgm_warp_smem *sm, int *err,
                                unsigned long long spin_ns, wgm_lq *q = nullptr) {
   const int V = J.V, G = J.G, rank = J.rank, cap = J.cap;
   const int lane = wgm_lane(), warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  __shared__ int s_grab[3]; /* chunk grab counters by level mod 3 */
+  if (threadIdx.x < 3) s_grab[threadIdx.x] = 0;
   unsigned nb = 0;
   const int tid = rank * blockDim.x + threadIdx.x, nth = G * blockDim.x;
   constexpr bool PACK = SSSP && !ASYNC; /* as in wgm_cta_lonestar */
@@ -770,6 +788,7 @@ __device__ int wgm_team_ls_run(const wgm_ls_job &J, wgm_warp_smem *sm, int *err,
       }
     }
     if (L > Lmax) break;
+    if (threadIdx.x == 0) s_grab[(L + 2) % 3] = 0; /* as in wgm_cta_lonestar */
     if (rank == 0 && threadIdx.x == 0) {
       lw[((L + 2) % 3) * (WGM_LINE / 2)] = 0ull;
       /* every member read the drained list's count before the last barrier */
@@ -830,7 +849,15 @@ __device__ int wgm_team_ls_run(const wgm_ls_job &J, wgm_warp_smem *sm, int *err,
     /* pieces per warp: 32, or fewer when the list is short, so a small
      * frontier spreads over every warp instead of queueing on a few */
     const int per = max(1, min(32, (m + NW - 1) / NW));
-    for (int b = gw * per; b < m; b += NW * per) {
+    /* chunk c of `per` pieces belongs to member c mod G; the member's warps
+     * take its chunks from a shared-memory counter as they finish the last */
+    for (;;) {
+      int t = 0;
+      if (lane == 0) t = atomicAdd(&s_grab[L % 3], 1);
+      t = __shfl_sync(WGM_FULL, t, 0);
+      const long long bc = ((long long)t * G + rank) * per;
+      if (bc >= m) break;
+      const int b = (int)bc;
       int i = b + lane, deg = 0, start = 0, src = 0;
       const bool valid = lane < per && i < m;
       if (valid) {
