@@ -29,8 +29,12 @@
 #include "wgm_graph.cuh"
 
 /* Whether batch BFS jobs read dist[dst] before the atomic (one more
- * dependent load, fewer atomics): no, a BFS claim mostly succeeds.  SSSP
- * jobs always pre-check: on the RMAT graphs most relaxations fail, and the
+ * dependent load, fewer atomics): no.  Most BFS claims fail (one per
+ * reached vertex out of one per edge: 6 % succeed on the batch's RMAT
+ * graphs, 25 % on its grids), yet the CAS alone measured as fast or faster
+ * (7.06-7.12 against 7.08-7.32 ms at 512 x 2 CTAs, 7.8-8.0 against 8.2-8.4
+ * at 256 x 3): the load it would save sits on the same chain.  SSSP jobs
+ * always pre-check: on the RMAT graphs most relaxations fail, and the
  * 64-bit atomics they skip cost more than the load (the batch's RMAT SSSP
  * CTA time fell 12 %, the launch 3.5 %). */
 #ifndef WGM_BATCH_PRECHECK
