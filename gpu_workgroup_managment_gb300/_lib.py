@@ -56,7 +56,7 @@ class WgmServeConfig(C.Structure):
                 ("reduce_groups", C.c_int), ("matmul_groups", C.c_int),
                 ("max_in_flight", C.c_int), ("keep_results", C.c_int),
                 ("threads_per_wg", C.c_int), ("bfs_edges_per_group", C.c_int64),
-                ("frac_int", C.c_double)]
+                ("frac_int", C.c_double), ("persist_max_groups", C.c_int)]
 
 
 class WgmServeStats(C.Structure):

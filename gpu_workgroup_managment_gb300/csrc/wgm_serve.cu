@@ -571,6 +571,8 @@ extern "C" int wgm_serve_run(wgm_serve *s, const wgm_serve_config *cfg, wgm_serv
   A.imat_n = s->imat_n;
   A.err = s->d_err;
   A.reserve = std::max(0, cfg->reserve);
+  A.persist_max = cfg->persist_max_groups > 0 ? cfg->persist_max_groups : lpg_max;
+  A.persist_groups = std::min(A.persist_groups, A.persist_max);
   A.rtimes = s->d_rtimes;
   A.max_requests = s->rtimes_cap;
   const uint64_t run_budget = rt->cfg.run_timeout_ns ? rt->cfg.run_timeout_ns : 120000000000ull;

@@ -131,6 +131,7 @@ struct wgm_serve_args {
   unsigned long long *rtimes; /* per request id: start, end (%globaltimer ns) */
   int max_requests;           /* entries of rtimes */
   int reserve;       /* free groups the fork leaves for requests */
+  int persist_max;   /* most groups the persistent job forks up to */
   unsigned long long idle_ns;
 };
 
@@ -511,7 +512,7 @@ static __device__ int wgm_serve_barrier(const wgm_launch &L, wgm_cta *c, wgm_ste
           slow = ((old >> 16) != 0 || wgm_ld_acquire_gpu(&st->groups_to_kill) > 0) ? 1 : 0;
           if (wgm_ld_acquire_gpu(&sd->pending) == 0) {
             int spare = wgm_ld_acquire_gpu(&st->available_workgroups) - A.reserve;
-            want = min(spare, WGM_SERVE_FORK_MAX);
+            want = min(min(spare, WGM_SERVE_FORK_MAX), A.persist_max - n);
             if (want > 0 && !wgm_try_lock(&st->pool_lock)) want = 0;
           }
         }
@@ -733,6 +734,7 @@ static __device__ bool wgm_serve_scheduler(const wgm_launch &L, const wgm_serve_
      * most once per barrier generation */
     if (lane == 0 && started == seen &&
         wgm_ld_acquire_gpu(&st->k_executing[1][0]) > 0 &&
+        wgm_ld_acquire_gpu(&st->k_executing[1][0]) < A.persist_max &&
         wgm_ld_acquire_gpu(&st->available_workgroups) - A.reserve >= WGM_SERVE_FORK_MIN) {
       const unsigned gen = (unsigned)wgm_ld_acquire_gpu_u64(&sd->gate);
       if (gen != fork_gen) {

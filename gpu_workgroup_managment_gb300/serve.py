@@ -59,10 +59,12 @@ class Serve:
             persist_groups: int = 0, reserve: int = 0, bfs_groups: int = 4,
             reduce_groups: int = 4, matmul_groups: int = 4, max_in_flight: int = 256,
             keep_results: bool = False, threads_per_wg: int = 0,
-            bfs_edges_per_group: int = 0, frac_int: float = 0.0) -> dict:
+            bfs_edges_per_group: int = 0, frac_int: float = 0.0,
+            persist_max_groups: int = 0) -> dict:
         c = WgmServeConfig(rate, duration_s, seed, frac_bfs, frac_reduce, reps, persist_groups,
                            reserve, bfs_groups, reduce_groups, matmul_groups, max_in_flight,
-                           int(keep_results), threads_per_wg, bfs_edges_per_group, frac_int)
+                           int(keep_results), threads_per_wg, bfs_edges_per_group, frac_int,
+                           persist_max_groups)
         st = WgmServeStats()
         rc = lib.wgm_serve_run(self._h, C.byref(c), C.byref(st))
         if rc:

@@ -492,6 +492,8 @@ typedef struct wgm_serve_config {
                                   most bfs_groups */
   double frac_int;     /* share of reduce/matmul requests run as the int32
                           reference variants (needs wgm_serve_set_int_data) */
+  int persist_max_groups; /* most groups the persistent job forks up to (0: no
+                             limit); the rest stay free for requests */
 } wgm_serve_config;
 typedef struct wgm_serve_stats {
   int64_t arrived, completed, waited_for_memory;

@@ -112,6 +112,33 @@ def test_persistent_job_cedes_and_takes_back_groups(data):
             assert g.min() <= st["persist_groups_mean"] <= g.max()
 
 
+def test_persistent_job_capped(data):
+    """persist_max_groups: the resident job starts on and forks up to at most
+    that many groups (the groups-over-time trace never exceeds it), leaving
+    the rest to requests; results stay exact."""
+    gs, vecs, mats = data
+    pg = graphs.rmat(14, 16, seed=13)
+    nv = graphs.seeded_node_values(pg.num_nodes, 7)
+    src = graphs.max_degree_vertex(pg)
+    with Runtime(**FAST) as rt:
+        with PersistentApp(rt, "color", pg, node_values=nv) as ca, \
+                PersistentApp(rt, "lonestar_bfs", pg, source=src) as ba, \
+                Serve(rt, ca, ba, graphs=gs, vecs=vecs, mats=mats, arena_bytes=64 << 20) as sv:
+            cap = max(2, rt.sm_count())
+            st = sv.run(rate=5000, duration_s=5.0, reps=20, seed=4, bfs_groups=8,
+                        reduce_groups=8, matmul_groups=8, persist_max_groups=cap)
+            assert st["persist_reps"] == 20
+            assert st["completed"] == st["arrived"] > 0
+            t, g = sv.groups_trace()
+            assert len(g) > 0 and g.max() <= cap, (g.max(), cap)
+            assert np.array_equal(ca.result(), oracle.color(pg, nv))
+            assert np.array_equal(ba.result(), oracle.lonestar_bfs(pg, src))
+            alone = sv.run(reps=5, persist_max_groups=cap)
+            assert alone["persist_reps"] == 5 and alone["kills"] == 0
+            t, g = sv.groups_trace()
+            assert len(g) == 0 or g.max() <= cap
+
+
 def test_admission_waits_for_memory(data):
     gs, vecs, mats = data
     with Runtime(**FAST) as rt, Serve(rt, graphs=gs, vecs=vecs, mats=mats,
