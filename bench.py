@@ -663,7 +663,7 @@ def main() -> int:
         b.reorder_by_last_run()
         tuned = {"threads": 256, "ctas_per_sm": 0, "piece": 0, "team_edges": 50000}
     else:
-        tuned = b.autotune(reps=2)
+        tuned = b.autotune(reps=3)
     for _ in range(warmup):
         b.launch(True)
     rt.synchronize()
